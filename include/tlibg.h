@@ -1,0 +1,156 @@
+/*
+ * tlibg -- GB300-native (sm_103a) mode-q tensor-times-vector engine, C ABI.
+ *
+ * Computes C = A x_q b for a dense tensor A of runtime order p with extents
+ * na, strides wa and layout permutation pia (one-based, as in tlib).  Every
+ * entry point takes plain pointers and sizes only, so any FFI (ctypes, cgo,
+ * JNI, N-API) can bind it; the C++ drop-in policy lives in tlib/ttv_gpu.h.
+ *
+ * Conventions shared by all entry points
+ *  - a, b, c are DEVICE pointers (except the *_host entry points); na, wa,
+ *    pia, nb, nc, wc, pic are HOST arrays read before the call returns.
+ *  - work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ *    stream) and is asynchronous with respect to the host, except where an
+ *    entry point says otherwise.
+ *  - the return value is a TLIBG_* status; the text of the last failure on
+ *    the calling thread is available from tlibg_last_error().  Invalid calls
+ *    fail with TLIBG_ERR_ARGUMENT and the exact exception text the reference
+ *    throws for the same call, in the same order of checks.
+ *  - C is overwritten (the reference's BLAS path uses beta = 0).
+ *  - the engine never falls back to the CPU: without a usable GB300 the
+ *    compute entry points fail with TLIBG_ERR_CUDA.
+ */
+#ifndef TLIBG_H
+#define TLIBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define TLIBG_OK               0
+#define TLIBG_ERR_ARGUMENT     1  /* invalid call: the reference throws std::runtime_error   */
+#define TLIBG_ERR_UNSUPPORTED  2  /* valid for the reference, outside this engine (see text)  */
+#define TLIBG_ERR_CUDA         3  /* CUDA runtime error or no usable device                   */
+#define TLIBG_ERR_NOMEM        4  /* device scratch could not be allocated                    */
+#define TLIBG_ERR_TIMEOUT      5  /* a bounded device-side wait expired (kernel returned)     */
+
+/* ---- element types ---- */
+#define TLIBG_F32    0   /* A, b, C float                                      */
+#define TLIBG_F64    1   /* A, b, C double                                     */
+#define TLIBG_BF16A  2   /* A bfloat16 (raw 16-bit patterns), b and C float    */
+
+/* ---- accumulation ---- */
+#define TLIBG_ACC_COMPENSATED 0  /* fp32: per-thread Kahan partials (default)  */
+#define TLIBG_ACC_PLAIN       1  /* fp32: plain FMA accumulation               */
+
+/* ---- kernel families chosen by the planner ---- */
+#define TLIBG_KIND_ROW 0   /* q is the fastest layout mode (prefix P == 1): lane-group dot products */
+#define TLIBG_KIND_COL 1   /* q is a middle or outer mode: coalesced column GEMV over the prefix    */
+
+typedef struct tlibg_options {
+    int accumulate;   /* TLIBG_ACC_*                                                      */
+    int kind;         /* -1: planner; else force TLIBG_KIND_* (must match the problem)    */
+    int group;        /* ROW: lanes per output (1..32, power of two); COL: warps along q  */
+                      /*   (1, 2, 4 or 8).  0 = planner                                   */
+    int vec;          /* elements per vector load (1, 2, 4 or 8); 0 = planner             */
+    int split;        /* segments of the contracted mode (two-phase reduce); 0 = planner  */
+    int sync;         /* nonzero: synchronise `stream` and check the device error word    */
+} tlibg_options;
+
+/* Launch configuration the planner picks for a canonical problem. */
+typedef struct tlibg_plan_info {
+    uint64_t P, nq, S;   /* prefix before q in the layout, contracted extent, suffix      */
+    int kind, group, vec, split, accumulate;
+    int grid, block;
+} tlibg_plan_info;
+
+/* ---------------------------------------------------------------------------
+ * Low-level TTV, one per element type.
+ * Replaces: template tlib::ttv::ttv(execution_t, slicing_t, fusion_t, q, p,
+ *   a, na, wa, pia, b, nb, c, nc, wc, pic)  -- include/tlib/ttv.h:54-92,
+ * dispatched there to detail::ttv (tensor_times_vector.h:416-421, 1208-1256).
+ * Same argument meaning, same checks and messages (ttv.h:64-89 and
+ * tensor_times_vector.h:160,164).  The slicing / fusion policies of the
+ * reference are scheduling hints on the CPU; this engine always folds every
+ * free mode into one grid (their `fusion_policy::all`).
+ * ------------------------------------------------------------------------- */
+int tlibg_ttv_f32(size_t q, size_t p,
+                  const float* a, const size_t* na, const size_t* wa, const size_t* pia,
+                  const float* b, const size_t* nb,
+                  float* c, const size_t* nc, const size_t* wc, const size_t* pic,
+                  void* stream);
+
+int tlibg_ttv_f64(size_t q, size_t p,
+                  const double* a, const size_t* na, const size_t* wa, const size_t* pia,
+                  const double* b, const size_t* nb,
+                  double* c, const size_t* nc, const size_t* wc, const size_t* pic,
+                  void* stream);
+
+/* A stored as bfloat16 (halves the bytes streamed from HBM), b and C float,
+ * fp32 accumulation.  No reference counterpart for the storage type; the
+ * call surface is that of ttv.h:54-60 with value_t = float for b and C. */
+int tlibg_ttv_bf16a_f32(size_t q, size_t p,
+                        const uint16_t* a, const size_t* na, const size_t* wa, const size_t* pia,
+                        const float* b, const size_t* nb,
+                        float* c, const size_t* nc, const size_t* wc, const size_t* pic,
+                        void* stream);
+
+/* Generic form of the three above with explicit options (NULL = defaults). */
+int tlibg_ttv_ex(int dtype, size_t q, size_t p,
+                 const void* a, const size_t* na, const size_t* wa, const size_t* pia,
+                 const void* b, const size_t* nb,
+                 void* c, const size_t* nc, const size_t* wc, const size_t* pic,
+                 const tlibg_options* opt, void* stream);
+
+/* Same call with HOST pointers a, b, c, as the reference takes them.  A is
+ * streamed to the device in chunks on copy streams overlapped with the
+ * kernels; C is copied back; the call returns when C is complete on the
+ * host (the reference's synchronous semantics).  Pinned (page-locked) host
+ * buffers give full copy bandwidth; pageable ones work at driver-staged
+ * speed. */
+int tlibg_ttv_host(int dtype, size_t q, size_t p,
+                   const void* a, const size_t* na, const size_t* wa, const size_t* pia,
+                   const void* b, const size_t* nb,
+                   void* c, const size_t* nc, const size_t* wc, const size_t* pic,
+                   const tlibg_options* opt);
+
+/* The plan the engine would use for a call (no device work, no CUDA calls
+ * except the one-time device-property query). */
+int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pia,
+               const tlibg_options* opt, tlibg_plan_info* out);
+
+/* ---------------------------------------------------------------------------
+ * Metadata helpers (host only, no device needed).
+ * Replace: detail::generate_output_shape (shape.h:103-158),
+ * detail::generate_output_layout (layout.h:143-207),
+ * detail::generate_strides (strides.h:31-74),
+ * detail::generate_k_order_layout (layout.h:57-84),
+ * detail::inverse_mode (layout.h:114-138).
+ * Return TLIBG_OK or TLIBG_ERR_ARGUMENT with the reference's message.
+ * ------------------------------------------------------------------------- */
+int tlibg_output_shape(const size_t* na, size_t p, size_t q, size_t* nc);
+int tlibg_output_layout(const size_t* pia, size_t p, size_t q, size_t* pic);
+int tlibg_strides(const size_t* n, const size_t* pi, size_t p, size_t* w);
+int tlibg_k_order_layout(size_t p, size_t k, size_t* pi);
+size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode);
+
+/* ---- diagnostics ---- */
+/* Copies the calling thread's last error text into buf (NUL-terminated,
+ * truncated to len); returns the full text length. */
+size_t tlibg_last_error(char* buf, size_t len);
+/* Reads and clears the device error word set by bounded waits that expired
+ * (synchronises the device).  0 = no device-side error. */
+int tlibg_device_error(void);
+/* Number of kernels this library launched since load (all entry points). */
+uint64_t tlibg_launch_count(void);
+/* Library version string. */
+const char* tlibg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TLIBG_H */

@@ -1,0 +1,211 @@
+"""The C ABI and the host-side logic, without a GPU.
+
+* libttvgpu.so loads and exports every entry point include/tlibg.h declares;
+* invalid calls fail with the reference's exception text, in the reference's
+  order of checks (golden errors.json), before any device work;
+* valid calls without a device fail loudly (no CPU fallback);
+* the metadata helpers reproduce the reference's (golden metadata.json);
+* the planner picks the kernel family the layout calls for;
+* the C++ drop-in header compiles against the reference's own dispatch and in
+  standalone mode, and maps errors to std::runtime_error with the same text;
+* ttvs' contraction order bookkeeping (forward / backward / optimal).
+"""
+import ctypes as C
+import json
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+HEADER = os.path.join(ROOT, "include", "tlibg.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(tlibg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol(engine):
+    lib = engine.library()
+    syms = declared_symbols()
+    assert len(syms) >= 14
+    for s in syms:
+        assert hasattr(lib, s), f"{s} declared in tlibg.h but not exported"
+
+
+def _call(engine, dtype, q, p, na, wa, pia, nb, nc, wc, pic, a=16, b=32, c=48):
+    sizes = engine._sizes
+    keep = [sizes(v) for v in (na, wa, pia, nb, nc, wc, pic)]
+    o = engine._options()
+    return engine.library().tlibg_ttv_ex(dtype, q, p, a, *[engine._p(k) for k in keep[:3]], b,
+                                         engine._p(keep[3]), c,
+                                         *[engine._p(k) for k in keep[4:]], C.byref(o), None)
+
+
+def test_invalid_calls_match_reference_messages(engine):
+    with open(os.path.join(GOLDEN, "errors.json")) as f:
+        cases = json.load(f)
+    for case in cases:
+        x = case["args"]
+        nc = x["nc"] if x["nc"] else []
+        for dt in (engine.F32, engine.F64):
+            st = _call(engine, dt, x["q"], x["p"], x["na"], x["wa"], x["pia"], x["nb"], nc or [0],
+                       x["wc"] or [0], x["pic"] or [0]) if x["p"] != 1 else _order1(engine, dt)
+            if case["status"] == 0:
+                # valid for the reference: without a device the engine refuses loudly
+                assert st in (engine.ERR_CUDA, engine.OK), engine._last_error()
+            else:
+                assert st == engine.ERR_ARGUMENT
+                assert engine._last_error() == case["message"]
+
+
+def _order1(engine, dt):
+    sizes = engine._sizes
+    keep = [sizes([3]), sizes([1]), sizes([1]), sizes([3])]
+    o = engine._options()
+    # C of an order-1 tensor has no modes: nc is an empty range
+    return engine.library().tlibg_ttv_ex(dt, 1, 1, 16, *[engine._p(k) for k in keep[:3]], 32,
+                                         engine._p(keep[3]), 48, engine._p(sizes([1])),
+                                         engine._p(sizes([1])), engine._p(sizes([1])), C.byref(o),
+                                         None)
+
+
+def test_null_pointer_checks(engine):
+    na, wa, pia = [2, 3, 4], [1, 2, 6], [1, 2, 3]
+    E = "Error in tlib::tensor_times_vector: "
+    st = _call(engine, engine.F32, 2, 3, na, wa, pia, [3], [2, 4], [1, 2], [1, 2], a=None)
+    assert st == engine.ERR_ARGUMENT
+    assert engine._last_error() == E + "pointer to input tensor A should not be zero."
+    st = _call(engine, engine.F32, 2, 3, na, wa, pia, [3], [2, 4], [1, 2], [1, 2], c=None)
+    assert engine._last_error() == E + "pointer to output tensor C should not be zero."
+    lib, o = engine.library(), engine._options()
+    st = lib.tlibg_ttv_ex(0, 2, 3, 16, None, engine._p(engine._sizes(wa)),
+                          engine._p(engine._sizes(pia)), 32, engine._p(engine._sizes([3])), 48,
+                          engine._p(engine._sizes([2, 4])), engine._p(engine._sizes([1, 2])),
+                          engine._p(engine._sizes([1, 2])), C.byref(o), None)
+    assert st == engine.ERR_ARGUMENT
+    assert engine._last_error() == E + "pointer to input tensor shape vector na should not be zero."
+
+
+def test_non_dense_strides_are_refused(engine):
+    # valid (monotone) for the reference, but not dense: outside this engine
+    st = _call(engine, engine.F32, 2, 3, [2, 3, 4], [1, 3, 9], [1, 2, 3], [3], [2, 4], [1, 2],
+               [1, 2])
+    assert st == engine.ERR_UNSUPPORTED
+    assert "dense" in engine._last_error()
+
+
+def test_valid_call_without_device_fails_loudly(engine):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    st = _call(engine, engine.F32, 2, 3, [2, 3, 4], [1, 2, 6], [1, 2, 3], [3], [2, 4], [1, 2],
+               [1, 2])
+    assert st == engine.ERR_CUDA
+    with pytest.raises(engine.DeviceError):
+        engine.ttv(2, 3, torch.zeros(24), [2, 3, 4], [1, 2, 6], [1, 2, 3], torch.zeros(3), [3],
+                   torch.zeros(8), [2, 4], [1, 2], [1, 2])
+
+
+def test_metadata_helpers_match_reference(engine):
+    with open(os.path.join(GOLDEN, "metadata.json")) as f:
+        meta = json.load(f)
+    for na, q, nc in meta["output_shape"]:
+        assert engine.output_shape(na, q) == nc
+    for pia, q, pic in meta["output_layout"]:
+        assert engine.output_layout(pia, q) == pic
+    for n, pi, w in meta["strides"]:
+        assert engine.strides(n, pi) == w
+    for p, k, pi in meta["k_order"]:
+        assert engine.k_order_layout(p, k) == pi
+    for pi in ([1, 2, 3], [3, 1, 2], [2, 4, 1, 3]):
+        for m in range(1, len(pi) + 1):
+            assert pi[engine.inverse_mode(pi, m) - 1] == m
+    with pytest.raises(engine.TTVError, match="input shape is not valid"):
+        engine.output_shape([2, 0, 3], 1)
+    with pytest.raises(engine.TTVError, match="input layout is not valid"):
+        engine.output_layout([1, 1, 3], 1)
+    with pytest.raises(engine.TTVError, match="compute_strides"):
+        engine.strides([2, 3], [1, 3])
+
+
+def test_planner_kernel_family(engine):
+    # q fastest in the layout -> row kernel; otherwise the column kernel
+    assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
+    assert engine.plan(3, [64, 32, 16], [3, 2, 1])["kind"] == engine.KIND_ROW
+    assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_COL
+    pl = engine.plan(2, [256, 256, 256], [1, 2, 3])
+    assert (pl["P"], pl["nq"], pl["S"]) == (256, 256, 256)
+    assert pl["vec"] == 4 and pl["accumulate"] == engine.ACC_COMPENSATED
+    # odd prefix: scalar loads; fp64: 2 per 16-byte load; bf16: 8
+    assert engine.plan(2, [25, 25, 25], [1, 2, 3])["vec"] == 1
+    assert engine.plan(2, [256, 256, 256], [1, 2, 3], dtype=engine.F64)["vec"] == 2
+    assert engine.plan(2, [256, 256, 256], [1, 2, 3], dtype=engine.BF16A)["vec"] == 8
+    # long contraction with a thin prefix is split, and segments fit the staged b
+    pl = engine.plan(2, [64, 1 << 22], [1, 2])
+    assert pl["split"] >= (1 << 22) // 4096
+    # forced options are honoured or refused
+    assert engine.plan(2, [256, 256, 256], [1, 2, 3], group=2, split=3)["group"] == 2
+    with pytest.raises(engine.TTVError):
+        engine.plan(1, [256, 256, 256], [1, 2, 3], kind=engine.KIND_COL)
+
+
+def _compile_cpp(tmp_path, standalone):
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ missing")
+    ref_inc = os.environ.get("TTV_REFERENCE_INCLUDE", "/root/reference/include")
+    if not standalone and not os.path.isdir(ref_inc):
+        pytest.skip("reference headers absent")
+    exe = str(tmp_path / ("kat_sa" if standalone else "kat_ref"))
+    cuda_inc = "/usr/local/cuda/include"
+    cmd = [gxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc,
+           os.path.join(ROOT, "tests", "cpp", "ttv_gpu_kat.cpp"), "-o", exe,
+           "-L", os.path.join(ROOT, "ttv_gb300"), "-lttvgpu", "-L/usr/local/cuda/lib64",
+           "-lcudart", "-Wl,-rpath," + os.path.join(ROOT, "ttv_gb300")]
+    if standalone:
+        cmd.insert(2, "-DTLIBG_STANDALONE")
+    else:
+        cmd[3:3] = ["-I", ref_inc, "-fopenmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+@pytest.mark.parametrize("standalone", [False, True])
+def test_cpp_header_dispatch_and_messages(engine, tmp_path, standalone):
+    exe = _compile_cpp(tmp_path, standalone)
+    r = subprocess.run([exe, "validate"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "PASSED" in r.stdout
+
+
+def test_ttvs_contraction_order(engine, monkeypatch):
+    """ttvs' mode bookkeeping against the reference's Python tests
+    (ttvpy/tests/test.py), with the per-step TTV done by einsum on the CPU."""
+    import torch
+
+    def cpu_ttv(q, A, b, **kw):
+        return torch.tensordot(A, b, dims=([q - 1], [0]))
+
+    monkeypatch.setattr(engine, "ttv_array", cpu_ttv)
+    A = torch.arange(3 * 2 * 4 * 5, dtype=torch.float64).reshape(3, 2, 4, 5)
+    for q in range(1, 5):
+        dims = [d for d in range(4) if d != q - 1]
+        B = [torch.arange(A.shape[d], dtype=torch.float64) for d in dims]
+        D = A
+        for d, bj in sorted(zip(dims, B), key=lambda t: -t[0]):
+            D = torch.tensordot(D, bj, dims=([d], [0]))
+        for order in ("forward", "backward", "optimal"):
+            Cq = engine.ttvs(q, A, B, order)
+            assert torch.equal(Cq, D), (q, order)
+    with pytest.raises(ValueError, match="multiplication order"):
+        engine.ttvs(1, A, B, "sideways")
+    with pytest.raises(ValueError, match="number of input vectors"):
+        engine.ttvs(1, A, B[:2])

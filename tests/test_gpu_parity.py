@@ -1,0 +1,366 @@
+"""Parity of the CUDA engine with the oracle (GPU; calls go through the C ABI).
+
+Bars (component-wise error normalised by sum_k |a_ik b_k|, against the
+oracle's double-double truth):
+  fp32 (compensated and plain, n_q <= 2^16)   1e-5
+  fp64                                        1e-13
+  bf16-stored A vs the fp32 A it came from    2e-3   (vs its own bf16 values: 1e-5)
+Integer-valued inputs (the reference's known-answer test, one-hot b) must
+match bit for bit.
+"""
+import itertools
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+TOL = {np.float32: 1e-5, np.float64: 1e-13}
+
+
+def meta(T, na, pia, q):
+    wa = T.strides(na, pia)
+    nc, pic = T.output_shape(na, q), T.output_layout(pia, q)
+    return wa, nc, T.strides(nc, pic), pic
+
+
+def run(T, torch, dev, q, na, pia, a, b, **opts):
+    wa, nc, wc, pic = meta(T, na, pia, q)
+    da = torch.from_numpy(a).to(dev)
+    db = torch.from_numpy(b).to(dev)
+    cdt = torch.float64 if a.dtype == np.float64 else torch.float32
+    dc = torch.full((max(int(np.prod(nc)), 1),), float("nan"), dtype=cdt, device=dev)
+    T.ttv(q, len(na), da, na, wa, pia, db, [na[q - 1]], dc, nc, wc, pic, sync=True, **opts)
+    return dc.cpu().numpy()
+
+
+def check(orc, T, torch, dev, q, na, pia, a, b, tol=None, truth=None, **opts):
+    c = run(T, torch, dev, q, na, pia, a, b, **opts)
+    P, nq, S = orc.canonical(na, pia, q)
+    ref, absn = truth if truth is not None else orc.truth(S, nq, P, a, b)
+    err = orc.rel_error(c, ref, absn)
+    bar = tol if tol is not None else TOL[a.dtype.type]
+    assert err <= bar, f"na={na} pia={pia} q={q} {a.dtype} opts={opts}: err {err:.3e} > {bar}"
+    return c, err
+
+
+@pytest.fixture(scope="module")
+def torch_dev(cuda):
+    import torch
+    return torch, cuda
+
+
+def kat_input(na, wa, pia, q, dtype):
+    p = len(na)
+    a = np.zeros(int(np.prod(na)), dtype=dtype)
+    q1 = pia.index(q)
+    order = [pia[r] - 1 for r in range(p - 1, -1, -1) if r != q1] + [q - 1]
+    offs = np.zeros(1, dtype=np.int64)
+    for m in order:
+        offs = (offs[:, None] + np.arange(na[m]) * wa[m]).ravel()
+    a[offs] = np.arange(1, a.size + 1, dtype=dtype)
+    return a
+
+
+@pytest.mark.parametrize("rank", [2, 3, 4])
+def test_kat_grid(engine, torch_dev, rank):
+    """The reference's known-answer test, every shape / layout / q, exact."""
+    torch, dev = torch_dev
+    T = engine
+    for na in itertools.product([2, 4, 8], repeat=rank):
+        na = list(na)
+        for pia in itertools.permutations(range(1, rank + 1)):
+            pia = list(pia)
+            wa = T.strides(na, pia)
+            for q in range(1, rank + 1):
+                nq = na[q - 1]
+                for dt in (np.float32, np.float64):
+                    a = kat_input(na, wa, pia, q, dt)
+                    b = np.ones(nq, dt)
+                    c = run(T, torch, dev, q, na, pia, a, b)
+                    i = np.arange(1, c.size + 1, dtype=np.float64)
+                    np.testing.assert_array_equal(c.astype(np.float64),
+                                                  (nq * nq * (2 * i - 1) + nq) / 2,
+                                                  err_msg=f"{na} {pia} q={q} {dt}")
+
+
+def test_cpp_kat_through_policy(engine, cuda, tmp_path):
+    """The same KAT through the C++ `execution_policy::gpu` drop-in."""
+    from test_abi import _compile_cpp
+    import subprocess
+    exe = _compile_cpp(tmp_path, standalone=True)
+    r = subprocess.run([exe, "kat"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "PASSED" in r.stdout, r.stdout + r.stderr
+
+
+def test_golden_fixtures(engine, orc, torch_dev):
+    """Outputs of the reference itself (fixtures made from it) on random inputs."""
+    torch, dev = torch_dev
+    data = np.load(os.path.join(GOLDEN, "ttv_random.npz"))
+    index = json.loads(bytes(data["index"]).decode())
+    for n, case in enumerate(index):
+        a, b, want = data[f"a{n}"], data[f"b{n}"], data[f"c{n}"]
+        c, err = check(orc, engine, torch, dev, case["q"], case["na"], case["pia"], a, b)
+        # and close to the reference's own rounding of the same sums
+        P, nq, S = orc.canonical(case["na"], case["pia"], case["q"])
+        _, absn = orc.truth(S, nq, P, a, b)
+        assert np.max(np.abs(c.astype(np.float64) - want) / np.maximum(absn, 1e-300)) <= \
+            2 * TOL[a.dtype.type]
+
+
+def random_case(rng, max_elems=1 << 18, max_p=8):
+    while True:
+        p = int(rng.integers(2, max_p + 1))
+        na = [int(x) for x in rng.integers(1, 40, p)]
+        if np.prod(na) <= max_elems:
+            break
+    pia = [int(x) + 1 for x in rng.permutation(p)]
+    q = int(rng.integers(1, p + 1))
+    return na, pia, q
+
+
+def test_random_shapes(engine, orc, torch_dev):
+    torch, dev = torch_dev
+    rng = np.random.default_rng(2026)
+    for t in range(300):
+        na, pia, q = random_case(rng)
+        dt = (np.float32, np.float64)[t % 2]
+        a = rng.uniform(-1, 1, int(np.prod(na))).astype(dt)
+        b = rng.uniform(-1, 1, na[q - 1]).astype(dt)
+        check(orc, engine, torch, dev, q, na, pia, a, b)
+        if dt == np.float32 and t % 5 == 0:
+            check(orc, engine, torch, dev, q, na, pia, a, b, accumulate=engine.ACC_PLAIN)
+
+
+SHAPES = [
+    ([256, 256, 256], [1, 2, 3], 2),
+    ([256, 256, 256], [1, 2, 3], 1),
+    ([256, 256, 256], [1, 2, 3], 3),
+    ([645, 64, 7], [1, 2, 3], 2),
+    ([25, 25, 25, 25], [4, 3, 2, 1], 3),
+    ([48, 48, 48], [3, 1, 2], 1),
+    ([1024, 4, 4, 4], [1, 2, 3, 4], 3),
+    ([16, 16, 16, 16, 16], [1, 2, 3, 4, 5], 5),
+    ([3, 50000], [1, 2], 2),
+    ([50000, 3], [1, 2], 1),
+    ([1, 1, 4096, 1], [1, 2, 3, 4], 3),
+    ([7, 1, 33], [2, 1, 3], 2),
+]
+
+
+@pytest.mark.parametrize("na,pia,q", SHAPES)
+def test_variant_sweep(engine, orc, torch_dev, na, pia, q):
+    """Every kernel instantiation the planner may pick gives the same answer."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(sum(na) + q)
+    P, nq, S = orc.canonical(na, pia, q)
+    for dt in (np.float32, np.float64):
+        a = rng.uniform(-1, 1, int(np.prod(na))).astype(dt)
+        b = rng.uniform(-1, 1, nq).astype(dt)
+        truth = orc.truth(S, nq, P, a, b)
+        vmax = 16 // np.dtype(dt).itemsize
+        groups = [1, 2, 4, 8, 16, 32] if P == 1 else [1, 2, 4, 8]
+        vecs = [v for v in (1, 2, 4, 8) if v <= vmax and (nq if P == 1 else P) % v == 0]
+        for g in groups:
+            for v in vecs:
+                bmax = 16384 // np.dtype(dt).itemsize   # b elements staged per segment
+                for split in (0, 1, 3, 17):
+                    if P > 1 and 0 < split < -(-nq // bmax):
+                        continue
+                    if split > nq:
+                        continue
+                    check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, group=g,
+                          vec=v, split=split)
+
+
+def test_bf16_stored_a(engine, orc, torch_dev):
+    torch, dev = torch_dev
+    rng = np.random.default_rng(5)
+    for na, pia, q in SHAPES[:8]:
+        a32 = rng.uniform(-1, 1, int(np.prod(na))).astype(np.float32)
+        b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)
+        abf = torch.from_numpy(a32).to(torch.bfloat16)
+        bits = abf.view(torch.int16).numpy().view(np.uint16).copy()
+        wa, nc, wc, pic = meta(engine, na, pia, q)
+        dc = torch.empty(int(np.prod(nc)), dtype=torch.float32, device=dev)
+        engine.ttv(q, len(na), abf.to(dev).view(torch.int16), na, wa, pia,
+                   torch.from_numpy(b).to(dev), [na[q - 1]], dc, nc, wc, pic,
+                   dtype=engine.BF16A, sync=True)
+        c = dc.cpu().numpy()
+        P, nq, S = orc.canonical(na, pia, q)
+        ref32, absn32 = orc.truth(S, nq, P, a32, b)
+        assert orc.rel_error(c, ref32, absn32) <= 2e-3
+        refb, absnb = orc.truth(S, nq, P, bits, b, kind="bf16a")
+        assert orc.rel_error(c, refb, absnb) <= 1e-5
+
+
+def test_misaligned_pointers(engine, orc, torch_dev):
+    """Views that start 1-3 elements into an allocation: narrower loads, same answer."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(9)
+    for na, pia, q in ([64, 64, 64], [1, 2, 3], 2), ([64, 64, 64], [1, 2, 3], 1), \
+            ([100, 300], [1, 2], 2):
+        wa, nc, wc, pic = meta(engine, na, pia, q)
+        N, M = int(np.prod(na)), int(np.prod(nc))
+        a = rng.uniform(-1, 1, N + 3).astype(np.float32)
+        b = rng.uniform(-1, 1, na[q - 1] + 3).astype(np.float32)
+        da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+        dc = torch.zeros(M + 3, dtype=torch.float32, device=dev)
+        P, nq, S = orc.canonical(na, pia, q)
+        for oa, ob, oc in ((1, 0, 0), (0, 1, 0), (0, 0, 1), (3, 2, 1)):
+            engine.ttv(q, len(na), da[oa:oa + N], na, wa, pia, db[ob:ob + nq], [nq],
+                       dc[oc:oc + M], nc, wc, pic, sync=True)
+            ref, absn = orc.truth(S, nq, P, a[oa:oa + N], b[ob:ob + nq])
+            assert orc.rel_error(dc[oc:oc + M].cpu().numpy(), ref, absn) <= 1e-5
+
+
+def test_unit_extents_and_degenerate(engine, orc, torch_dev):
+    torch, dev = torch_dev
+    rng = np.random.default_rng(1)
+    cases = [([1, 5], [1, 2], 1), ([5, 1], [1, 2], 2), ([1, 1], [1, 2], 1), ([1, 1, 1], [3, 2, 1], 2),
+             ([1, 300000], [1, 2], 2), ([300000, 1], [2, 1], 1), ([2, 1, 2], [1, 2, 3], 2),
+             ([1, 7, 1, 3], [2, 4, 1, 3], 4), ([9, 1, 11, 1, 2], [5, 1, 3, 2, 4], 1)]
+    for na, pia, q in cases:
+        for dt in (np.float32, np.float64):
+            a = rng.uniform(-1, 1, int(np.prod(na))).astype(dt)
+            b = rng.uniform(-1, 1, na[q - 1]).astype(dt)
+            check(orc, engine, torch, dev, q, na, pia, a, b)
+
+
+def test_long_contraction_precision(engine, orc, torch_dev):
+    """Precision configuration: 64 x 2^22 and 16 x 2^20 x 16, contraction over
+    the long mode, A = N(0,1) * 10^U(-3,3), b = U[-1,1]."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(77)
+    for na, pia, q in (([64, 1 << 22], [1, 2], 2), ([16, 1 << 20, 16], [1, 2, 3], 2)):
+        N = int(np.prod(na))
+        a = (rng.standard_normal(N) * 10.0 ** rng.uniform(-3, 3, N)).astype(np.float32)
+        b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)
+        P, nq, S = orc.canonical(na, pia, q)
+        truth = orc.truth(S, nq, P, a, b)
+        c, err = check(orc, engine, torch, dev, q, na, pia, a, b, tol=1e-5, truth=truth)
+        cp, errp = check(orc, engine, torch, dev, q, na, pia, a, b, tol=1e-3, truth=truth,
+                         accumulate=engine.ACC_PLAIN)
+        assert err <= errp * 1.01 + 1e-9   # compensation never worse than plain
+
+
+def test_full_size_properties(engine, torch_dev):
+    """Symmetric sweep sizes (2^28 elements): size-independent properties.
+    b = e_k picks one slice exactly; linearity in b; checksum of checksums."""
+    torch, dev = torch_dev
+    g = torch.Generator(device=dev)
+    g.manual_seed(123)
+    for p in (2, 3, 4):
+        n = int(np.floor(2 ** (28 / p) + 1e-9))
+        na = [n] * p
+        A = torch.rand(n ** p, generator=g, device=dev, dtype=torch.float32) * 2 - 1
+        for pia in (list(range(1, p + 1)), list(range(p, 0, -1))):
+            for q in (1, (p + 1) // 2, p):
+                wa, nc, wc, pic = meta(engine, na, pia, q)
+                M = n ** (p - 1)
+                C = torch.empty(M, dtype=torch.float32, device=dev)
+                # one-hot b: C is the slice k of A along q, bit for bit
+                k = n // 3
+                b = torch.zeros(n, dtype=torch.float32, device=dev)
+                b[k] = 1.0
+                engine.ttv(q, p, A, na, wa, pia, b, [n], C, nc, wc, pic, sync=True)
+                # the slice, addressed through A's layout: view A with mode strides
+                At = torch.as_strided(A, na, wa)
+                slice_ = At.select(q - 1, k)
+                # C's dense layout pic over the remaining modes
+                Ct = torch.as_strided(C, nc, wc)
+                assert torch.equal(Ct, slice_), (p, pia, q)
+                # linearity
+                b1 = torch.rand(n, generator=g, device=dev) * 2 - 1
+                b2 = torch.rand(n, generator=g, device=dev) * 2 - 1
+                C1, C2, C12 = (torch.empty_like(C) for _ in range(3))
+                for bb, cc in ((b1, C1), (b2, C2), (b1 + b2, C12)):
+                    engine.ttv(q, p, A, na, wa, pia, bb, [n], cc, nc, wc, pic, sync=True)
+                # each result is within 1e-5 * sum|a b| <= 1e-5 * 2n of exact
+                assert float((C12.double() - C1.double() - C2.double()).abs().max()) <= 4e-5 * n
+                # checksum of checksums: sum_j C = sum_i b_i * (sum of slice i)
+                slice_sums = At.double().sum(dim=[d for d in range(p) if d != q - 1])
+                want = float((slice_sums * b1.double()).sum())
+                got = float(C1.double().sum())
+                assert abs(got - want) <= 1e-5 * float(At.double().abs().sum()), (got, want)
+        del A
+        torch.cuda.empty_cache()
+
+
+def test_host_buffers(engine, orc, torch_dev):
+    """The host-pointer entry point (the reference's own calling convention)."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(4)
+    for na, pia, q in (([200, 300, 50], [1, 2, 3], 2), ([128, 64, 300], [3, 1, 2], 3),
+                       ([4096, 4096], [1, 2], 2)):
+        wa, nc, wc, pic = meta(engine, na, pia, q)
+        a = rng.uniform(-1, 1, int(np.prod(na))).astype(np.float32)
+        b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)
+        P, nq, S = orc.canonical(na, pia, q)
+        ref, absn = orc.truth(S, nq, P, a, b)
+        # pageable numpy buffers
+        c = np.zeros(int(np.prod(nc)), np.float32)
+        engine.ttv_host(q, len(na), a, na, wa, pia, b, [nq], c, nc, wc, pic)
+        assert orc.rel_error(c, ref, absn) <= 1e-5
+        # pinned torch buffers
+        ta = torch.from_numpy(a).pin_memory()
+        tb = torch.from_numpy(b).pin_memory()
+        tc = torch.zeros(int(np.prod(nc)), dtype=torch.float32).pin_memory()
+        engine.ttv_host(q, len(na), ta, na, wa, pia, tb, [nq], tc, nc, wc, pic)
+        assert orc.rel_error(tc.numpy(), ref, absn) <= 1e-5
+
+
+def test_array_api_matches_einsum(engine, torch_dev):
+    """ttvpy's tests (ttvpy/tests/test.py), restated on device tensors."""
+    torch, dev = torch_dev
+    A = torch.arange(3 * 2 * 4, dtype=torch.float64).reshape(3, 2, 4)
+    for q, spec in ((1, "ijk,i->jk"), (2, "ijk,j->ik"), (3, "ijk,k->ij")):
+        b = torch.arange(A.shape[q - 1], dtype=torch.float64)
+        D = torch.einsum(spec, A, b)
+        C_ = engine.ttv_array(q, A.to(dev), b.to(dev))
+        assert torch.equal(C_.cpu(), D)
+    for shape in ((3, 2, 4, 5), (5, 5, 5, 5)):
+        A = torch.arange(int(np.prod(shape)), dtype=torch.float64).reshape(*shape)
+        for q in range(1, 5):
+            dims = [d for d in range(4) if d != q - 1]
+            B = [torch.arange(A.shape[d], dtype=torch.float64) for d in dims]
+            D = A
+            for d, bj in sorted(zip(dims, B), key=lambda t: -t[0]):
+                D = torch.tensordot(D, bj, dims=([d], [0]))
+            for order in ("forward", "backward", "optimal"):
+                C_ = engine.ttvs(q, A.to(dev), [bj.to(dev) for bj in B], order)
+                assert torch.equal(C_.cpu(), D), (shape, q, order)
+
+
+def test_determinism_and_streams(engine, torch_dev):
+    torch, dev = torch_dev
+    na, pia, q = [64, 1 << 20], [1, 2], 2
+    wa, nc, wc, pic = meta(engine, na, pia, q)
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    A = torch.rand(int(np.prod(na)), generator=g, device=dev)
+    b = torch.rand(na[q - 1], generator=g, device=dev)
+    outs = []
+    s = torch.cuda.Stream()
+    for i in range(3):
+        c = torch.empty(64, device=dev)
+        with torch.cuda.stream(s):
+            engine.ttv(q, 2, A, na, wa, pia, b, [na[1]], c, nc, wc, pic)
+        s.synchronize()
+        outs.append(c.cpu())
+    assert all(torch.equal(outs[0], o) for o in outs[1:])
+    assert engine.device_error() == 0
+
+
+def test_launch_counter(engine, torch_dev):
+    torch, dev = torch_dev
+    before = engine.launch_count()
+    na, pia, q = [32, 32], [1, 2], 2
+    wa, nc, wc, pic = meta(engine, na, pia, q)
+    engine.ttv(q, 2, torch.ones(1024, device=dev), na, wa, pia, torch.ones(32, device=dev), [32],
+               torch.empty(32, device=dev), nc, wc, pic, sync=True)
+    assert engine.launch_count() > before

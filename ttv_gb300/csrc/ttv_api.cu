@@ -1,0 +1,754 @@
+// C ABI of the GB300 TTV engine: argument validation with the reference's
+// exact messages, the canonical-view planner, device scratch, dispatch and
+// the host-buffer path.  Declarations: include/tlibg.h.
+#include "../../include/tlibg.h"
+#include "ttv_kernels.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace tlibg;
+
+namespace {
+
+thread_local std::string t_last_error;
+std::atomic<uint64_t> g_launches{0};
+
+int fail(int code, const std::string& msg)
+{
+    t_last_error = msg;
+    return code;
+}
+
+int ok()
+{
+    t_last_error.clear();
+    return TLIBG_OK;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+    std::string m = "tlibg: CUDA error in ";
+    m += where;
+    m += ": ";
+    m += cudaGetErrorString(e);
+    cudaGetLastError();   // clear a non-sticky error
+    return fail(TLIBG_ERR_CUDA, m);
+}
+
+// --------------------------------------------------------------------------
+// metadata predicates (shape.h, layout.h, strides.h of the reference)
+// --------------------------------------------------------------------------
+bool valid_shape(const size_t* n, size_t len)
+{
+    if (len == 0) return false;
+    for (size_t r = 0; r < len; ++r)
+        if (n[r] == 0) return false;
+    return true;
+}
+
+bool valid_layout(const size_t* pi, size_t len)
+{
+    if (len == 0) return false;
+    // a permutation of 1..len: every value in range and seen once
+    std::vector<char> seen(len + 1, 0);
+    for (size_t r = 0; r < len; ++r) {
+        if (pi[r] == 0 || pi[r] > len || seen[pi[r]]) return false;
+        seen[pi[r]] = 1;
+    }
+    return true;
+}
+
+// strides must not decrease along the layout (strides.h:76-101)
+bool valid_strides(const size_t* pi, size_t len, const size_t* w)
+{
+    if (len == 1 && w[0] == 1) return true;
+    for (size_t r = 0; r + 1 < len; ++r)
+        if (w[pi[r] - 1] > w[pi[r + 1] - 1]) return false;
+    return true;
+}
+
+bool shape_is_scalar(const size_t* n, size_t len)
+{
+    for (size_t r = 0; r < len; ++r)
+        if (n[r] != 1) return false;
+    return true;
+}
+
+bool shape_is_vector(const size_t* n, size_t len)
+{
+    if (len == 1) return n[0] > 1;
+    bool gt = n[0] > 1 || n[1] > 1, eq = n[0] == 1 || n[1] == 1;
+    for (size_t r = 2; r < len; ++r)
+        if (n[r] != 1) return false;
+    return gt && eq;
+}
+
+// dense strides of (n, pi), with the reference's convention that vectors and
+// scalars get all-ones strides (strides.h:31-57)
+void dense_strides(const size_t* n, const size_t* pi, size_t p, size_t* w)
+{
+    for (size_t r = 0; r < p; ++r) w[r] = 1;
+    if (shape_is_vector(n, p) || shape_is_scalar(n, p)) return;
+    for (size_t r = 1; r < p; ++r) w[pi[r] - 1] = w[pi[r - 1] - 1] * n[pi[r - 1] - 1];
+}
+
+const char* const MSG[] = {
+    "",
+    "Error in tlib::tensor_times_vector: input tensor order should be greater zero.",
+    "Error in tlib::tensor_times_vector: contraction mode should be greater zero or less than or equal to p.",
+    "Error in tlib::tensor_times_vector: pointer to input tensor A should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to input vector B should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to output tensor C should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to input tensor shape vector na should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to input vector shape vector nb should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to output tensor shape vector nc should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to input tensor stride vector wa should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to output tensor stride vector wc should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to input tensor permutation vector pia should not be zero.",
+    "Error in tlib::tensor_times_vector: pointer to output tensor permutation vector pic should not be zero.",
+    "Error in tlib::tensor_times_vector: contraction dimension of A and B are not equal.",
+    "Error in tlib::tensor_times_vector: shape vector of A is not valid.",
+    "Error in tlib::tensor_times_vector: shape vector of C is not valid.",
+    "Error in tlib::tensor_times_vector: layout vector of A is not valid.",
+    "Error in tlib::tensor_times_vector: layout vector of C is not valid.",
+    "Error in tlib::tensor_times_vector: stride vector of A is not valid.",
+    "Error in tlib::tensor_times_vector: stride vector of C is not valid.",
+    "Error in tlib::detail::compute_inverse_pia_m: beginning of layout tuples of both tensors are not correct.",
+    "Error in tlib::detail::compute_inverse_pia_m: end of layout tuples of both tensors are not correct.",
+};
+
+// The reference's checks in its order (ttv.h:64-89).
+int check_call(size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+               const size_t* pia, const void* b, const size_t* nb, const void* c, const size_t* nc,
+               const size_t* wc, const size_t* pic)
+{
+    if (p == 0) return 1;
+    if (q == 0 || q > p) return 2;
+    if (!a) return 3;
+    if (!b) return 4;
+    if (!c) return 5;
+    if (!na) return 6;
+    if (!nb) return 7;
+    if (!nc) return 8;
+    if (!wa) return 9;
+    if (!wc) return 10;
+    if (!pia) return 11;
+    if (!pic) return 12;
+    if (na[q - 1] != nb[0]) return 13;
+    if (!valid_shape(na, p)) return 14;
+    if (!valid_shape(nc, p - 1)) return 15;
+    if (!valid_layout(pia, p)) return 16;
+    if (!valid_layout(pic, p - 1)) return 17;
+    if (!valid_strides(pia, p, wa)) return 18;
+    if (!valid_strides(pic, p - 1, wc)) return 19;
+    return 0;
+}
+
+// pic must be the layout that pia induces once mode q is removed
+// (tensor_times_vector.h:147-168); only the reference's case 8 checks it.
+int check_pic(const size_t* pia, const size_t* pic, size_t p, size_t q)
+{
+    size_t k = 0;
+    while (k < p && pia[k] != q) ++k;
+    for (size_t i = 0; i < k; ++i)
+        if ((pia[i] > q && pic[i] + 1 != pia[i]) || (pia[i] < q && pic[i] != pia[i])) return 20;
+    for (size_t i = k; i + 1 < p; ++i)
+        if ((pia[i + 1] > q && pic[i] + 1 != pia[i + 1]) || (pia[i + 1] < q && pic[i] != pia[i + 1])) return 21;
+    return 0;
+}
+
+bool mul_overflows(uint64_t x, uint64_t y, uint64_t* r)
+{
+    if (x != 0 && y > (uint64_t(1) << 62) / x) return true;
+    *r = x * y;
+    return false;
+}
+
+struct Canon {
+    uint64_t P = 1, nq = 1, S = 1;
+    int ref_case = 0;
+};
+
+// Validate a call and reduce it to the canonical (S, nq, P) view.
+int analyse(size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+            const size_t* pia, const void* b, const size_t* nb, const void* c, const size_t* nc,
+            const size_t* wc, const size_t* pic, Canon* out)
+{
+    const int code = check_call(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic);
+    if (code) return fail(TLIBG_ERR_ARGUMENT, MSG[code]);
+
+    // reference case (cases.h:24-36); p == 1 never reaches here (C's shape is empty)
+    int kase;
+    if (p == 2)
+        kase = (q == 1) ? (pia[0] == 1 ? 2 : 4) : (pia[0] == 1 ? 3 : 5);
+    else if (pia[0] == q)
+        kase = 6;
+    else if (pia[p - 1] == q)
+        kase = 7;
+    else
+        kase = 8;
+    if (kase == 8) {
+        const int pc = check_pic(pia, pic, p, q);
+        if (pc) return fail(TLIBG_ERR_ARGUMENT, MSG[pc]);
+    }
+
+    Canon cn;
+    cn.ref_case = kase;
+    size_t k = 0;
+    while (pia[k] != q) ++k;
+    uint64_t total = 1;
+    for (size_t r = 0; r < p; ++r)
+        if (mul_overflows(total, na[r], &total))
+            return fail(TLIBG_ERR_UNSUPPORTED, "tlibg: the number of elements of A exceeds 2^62");
+    for (size_t r = 0; r < k; ++r) cn.P *= na[pia[r] - 1];
+    for (size_t r = k + 1; r < p; ++r) cn.S *= na[pia[r] - 1];
+    cn.nq = na[q - 1];
+
+    // A must be dense in its layout: every mode with extent > 1 carries the
+    // stride the reference's generate_strides gives it.
+    std::vector<size_t> w(p), running(p);
+    {
+        size_t acc = 1;
+        for (size_t r = 0; r < p; ++r) {
+            running[pia[r] - 1] = acc;
+            acc *= na[pia[r] - 1];
+        }
+        for (size_t r = 0; r < p; ++r)
+            if (na[r] > 1 && wa[r] != running[r])
+                return fail(TLIBG_ERR_UNSUPPORTED,
+                            "tlibg: the gpu policy requires a dense tensor A: stride vector wa does "
+                            "not match the shape and layout (as generate_strides makes them)");
+    }
+    // In case 8 the reference addresses C through wc: it must be dense too.
+    // (Cases 2-7 write C in canonical order and ignore nc, wc and pic.)
+    if (kase == 8) {
+        std::vector<size_t> ncx;
+        for (size_t r = 0; r < p; ++r)
+            if (r != q - 1) ncx.push_back(na[r]);
+        size_t acc = 1;
+        std::vector<size_t> run(p - 1);
+        for (size_t r = 0; r + 1 < p; ++r) {
+            run[pic[r] - 1] = acc;
+            acc *= ncx[pic[r] - 1];
+        }
+        for (size_t r = 0; r + 1 < p; ++r)
+            if (ncx[r] > 1 && wc[r] != run[r])
+                return fail(TLIBG_ERR_UNSUPPORTED,
+                            "tlibg: the gpu policy requires a dense tensor C: stride vector wc does "
+                            "not match the output shape and layout");
+    }
+    *out = cn;
+    return TLIBG_OK;
+}
+
+// --------------------------------------------------------------------------
+// device properties
+// --------------------------------------------------------------------------
+struct DevInfo {
+    int sms = 0;
+    bool ok = false;
+};
+
+DevInfo dev_info()
+{
+    static std::mutex mu;
+    static std::map<int, DevInfo> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return DevInfo{};
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    DevInfo d;
+    if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess) d.ok = true;
+    else cudaGetLastError();
+    cache[dev] = d;
+    return d;
+}
+
+// --------------------------------------------------------------------------
+// planner
+// --------------------------------------------------------------------------
+size_t elem_size_a(int dt) { return dt == F64 ? 8 : (dt == BF16A ? 2 : 4); }
+size_t elem_size_t(int dt) { return dt == F64 ? 8 : 4; }
+bool aligned(const void* p, size_t n) { return (reinterpret_cast<uintptr_t>(p) % n) == 0; }
+uint64_t cdiv(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+int pow2_floor(uint64_t x)
+{
+    int r = 1;
+    while ((uint64_t)r * 2 <= x && r < (1 << 30)) r *= 2;
+    return r;
+}
+
+int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
+              int sms, Plan* out)
+{
+    Plan pl;
+    pl.dtype = dtype;
+    pl.P = cn.P;
+    pl.nq = cn.nq;
+    pl.S = cn.S;
+    pl.kahan = (dtype == F64) ? 0 : ((opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1);
+    pl.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
+    if (opt && opt->kind >= 0 && opt->kind != pl.kind)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
+                                        "(row kernel needs prefix P == 1, column kernel P > 1)");
+    const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
+    const int vmax = (int)(16 / ea);
+
+    // vector width: the widest load that keeps every access aligned
+    int V = (opt && opt->vec > 0) ? opt->vec : vmax;
+    if (V > vmax || (V & (V - 1)))
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: vector width must be a power of two up to 16 bytes");
+    auto vec_ok = [&](int v) {
+        if (pl.kind == KIND_ROW)
+            return cn.nq % v == 0 && aligned(a, v * ea) && aligned(b, std::min<size_t>(16, v * et));
+        return cn.P % v == 0 && aligned(a, v * ea);
+    };
+    if (opt && opt->vec > 0) {
+        if (!vec_ok(V)) return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced vector width violates alignment");
+    } else {
+        while (V > 1 && !vec_ok(V)) V /= 2;
+    }
+    pl.vec = V;
+
+    const int force_split = opt ? opt->split : 0;
+    const int force_group = opt ? opt->group : 0;
+    if (pl.kind == KIND_ROW) {
+        const uint64_t nvec = cdiv(cn.nq, V);
+        int G = force_group > 0 ? force_group : std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / 4)));
+        if (G < 1 || G > 32 || (G & (G - 1)))
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: lanes per row must be a power of two in 1..32");
+        pl.group = G;
+        const int cps = std::max(1, plan_ctas_per_sm(pl));
+        const uint64_t slots = (uint64_t)sms * cps * (BLOCK / G);
+        uint64_t nseg = 1;
+        if (force_split > 0) {
+            nseg = (uint64_t)force_split;
+        } else if (cn.S < 2 * slots) {
+            nseg = cdiv(2 * slots, cn.S);
+            const uint64_t min_len = (uint64_t)V * G * 4;
+            nseg = std::min<uint64_t>(nseg, std::max<uint64_t>(1, cn.nq / min_len));
+        }
+        nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
+        uint64_t seg_len = cdiv(cn.nq, nseg);
+        seg_len = cdiv(seg_len, V) * V;
+        nseg = cdiv(cn.nq, seg_len);
+        pl.split = (int)nseg;
+        pl.seg_len = seg_len;
+        pl.items = cn.S * nseg;
+        const uint64_t groups_per_cta = BLOCK / G;
+        pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * cps, cdiv(pl.items, groups_per_cta)));
+        pl.items_per_cta = 0;
+    } else {
+        const uint64_t outputs = cn.S * cn.P;
+        const uint64_t bmax = BSTAGE_BYTES / et;
+        int WI = force_group > 0 ? force_group : 1;
+        if (WI != 1 && WI != 2 && WI != 4 && WI != 8)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: warps along the contracted mode must be 1, 2, 4 or 8");
+        auto tiles_for = [&](int wi) { return cdiv(outputs, (uint64_t)((BLOCK / 32) / wi) * 32 * V); };
+        pl.group = WI;
+        int cps = std::max(1, plan_ctas_per_sm(pl));
+        const uint64_t want = (uint64_t)sms * cps * 8;   // items for good balance of the blocked split
+        if (force_group <= 0) {
+            while (WI < 8 && tiles_for(WI) < want && cn.nq >= (uint64_t)WI * 2 * 4) WI *= 2;
+            pl.group = WI;
+            cps = std::max(1, plan_ctas_per_sm(pl));
+        }
+        const uint64_t tiles = tiles_for(WI);
+        uint64_t nseg = cdiv(cn.nq, bmax);
+        if (force_split > 0) {
+            nseg = std::max<uint64_t>(nseg, (uint64_t)force_split);
+            if ((uint64_t)force_split < cdiv(cn.nq, bmax))
+                return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced split leaves a segment longer than the staged b buffer");
+        } else if (tiles * nseg < want) {
+            const uint64_t min_len = (uint64_t)WI * 4 * 4;
+            nseg = std::max<uint64_t>(nseg, std::min<uint64_t>(cdiv(want, tiles), std::max<uint64_t>(1, cn.nq / min_len)));
+        }
+        nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
+        uint64_t seg_len = cdiv(cn.nq, nseg);
+        nseg = cdiv(cn.nq, seg_len);
+        pl.split = (int)nseg;
+        pl.seg_len = seg_len;
+        pl.items = tiles * nseg;
+        const uint64_t max_grid = (uint64_t)sms * cps;
+        uint64_t grid = std::min<uint64_t>(max_grid, pl.items);
+        pl.items_per_cta = cdiv(pl.items, grid);
+        pl.grid = (int)cdiv(pl.items, pl.items_per_cta);
+    }
+    pl.f64_combine = (dtype != F64) && pl.split > 1 && cn.nq > (uint64_t(1) << 20);
+    pl.smem = plan_smem_bytes(pl);
+    *out = pl;
+    return TLIBG_OK;
+}
+
+// --------------------------------------------------------------------------
+// per-(device, stream) scratch for split partials (grow-only)
+// --------------------------------------------------------------------------
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+std::mutex g_scratch_mu;
+std::map<std::pair<int, uintptr_t>, Scratch> g_scratch;
+
+int get_scratch(cudaStream_t stream, size_t bytes, void** out)
+{
+    if (bytes == 0) {
+        *out = nullptr;
+        return TLIBG_OK;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    Scratch& s = g_scratch[{dev, reinterpret_cast<uintptr_t>(stream)}];
+    if (s.bytes < bytes) {
+        if (s.ptr) {
+            // the previous buffer may still be read by work queued on this stream
+            cudaStreamSynchronize(stream);
+            cudaFree(s.ptr);
+            s.ptr = nullptr;
+            s.bytes = 0;
+        }
+        size_t want = std::max(bytes, (size_t)1 << 20);
+        cudaError_t e = cudaMalloc(&s.ptr, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(TLIBG_ERR_NOMEM, std::string("tlibg: cannot allocate split scratch: ") + cudaGetErrorString(e));
+        }
+        s.bytes = want;
+    }
+    *out = s.ptr;
+    return TLIBG_OK;
+}
+
+int run_device(int dtype, size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+               const size_t* pia, const void* b, const size_t* nb, void* c, const size_t* nc,
+               const size_t* wc, const size_t* pic, const tlibg_options* opt, cudaStream_t stream)
+{
+    Canon cn;
+    int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
+    if (st) return st;
+    DevInfo d = dev_info();
+    if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    Plan pl;
+    st = make_plan(dtype, cn, a, b, opt, d.sms, &pl);
+    if (st) return st;
+    void* part = nullptr;
+    st = get_scratch(stream, partial_bytes(pl), &part);
+    if (st) return st;
+    uint64_t launches = 0;
+    cudaError_t e = launch_plan(pl, a, b, c, part, stream, &launches);
+    g_launches += launches;
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    if (opt && opt->sync) {
+        e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
+        unsigned int derr = read_and_clear_device_error();
+        if (derr) return fail(TLIBG_ERR_TIMEOUT, "tlibg: a bounded device wait expired; results are invalid");
+    }
+    return ok();
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int tlibg_ttv_f32(size_t q, size_t p, const float* a, const size_t* na, const size_t* wa,
+                  const size_t* pia, const float* b, const size_t* nb, float* c, const size_t* nc,
+                  const size_t* wc, const size_t* pic, void* stream)
+{
+    return run_device(F32, q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, nullptr,
+                      static_cast<cudaStream_t>(stream));
+}
+
+int tlibg_ttv_f64(size_t q, size_t p, const double* a, const size_t* na, const size_t* wa,
+                  const size_t* pia, const double* b, const size_t* nb, double* c, const size_t* nc,
+                  const size_t* wc, const size_t* pic, void* stream)
+{
+    return run_device(F64, q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, nullptr,
+                      static_cast<cudaStream_t>(stream));
+}
+
+int tlibg_ttv_bf16a_f32(size_t q, size_t p, const uint16_t* a, const size_t* na, const size_t* wa,
+                        const size_t* pia, const float* b, const size_t* nb, float* c,
+                        const size_t* nc, const size_t* wc, const size_t* pic, void* stream)
+{
+    return run_device(BF16A, q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, nullptr,
+                      static_cast<cudaStream_t>(stream));
+}
+
+int tlibg_ttv_ex(int dtype, size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+                 const size_t* pia, const void* b, const size_t* nb, void* c, const size_t* nc,
+                 const size_t* wc, const size_t* pic, const tlibg_options* opt, void* stream)
+{
+    if (dtype != F32 && dtype != F64 && dtype != BF16A)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: unknown element type");
+    return run_device(dtype, q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, opt,
+                      static_cast<cudaStream_t>(stream));
+}
+
+int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pia,
+               const tlibg_options* opt, tlibg_plan_info* out)
+{
+    if (!out) return fail(TLIBG_ERR_ARGUMENT, "tlibg: plan output is null");
+    if (dtype != F32 && dtype != F64 && dtype != BF16A)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: unknown element type");
+    if (p == 0) return fail(TLIBG_ERR_ARGUMENT, MSG[1]);
+    if (q == 0 || q > p) return fail(TLIBG_ERR_ARGUMENT, MSG[2]);
+    if (!na || !pia) return fail(TLIBG_ERR_ARGUMENT, "tlibg: shape and layout are required");
+    if (!valid_shape(na, p)) return fail(TLIBG_ERR_ARGUMENT, MSG[14]);
+    if (!valid_layout(pia, p)) return fail(TLIBG_ERR_ARGUMENT, MSG[16]);
+    Canon cn;
+    size_t k = 0;
+    while (pia[k] != q) ++k;
+    for (size_t r = 0; r < k; ++r) cn.P *= na[pia[r] - 1];
+    for (size_t r = k + 1; r < p; ++r) cn.S *= na[pia[r] - 1];
+    cn.nq = na[q - 1];
+    DevInfo d = dev_info();
+    const int sms = d.ok ? d.sms : 152;
+    Plan pl;
+    // plan for 256-byte aligned device buffers (what cudaMalloc returns)
+    static const uint4 probe_a[1] = {};
+    int st = make_plan(dtype, cn, probe_a, probe_a, opt, sms, &pl);
+    if (st) return st;
+    out->P = pl.P;
+    out->nq = pl.nq;
+    out->S = pl.S;
+    out->kind = pl.kind;
+    out->group = pl.group;
+    out->vec = pl.vec;
+    out->split = pl.split;
+    out->accumulate = pl.kahan ? TLIBG_ACC_COMPENSATED : TLIBG_ACC_PLAIN;
+    out->grid = pl.grid;
+    out->block = BLOCK;
+    return ok();
+}
+
+// ---------------------------------------------------------------------------
+// host-buffer path: chunked copies overlapped with the kernels
+// ---------------------------------------------------------------------------
+int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+                   const size_t* pia, const void* b, const size_t* nb, void* c, const size_t* nc,
+                   const size_t* wc, const size_t* pic, const tlibg_options* opt)
+{
+    if (dtype != F32 && dtype != F64 && dtype != BF16A)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: unknown element type");
+    Canon cn;
+    int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
+    if (st) return st;
+    DevInfo d = dev_info();
+    if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+
+    const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
+    // chunk along the suffix S (independent panels); one chunk when S == 1
+    const uint64_t panel = cn.nq * cn.P;                     // elements of A per panel
+    const uint64_t chunk_bytes_target = 64ull << 20;
+    uint64_t spc = std::max<uint64_t>(1, chunk_bytes_target / std::max<uint64_t>(1, panel * ea));
+    spc = std::min<uint64_t>(spc, cn.S);
+    const uint64_t nchunks = cdiv(cn.S, spc);
+
+    struct HostCtx {
+        cudaStream_t comp = nullptr, copy = nullptr;
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        cudaEvent_t done[2] = {nullptr, nullptr};
+        void* abuf[2] = {nullptr, nullptr};
+        size_t abytes = 0;
+        void* bbuf = nullptr;
+        size_t bbytes = 0;
+        void* cbuf = nullptr;
+        size_t cbytes = 0;
+    };
+    static std::mutex mu;
+    static std::map<int, HostCtx> ctxs;
+    std::lock_guard<std::mutex> lk(mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    HostCtx& hc = ctxs[dev];
+    cudaError_t e;
+    if (!hc.comp) {
+        if ((e = cudaStreamCreateWithFlags(&hc.comp, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream create");
+        if ((e = cudaStreamCreateWithFlags(&hc.copy, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream create");
+        for (int i = 0; i < 2; ++i) {
+            cudaEventCreateWithFlags(&hc.ev[i], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&hc.done[i], cudaEventDisableTiming);
+        }
+    }
+    const size_t need_a = (size_t)(spc * panel * ea);
+    const size_t need_b = (size_t)(cn.nq * et);
+    const size_t need_c = (size_t)(cn.S * cn.P * et);
+    auto grow = [&](void** p_, size_t* have, size_t need) -> int {
+        if (*have >= need) return TLIBG_OK;
+        if (*p_) cudaFree(*p_);
+        *p_ = nullptr;
+        *have = 0;
+        cudaError_t ee = cudaMalloc(p_, need);
+        if (ee != cudaSuccess) {
+            cudaGetLastError();
+            return fail(TLIBG_ERR_NOMEM, "tlibg: cannot allocate device staging buffers");
+        }
+        *have = need;
+        return TLIBG_OK;
+    };
+    if (hc.abytes < need_a) {
+        cudaStreamSynchronize(hc.comp);
+        for (int i = 0; i < 2; ++i) {
+            if (hc.abuf[i]) cudaFree(hc.abuf[i]);
+            hc.abuf[i] = nullptr;
+        }
+        hc.abytes = 0;
+        for (int i = 0; i < 2; ++i)
+            if (cudaMalloc(&hc.abuf[i], need_a) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(TLIBG_ERR_NOMEM, "tlibg: cannot allocate device staging buffers");
+            }
+        hc.abytes = need_a;
+    }
+    if ((st = grow(&hc.bbuf, &hc.bbytes, need_b))) return st;
+    if ((st = grow(&hc.cbuf, &hc.cbytes, need_c))) return st;
+
+    if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess)
+        return cuda_fail(e, "copy of b");
+    Plan pl_full;
+    uint64_t launches = 0;
+    for (uint64_t k = 0; k < nchunks; ++k) {
+        const int slot = (int)(k & 1);
+        const uint64_t s0 = k * spc;
+        const uint64_t sn = std::min<uint64_t>(spc, cn.S - s0);
+        // the copy into this slot must wait until the kernels that read it are done
+        if (k >= 2) cudaStreamWaitEvent(hc.copy, hc.done[slot], 0);
+        const char* src = static_cast<const char*>(a) + s0 * panel * ea;
+        if ((e = cudaMemcpyAsync(hc.abuf[slot], src, (size_t)(sn * panel * ea), cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess)
+            return cuda_fail(e, "copy of A");
+        cudaEventRecord(hc.ev[slot], hc.copy);
+        cudaStreamWaitEvent(hc.comp, hc.ev[slot], 0);
+        Canon ck = cn;
+        ck.S = sn;
+        Plan pl;
+        if ((st = make_plan(dtype, ck, hc.abuf[slot], hc.bbuf, opt, d.sms, &pl))) return st;
+        void* part = nullptr;
+        if ((st = get_scratch(hc.comp, partial_bytes(pl), &part))) return st;
+        char* cdst = static_cast<char*>(hc.cbuf) + s0 * cn.P * et;
+        e = launch_plan(pl, hc.abuf[slot], hc.bbuf, cdst, part, hc.comp, &launches);
+        if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        cudaEventRecord(hc.done[slot], hc.comp);
+        pl_full = pl;
+    }
+    g_launches += launches;
+    if ((e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
+        return cuda_fail(e, "copy of C");
+    if ((e = cudaStreamSynchronize(hc.comp)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
+    unsigned int derr = read_and_clear_device_error();
+    if (derr) return fail(TLIBG_ERR_TIMEOUT, "tlibg: a bounded device wait expired; results are invalid");
+    (void)pl_full;
+    return ok();
+}
+
+// ---------------------------------------------------------------------------
+// metadata helpers
+// ---------------------------------------------------------------------------
+int tlibg_output_shape(const size_t* na, size_t p, size_t q, size_t* nc)
+{
+    if (!na || !valid_shape(na, p))
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::generate_output_shape(): input shape is not valid.");
+    if (q == 0 || q > p)
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::generate_output_shape(): constraction mode q "
+                                        "should be greater than 0 and less than or equal to the tensor order.");
+    size_t o = 0;
+    for (size_t r = 0; r < p; ++r)
+        if (r != q - 1) nc[o++] = na[r];
+    return ok();
+}
+
+int tlibg_output_layout(const size_t* pia, size_t p, size_t q, size_t* pic)
+{
+    if (!pia || !valid_layout(pia, p))
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::generate_output_layout(): input layout is not valid.");
+    if (q == 0 || q > p)
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::generate_output_layout(): constraction mode q "
+                                        "should be greater than 0 and less than or equal to the tensor order.");
+    size_t o = 0;
+    for (size_t r = 0; r < p; ++r) {
+        if (pia[r] == q) continue;
+        pic[o++] = pia[r] > q ? pia[r] - 1 : pia[r];
+    }
+    return ok();
+}
+
+int tlibg_strides(const size_t* n, const size_t* pi, size_t p, size_t* w)
+{
+    if (!n || !valid_shape(n, p))
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::compute_strides(): input shape is not valid.");
+    if (!pi || !valid_layout(pi, p))
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::compute_strides(): input layout is not valid.");
+    dense_strides(n, pi, p, w);
+    return ok();
+}
+
+int tlibg_k_order_layout(size_t p, size_t k, size_t* pi)
+{
+    if (p == 0)
+        return fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::compute_k_order: range provided by begin and end not correct!");
+    if (k == 0) k = p;
+    const size_t m = std::min(k, p);
+    size_t r = 0;
+    for (size_t v = m; r < m; --v, ++r) pi[r] = v;
+    for (size_t v = m + 1; r < p; ++v, ++r) pi[r] = v;
+    return ok();
+}
+
+size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode)
+{
+    if (!pi || !valid_layout(pi, p)) {
+        fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::inverse_mode(): input layout is not valid.");
+        return 0;
+    }
+    if (mode == 0 || mode > p) {
+        fail(TLIBG_ERR_ARGUMENT, "Error in tlib::detail::inverse_mode(): mode should be one-based and equal "
+                                 "to or less than layout size.");
+        return 0;
+    }
+    for (size_t r = 0; r < p; ++r)
+        if (pi[r] == mode) {
+            ok();
+            return r + 1;
+        }
+    return 0;
+}
+
+size_t tlibg_last_error(char* buf, size_t len)
+{
+    if (buf && len) {
+        size_t n = std::min(len - 1, t_last_error.size());
+        std::memcpy(buf, t_last_error.data(), n);
+        buf[n] = 0;
+    }
+    return t_last_error.size();
+}
+
+int tlibg_device_error(void)
+{
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return (int)read_and_clear_device_error();
+}
+
+uint64_t tlibg_launch_count(void) { return g_launches.load(); }
+
+const char* tlibg_version(void) { return "tlibg 0.1 (sm_103a)"; }
+
+}  // extern "C"

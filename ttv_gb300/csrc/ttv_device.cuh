@@ -1,0 +1,199 @@
+// Device-side building blocks of the TTV kernels (sm_103a).
+//
+//  * vector loads of A in 16/8/4-byte units, streamed with evict-first hints
+//  * fp32 compensated (Kahan) and plain accumulators, pairwise-compensated
+//    combination of partial sums
+//  * 1-D TMA bulk copy global -> shared (cp.async.bulk) completed on an
+//    mbarrier, with a bounded wait that records a device error instead of
+//    spinning forever
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tlibg {
+
+// Device error word bits (each translation unit keeps its own word and
+// passes its address): bit 0 = a bounded mbarrier wait expired.
+constexpr unsigned ERR_WAIT_TIMEOUT = 1u;
+// Upper bound of try_wait polls before a wait gives up (each poll may block
+// for a hardware-defined slice; the bound is far above any legitimate copy).
+constexpr uint32_t WAIT_POLL_LIMIT = 1u << 22;
+
+// --------------------------------------------------------------------------
+// element conversion: A may be float, double or raw bfloat16 bits
+// --------------------------------------------------------------------------
+template <typename TA, typename T> struct Cvt;
+template <> struct Cvt<float, float> {
+    __device__ static float f(float x) { return x; }
+};
+template <> struct Cvt<double, double> {
+    __device__ static double f(double x) { return x; }
+};
+template <> struct Cvt<uint16_t, float> {
+    __device__ static float f(uint16_t x) { return __uint_as_float(((uint32_t)x) << 16); }
+};
+
+// Raw storage unit of V consecutive elements of TA (16, 8, 4 or 2 bytes).
+template <int BYTES> struct RawVec;
+template <> struct RawVec<16> { typedef uint4 type; };
+template <> struct RawVec<8> { typedef uint2 type; };
+template <> struct RawVec<4> { typedef uint32_t type; };
+template <> struct RawVec<2> { typedef uint16_t type; };
+
+// Streaming (read-once) load of V elements of A, converted to T.
+template <typename TA, typename T, int V>
+__device__ __forceinline__ void load_a(const TA* p, T (&out)[V])
+{
+    constexpr int B = (int)sizeof(TA) * V;
+    typedef typename RawVec<B>::type R;
+    R r = __ldcs(reinterpret_cast<const R*>(p));
+    const TA* e = reinterpret_cast<const TA*>(&r);
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[v] = Cvt<TA, T>::f(e[v]);
+}
+template <> __device__ __forceinline__ void load_a<uint16_t, float, 1>(const uint16_t* p, float (&out)[1])
+{
+    unsigned short r;
+    asm volatile("ld.global.cs.u16 %0, [%1];" : "=h"(r) : "l"(p));
+    out[0] = __uint_as_float(((uint32_t)r) << 16);
+}
+
+// --------------------------------------------------------------------------
+// accumulators.  Value represented = s - c (c carries the negated error).
+// --------------------------------------------------------------------------
+template <typename T, bool KAHAN> struct Acc {
+    T s, c;
+    __device__ __forceinline__ void init() { s = T(0); c = T(0); }
+    __device__ __forceinline__ void fma_add(T a, T b)
+    {
+        if (KAHAN) {
+            T y = fma(a, b, -c);     // product minus the running compensation
+            T t = s + y;
+            c = (t - s) - y;         // what was lost adding y to s
+            s = t;
+        } else {
+            s = fma(a, b, s);
+        }
+    }
+    // Combine with another accumulator (order-fixed, compensated).
+    __device__ __forceinline__ void merge(T os, T oc)
+    {
+        if (KAHAN) {
+            T t = s + os;                      // two-sum of the two leading parts
+            T bp = t - s;
+            T e = (s - (t - bp)) + (os - bp);  // exact rounding error of s + os
+            c = (c + oc) - e;
+            s = t;
+        } else {
+            s = s + os;
+        }
+    }
+    __device__ __forceinline__ T value() const { return KAHAN ? (s - c) : s; }
+};
+
+// --------------------------------------------------------------------------
+// mbarrier + 1-D TMA bulk copy
+// --------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// dst and src 16-byte aligned, bytes a positive multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; false (and the device error word set) if the phase never
+// completed within WAIT_POLL_LIMIT polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned int* err)
+{
+    for (uint32_t it = 0; it < WAIT_POLL_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicOr(err, ERR_WAIT_TIMEOUT);
+    return false;
+}
+
+// Stage b[ib, ie) into shared memory so that element e lands at
+//   smem_b[off + (e - ib)],   off = ((uintptr)(b + ib) % 16) / sizeof(T),
+// i.e. shared and global addresses agree modulo 16.  The 16-byte-aligned body
+// moves with one TMA bulk copy issued by thread 0; the ragged head and tail
+// (at most 15 bytes each) are plain loads.  Must be called by the whole CTA;
+// returns false on an expired wait (all threads then leave the kernel).
+template <typename T>
+__device__ __forceinline__ bool stage_b(T* smem_b, const T* b, uint64_t ib, uint64_t ie,
+                                        uint64_t* bar, uint32_t& phase, int* abort_flag,
+                                        unsigned int* err)
+{
+    const uintptr_t g0 = reinterpret_cast<uintptr_t>(b + ib);
+    const uintptr_t g1 = reinterpret_cast<uintptr_t>(b + ie);
+    const uintptr_t body0 = (g0 + 15) & ~uintptr_t(15);
+    uintptr_t body1 = g1 & ~uintptr_t(15);
+    if (body1 < body0) body1 = body0;
+    const uint32_t off = (uint32_t)((g0 & 15) / sizeof(T));
+    const uint32_t body_bytes = (uint32_t)(body1 - body0);
+    const uint64_t head_n = (body0 - g0) / sizeof(T) < (ie - ib) ? (body0 - g0) / sizeof(T) : (ie - ib);
+    const uint64_t body_first = ib + head_n;                     // first element of the body
+    const uint64_t tail_first = body_first + body_bytes / sizeof(T);
+
+    if (threadIdx.x == 0) {
+        fence_proxy_async_smem();   // order earlier generic reads of smem_b before the async write
+        mbar_arrive_expect_tx(bar, body_bytes);
+        if (body_bytes) bulk_g2s(smem_b + off + head_n, b + body_first, body_bytes, bar);
+    }
+    for (uint64_t e = ib + threadIdx.x; e < body_first; e += blockDim.x) smem_b[off + (e - ib)] = __ldg(b + e);
+    for (uint64_t e = tail_first + threadIdx.x; e < ie; e += blockDim.x) smem_b[off + (e - ib)] = __ldg(b + e);
+    if (threadIdx.x == 0) {
+        if (!mbar_wait_bounded(bar, phase, err)) {
+            *abort_flag = 1;
+            // give an in-flight copy a second bounded chance to land before leaving
+            mbar_wait_bounded(bar, phase, err);
+        }
+    }
+    phase ^= 1u;
+    __syncthreads();
+    return *abort_flag == 0;
+}
+
+}  // namespace tlibg

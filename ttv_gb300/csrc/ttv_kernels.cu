@@ -1,0 +1,469 @@
+// TTV kernels for sm_103a.
+//
+// Every layout of a dense tensor reduces to the canonical product
+//     C[s, j] = sum_i A[s, i, j] * b[i],   A (S, nq, P) row-major, C (S, P),
+// where P is the product of the extents laid out before mode q, nq = n_q and
+// S the product of the extents after it (the reference's "subtensor" view,
+// tensor_times_vector.h:1208-1256, with all free modes fused, fusion::all).
+//
+//  row_kernel  (P == 1, q is the fastest mode; the reference's gemv_row /
+//              dot, matrix_times_vector.h:52-91,265-295): a group of G lanes
+//              (1..32) owns one row segment, streams it with 16-byte loads
+//              and reduces with warp shuffles.
+//  col_kernel  (P > 1; the reference's gemv_col over subtensors,
+//              matrix_times_vector.h:109-221): each thread owns V consecutive
+//              outputs of the contiguous prefix, warps are stacked along i
+//              (WI per CTA) and reduced through shared memory; the b segment
+//              of the CTA's work is staged in shared memory by a TMA bulk copy.
+//  combine_kernel: deterministic second phase of the split-n_q reduction,
+//              partials summed in a fixed order (fp64 for long fp32 rows).
+//
+// Both main kernels are HBM-streaming: A is read exactly once with
+// evict-first loads, C written once.
+#include "ttv_device.cuh"
+#include "ttv_kernels.cuh"
+
+#include <mutex>
+#include <unordered_map>
+
+namespace tlibg {
+
+static __device__ unsigned int g_device_error = 0u;
+
+template <typename T> struct Pair {
+    T s, c;
+};
+
+// --------------------------------------------------------------------------
+// vector load of b (V elements of T, aligned), via the read-only path
+// --------------------------------------------------------------------------
+template <typename T, int V>
+__device__ __forceinline__ void load_b(const T* p, T (&out)[V])
+{
+    constexpr int B = (int)sizeof(T) * V;
+    if constexpr (B <= 16) {
+        typedef typename RawVec<B < 4 ? 4 : B>::type R;
+        if constexpr (B >= 4) {
+            R r = __ldg(reinterpret_cast<const R*>(p));
+            const T* e = reinterpret_cast<const T*>(&r);
+#pragma unroll
+            for (int v = 0; v < V; ++v) out[v] = e[v];
+        }
+    } else {
+        // 32 bytes: two 16-byte loads
+        uint4 r0 = __ldg(reinterpret_cast<const uint4*>(p));
+        uint4 r1 = __ldg(reinterpret_cast<const uint4*>(p) + 1);
+        const T* e0 = reinterpret_cast<const T*>(&r0);
+        const T* e1 = reinterpret_cast<const T*>(&r1);
+        constexpr int H = 16 / (int)sizeof(T);
+#pragma unroll
+        for (int v = 0; v < H; ++v) out[v] = e0[v];
+#pragma unroll
+        for (int v = 0; v < H; ++v) out[H + v] = e1[v];
+    }
+}
+
+// --------------------------------------------------------------------------
+// row kernel: P == 1
+// --------------------------------------------------------------------------
+template <typename TA, typename T, int V, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
+{
+    const uint32_t G = k.group;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gl = lane & (G - 1u);
+    const uint32_t gpw = 32u / G;
+    const uint64_t warp_id = (uint64_t(blockIdx.x) * BLOCK + threadIdx.x) >> 5;
+    const uint64_t nwarps = (uint64_t(gridDim.x) * BLOCK) >> 5;
+    const TA* __restrict__ A = static_cast<const TA*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    constexpr int U = 4;
+
+    for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
+        const uint64_t item = wbase + lane / G;
+        const bool valid = item < k.items;
+        Acc<T, KAHAN> acc[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].init();
+        uint64_t row = 0, seg = 0;
+        if (valid) {
+            if (k.nseg == 1) {
+                row = item;
+            } else {
+                row = item / k.nseg;
+                seg = item - row * k.nseg;
+            }
+            const uint64_t ib = seg * k.seg_len;
+            const uint64_t ie = min(k.nq, ib + k.seg_len);
+            const TA* ap = A + row * k.nq + ib;
+            const T* bp = B + ib;
+            const uint64_t n = ie - ib;
+            const uint64_t nv = n / V;
+            uint64_t kv = gl;
+            for (; kv + (U - 1) * G < nv; kv += U * G) {
+                T av[U][V], bv[U][V];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    load_a<TA, T, V>(ap + (kv + u * G) * V, av[u]);
+                    load_b<T, V>(bp + (kv + u * G) * V, bv[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
+            }
+            for (; kv < nv; kv += G) {
+                T av[V], bv[V];
+                load_a<TA, T, V>(ap + kv * V, av);
+                load_b<T, V>(bp + kv * V, bv);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bv[v]);
+            }
+            for (uint64_t e = nv * V + gl; e < n; e += G) {
+                T av[1];
+                load_a<TA, T, 1>(ap + e, av);
+                acc[0].fma_add(av[0], __ldg(bp + e));
+            }
+        }
+#pragma unroll
+        for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
+        for (uint32_t off = G >> 1; off > 0; off >>= 1) {
+            T os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
+            T oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
+            acc[0].merge(os, oc);
+        }
+        if (valid && gl == 0) {
+            if (k.nseg == 1) {
+                static_cast<T*>(k.out)[row] = acc[0].value();
+            } else {
+                Pair<T> pr;
+                pr.s = acc[0].s;
+                pr.c = KAHAN ? acc[0].c : T(0);
+                static_cast<Pair<T>*>(k.partial)[seg * k.S + row] = pr;
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// column kernel: P > 1
+// --------------------------------------------------------------------------
+template <typename TA, typename T, int V, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
+    T* sb = reinterpret_cast<T*>(smem_raw + 16);
+    constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));
+
+    const uint32_t WI = k.group;
+    const uint32_t WO = (BLOCK / 32) / WI;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t wi = warp % WI, wo = warp / WI;
+    const uint64_t TO = uint64_t(WO) * 32u * V;
+    const uint64_t outputs = k.S * k.P;
+    const TA* __restrict__ A = static_cast<const TA*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    constexpr int U = 4;
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    uint32_t phase = 0;
+    uint64_t staged_seg = ~uint64_t(0);
+    uint32_t off = 0;
+    const uint64_t first = uint64_t(blockIdx.x) * k.items_per_cta;
+    const uint64_t last = min(k.items, first + k.items_per_cta);
+
+    for (uint64_t item = first; item < last; ++item) {
+        const uint64_t seg = item / k.ntiles;
+        const uint64_t tile = item - seg * k.ntiles;
+        const uint64_t ib = seg * k.seg_len;
+        const uint64_t ie = min(k.nq, ib + k.seg_len);
+        if (seg != staged_seg) {
+            __syncthreads();   // every reader of the previous segment is done
+            if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
+            staged_seg = seg;
+            off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+        }
+        const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+
+        const uint64_t o0 = tile * TO + (uint64_t(wo) * 32u + lane) * V;
+        const bool valid = o0 < outputs;
+        Acc<T, KAHAN> acc[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].init();
+        if (valid) {
+            const uint64_t s = o0 / k.P;
+            const uint64_t j = o0 - s * k.P;
+            const TA* ap = A + (s * k.nq) * k.P + j;
+            uint64_t i = ib + wi;
+            for (; i + (U - 1) * WI < ie; i += U * WI) {
+                T av[U][V];
+#pragma unroll
+                for (int u = 0; u < U; ++u) load_a<TA, T, V>(ap + (i + u * WI) * k.P, av[u]);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const T bb = bs[i + u * WI];
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
+                }
+            }
+            for (; i < ie; i += WI) {
+                T av[V];
+                load_a<TA, T, V>(ap + i * k.P, av);
+                const T bb = bs[i];
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
+            }
+        }
+        if (WI > 1) {
+            // warps stacked along i hand their partials to warp row wi == 0
+            const uint32_t slot = wo * 32u + lane;
+            if (wi > 0) {
+                T* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    r[2 * v] = acc[v].s;
+                    r[2 * v + 1] = acc[v].c;
+                }
+            }
+            __syncthreads();
+            if (wi == 0) {
+                for (uint32_t w = 1; w < WI; ++w) {
+                    const T* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].merge(r[2 * v], r[2 * v + 1]);
+                }
+            }
+            __syncthreads();
+        }
+        if (wi == 0 && valid) {
+            if (k.nseg == 1) {
+                T* out = static_cast<T*>(k.out) + o0;
+                const bool vec_ok = ((reinterpret_cast<uintptr_t>(out) % (sizeof(T) * V)) == 0) &&
+                                    (sizeof(T) * V <= 16);
+                if (vec_ok && V > 1) {
+                    T vals[V];
+#pragma unroll
+                    for (int v = 0; v < V; ++v) vals[v] = acc[v].value();
+                    if constexpr (sizeof(T) * V == 16) {
+                        *reinterpret_cast<uint4*>(out) = *reinterpret_cast<const uint4*>(vals);
+                    } else if constexpr (sizeof(T) * V == 8) {
+                        *reinterpret_cast<uint2*>(out) = *reinterpret_cast<const uint2*>(vals);
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < V; ++v) out[v] = vals[v];
+                    }
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) out[v] = acc[v].value();
+                }
+            } else {
+                Pair<T>* pp = static_cast<Pair<T>*>(k.partial) + seg * outputs + o0;
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    Pair<T> pr;
+                    pr.s = acc[v].s;
+                    pr.c = KAHAN ? acc[v].c : T(0);
+                    pp[v] = pr;
+                }
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// combine kernel: C[o] = sum over segments of partial[seg][o], fixed order
+// --------------------------------------------------------------------------
+template <typename T, bool KAHAN, bool F64>
+__global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restrict__ part,
+                                                        T* __restrict__ out, uint64_t outputs,
+                                                        uint32_t nseg)
+{
+    for (uint64_t o = uint64_t(blockIdx.x) * BLOCK + threadIdx.x; o < outputs;
+         o += uint64_t(gridDim.x) * BLOCK) {
+        if (F64) {
+            double acc = 0.0;
+            for (uint32_t g = 0; g < nseg; ++g) {
+                const Pair<T> p = part[uint64_t(g) * outputs + o];
+                acc += (double)p.s - (double)p.c;
+            }
+            out[o] = (T)acc;
+        } else {
+            Acc<T, KAHAN> acc;
+            const Pair<T> p0 = part[o];
+            acc.s = p0.s;
+            acc.c = p0.c;
+            for (uint32_t g = 1; g < nseg; ++g) {
+                const Pair<T> p = part[uint64_t(g) * outputs + o];
+                acc.merge(p.s, p.c);
+            }
+            out[o] = acc.value();
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// host side: instantiation tables
+// --------------------------------------------------------------------------
+typedef void (*KernelFn)(KArgs);
+
+template <typename TA, typename T, bool KAHAN>
+static KernelFn pick_main(int kind, int vec)
+{
+    constexpr int VMAX = 16 / (int)sizeof(TA);
+    if (kind == KIND_ROW) {
+        switch (vec) {
+        case 1: return row_kernel<TA, T, 1, KAHAN>;
+        case 2: return row_kernel<TA, T, 2, KAHAN>;
+        case 4: if constexpr (VMAX >= 4) return row_kernel<TA, T, 4, KAHAN>; else return nullptr;
+        case 8: if constexpr (VMAX >= 8) return row_kernel<TA, T, 8, KAHAN>; else return nullptr;
+        }
+    } else {
+        switch (vec) {
+        case 1: return col_kernel<TA, T, 1, KAHAN>;
+        case 2: return col_kernel<TA, T, 2, KAHAN>;
+        case 4: if constexpr (VMAX >= 4) return col_kernel<TA, T, 4, KAHAN>; else return nullptr;
+        case 8: if constexpr (VMAX >= 8) return col_kernel<TA, T, 8, KAHAN>; else return nullptr;
+        }
+    }
+    return nullptr;
+}
+
+static KernelFn main_kernel(const Plan& p)
+{
+    switch (p.dtype) {
+    case F32:
+        return p.kahan ? pick_main<float, float, true>(p.kind, p.vec)
+                       : pick_main<float, float, false>(p.kind, p.vec);
+    case F64:
+        return pick_main<double, double, false>(p.kind, p.vec);
+    case BF16A:
+        return p.kahan ? pick_main<uint16_t, float, true>(p.kind, p.vec)
+                       : pick_main<uint16_t, float, false>(p.kind, p.vec);
+    }
+    return nullptr;
+}
+
+static size_t acc_size(int dtype) { return dtype == F64 ? 8 : 4; }
+
+size_t plan_smem_bytes(const Plan& p)
+{
+    if (p.kind == KIND_ROW) return 0;
+    const size_t es = acc_size(p.dtype);
+    const size_t bcap = BSTAGE_BYTES / es + 16 / es;
+    const size_t WO = (BLOCK / 32) / p.group;
+    const size_t red = p.group > 1 ? (size_t)(p.group - 1) * WO * 32 * 2 * p.vec * es : 0;
+    return 16 + bcap * es + red;
+}
+
+size_t partial_bytes(const Plan& p)
+{
+    if (p.split <= 1) return 0;
+    return (size_t)p.split * p.S * p.P * 2 * acc_size(p.dtype);
+}
+
+int plan_ctas_per_sm(const Plan& p)
+{
+    static std::mutex mu;
+    static std::unordered_map<uint64_t, int> cache;
+    KernelFn fn = main_kernel(p);
+    if (!fn) return 0;
+    const size_t smem = plan_smem_bytes(p);
+    const uint64_t key = (reinterpret_cast<uintptr_t>(fn) << 20) ^ smem;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    int n = 0;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(fn), BLOCK, smem) !=
+        cudaSuccess)
+        n = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = n;
+    return n;
+}
+
+cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c, void* partial,
+                        cudaStream_t stream, uint64_t* launches)
+{
+    KernelFn fn = main_kernel(plan);
+    if (!fn) return cudaErrorInvalidConfiguration;
+    KArgs k;
+    k.a = a;
+    k.b = b;
+    k.out = c;
+    k.partial = partial;
+    k.S = plan.S;
+    k.nq = plan.nq;
+    k.P = plan.P;
+    k.seg_len = plan.seg_len;
+    k.items = plan.items;
+    k.items_per_cta = plan.items_per_cta;
+    k.nseg = (uint32_t)plan.split;
+    k.group = (uint32_t)plan.group;
+    if (plan.kind == KIND_COL) {
+        const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec;
+        k.ntiles = (plan.S * plan.P + TO - 1) / TO;
+    } else {
+        k.ntiles = 0;
+    }
+    const size_t smem = plan_smem_bytes(plan);
+    fn<<<plan.grid, BLOCK, smem, stream>>>(k);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    if (launches) ++*launches;
+    if (plan.split > 1) {
+        const uint64_t outputs = plan.S * plan.P;
+        int g = (int)((outputs + BLOCK - 1) / BLOCK);
+        if (g > 152 * 16) g = 152 * 16;
+        if (g < 1) g = 1;
+        switch (plan.dtype) {
+        case F32:
+        case BF16A:
+            if (plan.f64_combine)
+                combine_kernel<float, true, true><<<g, BLOCK, 0, stream>>>(
+                    static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
+                    (uint32_t)plan.split);
+            else if (plan.kahan)
+                combine_kernel<float, true, false><<<g, BLOCK, 0, stream>>>(
+                    static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
+                    (uint32_t)plan.split);
+            else
+                combine_kernel<float, false, false><<<g, BLOCK, 0, stream>>>(
+                    static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
+                    (uint32_t)plan.split);
+            break;
+        case F64:
+            combine_kernel<double, false, false><<<g, BLOCK, 0, stream>>>(
+                static_cast<const Pair<double>*>(partial), static_cast<double*>(c), outputs,
+                (uint32_t)plan.split);
+            break;
+        }
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        if (launches) ++*launches;
+    }
+    return cudaSuccess;
+}
+
+unsigned int read_and_clear_device_error()
+{
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_device_error, sizeof(v)) != cudaSuccess) return 0xffffffffu;
+    cudaMemcpyToSymbol(g_device_error, &zero, sizeof(zero));
+    return v;
+}
+
+}  // namespace tlibg
