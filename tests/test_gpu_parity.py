@@ -4,7 +4,9 @@ Bars (component-wise error normalised by sum_k |a_ik b_k|, against the
 oracle's double-double truth):
   fp32 (compensated and plain, n_q <= 2^16)   1e-5
   fp64                                        1e-13
-  bf16-stored A vs the fp32 A it came from    2e-3   (vs its own bf16 values: 1e-5)
+  bf16-stored A vs its own bf16 values        1e-5
+  bf16-stored A vs the fp32 A it came from    2e-3 for n_q >= 64 (2^-8 + 1e-5 always:
+                                              bf16 rounds each element by up to 2^-8)
 Integer-valued inputs (the reference's known-answer test, one-hot b) must
 match bit for bit.
 """
@@ -193,7 +195,13 @@ def test_bf16_stored_a(engine, orc, torch_dev):
         c = dc.cpu().numpy()
         P, nq, S = orc.canonical(na, pia, q)
         ref32, absn32 = orc.truth(S, nq, P, a32, b)
-        assert orc.rel_error(c, ref32, absn32) <= 2e-3
+        err32 = orc.rel_error(c, ref32, absn32)
+        # bf16 keeps 8 significant bits: each stored element is within 2^-8 of
+        # the fp32 one, so the storage alone can cost up to 2^-8 of sum|a*b|;
+        # over longer contractions the roundings average out below 2e-3
+        assert err32 <= 2.0 ** -8 + 1e-5
+        if nq >= 64:
+            assert err32 <= 2e-3
         refb, absnb = orc.truth(S, nq, P, bits, b, kind="bf16a")
         assert orc.rel_error(c, refb, absnb) <= 1e-5
 

@@ -34,6 +34,14 @@ template <typename T> struct Pair {
     T s, c;
 };
 
+// Independent loads each thread keeps in flight: 64 bytes per thread whatever
+// the load width, so narrow (misaligned or odd-extent) layouts still cover the
+// HBM latency-bandwidth product.
+template <typename TA, int V> __host__ __device__ constexpr int loads_in_flight()
+{
+    return (int)sizeof(TA) * V >= 16 ? 4 : (64 / ((int)sizeof(TA) * V) > 16 ? 16 : 64 / ((int)sizeof(TA) * V));
+}
+
 // --------------------------------------------------------------------------
 // vector load of b (V elements of T, aligned), via the read-only path
 // --------------------------------------------------------------------------
@@ -77,7 +85,7 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
     const uint64_t nwarps = (uint64_t(gridDim.x) * BLOCK) >> 5;
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
-    constexpr int U = 4;
+    constexpr int U = loads_in_flight<TA, V>();
 
     for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
         const uint64_t item = wbase + lane / G;
@@ -112,6 +120,7 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
 #pragma unroll
                     for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
             }
+#pragma unroll 4
             for (; kv < nv; kv += G) {
                 T av[V], bv[V];
                 load_a<TA, T, V>(ap + kv * V, av);
@@ -166,7 +175,7 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
     const uint64_t outputs = k.S * k.P;
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
-    constexpr int U = 4;
+    constexpr int U = loads_in_flight<TA, V>();
 
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -215,6 +224,7 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
                     for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
                 }
             }
+#pragma unroll 4
             for (; i < ie; i += WI) {
                 T av[V];
                 load_a<TA, T, V>(ap + i * k.P, av);
