@@ -328,6 +328,14 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk.summary(),
     }
 
+    if rank == 0 and args.detail:
+        with open(args.detail, "w") as f:
+            json.dump([{"na": c["na"], "pia": c["pia"], "q": c["q"], "dtype": c["dtype"],
+                        "kernel": kn, "ms": per_case_ms[i],
+                        "GB/s": nb / (per_case_ms[i] / 1e3) / 1e9,
+                        "plan": T.plan(c["q"], c["na"], c["pia"],
+                                       dtype=T.F32 if c["dtype"] == "f32" else T.F64)}
+                       for i, (_f, _a, _k, nb, kn, c) in enumerate(prepared)], f, indent=0)
     if rank == 0:
         out["accuracy"] = accuracy_sample(T, torch, dev, A, Bv, Cv, prepared)
         if not args.no_e2e:
@@ -481,6 +489,16 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
 
 
+def parse_case(spec):
+    """'na=645,645,128 pia=1,2,3 q=2 dtype=f32' -> a one-TTV workload."""
+    kv = dict(x.split("=", 1) for x in spec.split())
+    c = {"na": [int(x) for x in kv["na"].split(",")], "q": int(kv["q"]),
+         "dtype": kv.get("dtype", "f32")}
+    c["pia"] = [int(x) for x in kv["pia"].split(",")] if "pia" in kv else \
+        list(range(1, len(c["na"]) + 1))
+    return c
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,7 +509,15 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--detail", default=None, help="write per-TTV timings and plans (JSON)")
+    ap.add_argument("--case", default=None,
+                    help="one TTV instead of a sweep, e.g. 'na=645,645,128 pia=1,2,3 q=2 "
+                         "dtype=f32' (profiling)")
     args = ap.parse_args()
+    if args.case:
+        case = parse_case(args.case)
+        WORKLOADS["case"] = (lambda: [case], f"single TTV {args.case}")
+        args.workload = "case"
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
     rank = int(os.environ.get("RANK", "0"))
