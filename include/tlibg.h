@@ -138,6 +138,34 @@ int tlibg_strides(const size_t* n, const size_t* pi, size_t p, size_t* w);
 int tlibg_k_order_layout(size_t p, size_t k, size_t* pi);
 size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free fp32 TTV.  No counterpart in the reference.
+ *
+ * For callers that cannot have device memory allocated on their behalf:
+ * frameworks whose caching allocator owns and accounts for every device byte,
+ * memory-budgeted or multi-tenant processes, and latency-critical loops that
+ * cannot absorb the implicit device synchronisation of cudaMalloc/cudaFree.
+ * Same arguments and checks as tlibg_ttv_f32; the caller passes a, b and c.
+ * The split-n_q partial sums live in one fixed array of
+ * TLIBG_NOALLOC_SCRATCH_BYTES compiled into the library, which every device
+ * that loads the library holds until the process exits.  The call never
+ * allocates or frees memory.
+ *  - Problems whose split reduction needs more scratch than the array are
+ *    refused with TLIBG_ERR_UNSUPPORTED and a message giving both sizes.
+ *  - The first call on each device looks up the array's device address (once,
+ *    with that device current); make that first call before any stream
+ *    capture.
+ *  - All calls share the one array: calls that overlap on the GPU (different
+ *    streams, or host threads) race on it and must be serialised by the caller.
+ *    Nothing in it needs to start at zero; each call writes every slot it reads.
+ * ------------------------------------------------------------------------- */
+#define TLIBG_NOALLOC_SCRATCH_BYTES (8u << 20)
+int tlibg_ttv_f32_noalloc(size_t q, size_t p,
+                          const float* a, const size_t* na, const size_t* wa, const size_t* pia,
+                          const float* b, const size_t* nb,
+                          float* c, const size_t* nc, const size_t* wc, const size_t* pic,
+                          void* stream);
+
 /* ---- diagnostics ---- */
 /* Copies the calling thread's last error text into buf (NUL-terminated,
  * truncated to len); returns the full text length. */

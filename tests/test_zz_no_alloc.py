@@ -1,0 +1,118 @@
+"""The allocation-free entry point, tlibg_ttv_f32_noalloc (GPU, through the C ABI).
+
+Some callers cannot let this library allocate device memory: frameworks whose
+caching allocator owns and accounts for every device byte, memory-budgeted or
+multi-tenant processes, and latency-critical loops that cannot absorb the
+implicit device synchronisation of cudaMalloc/cudaFree.  For them the split
+reduction's partial sums live in one fixed array compiled into the library
+(TLIBG_NOALLOC_SCRATCH_BYTES).  Here its results are checked against the
+regular tlibg_ttv_f32 on the same inputs, on two calls in a row with different
+data (stale partial sums of the first call would show in the second), and a
+problem needing more scratch than the array holds must be refused.
+
+The file is named to be collected last, so a run that stops at the first
+failure has already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LIMIT = 8 << 20   # TLIBG_NOALLOC_SCRATCH_BYTES in include/tlibg.h
+
+
+def bind(engine):
+    lib = engine.library()
+    f = lib.tlibg_ttv_f32_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.c_size_t, C.c_size_t, C.c_void_p, engine._psz, engine._psz, engine._psz,
+                  C.c_void_p, engine._psz, C.c_void_p, engine._psz, engine._psz, engine._psz,
+                  C.c_void_p]
+    return lib
+
+
+def call(engine, fn, q, na, pia, A, b, c, stream):
+    wa = engine.strides(na, pia)
+    nc, pic = engine.output_shape(na, q), engine.output_layout(pia, q)
+    wc = engine.strides(nc, pic)
+    keep = [engine._sizes(v) for v in (na, wa, pia, [na[q - 1]], nc, wc, pic)]
+    p = [engine._p(k) for k in keep]
+    return fn(q, len(na), A.data_ptr(), p[0], p[1], p[2], b.data_ptr(), p[3], c.data_ptr(),
+              p[4], p[5], p[6], stream)
+
+
+def split_scratch_bytes(engine, q, na, pia):
+    pl = engine.plan(q, na, pia)
+    return pl["split"] * pl["S"] * pl["P"] * 8 if pl["split"] > 1 else 0
+
+
+CASES = [
+    ([64, 1 << 20], [1, 2], 2),           # thin prefix, long contraction: heavy split
+    ([256, 256, 256], [1, 2, 3], 2),      # the plain CPU configuration's shape
+    ([6, 1 << 20], [2, 1], 2),            # row kernel: q is the fastest mode
+    ([33, 4099, 7], [1, 2, 3], 2),        # odd extents, scalar loads
+]
+
+
+@pytest.mark.parametrize("na,pia,q", CASES)
+def test_noalloc_matches_regular_entry_point(engine, cuda, na, pia, q):
+    import torch
+    lib = bind(engine)
+    assert split_scratch_bytes(engine, q, na, pia) <= LIMIT
+    stream = torch.cuda.current_stream().cuda_stream
+    g = torch.Generator(device=cuda)
+    g.manual_seed(sum(na) + q)
+    N = int(np.prod(na))
+    M = N // na[q - 1]
+    for round_ in range(2):   # two calls in a row, different inputs each time
+        A = torch.rand(N, generator=g, device=cuda) * 2 - 1
+        b = torch.rand(na[q - 1], generator=g, device=cuda) * 2 - 1
+        c_ref = torch.full((M,), float("nan"), device=cuda)
+        c_new = torch.full((M,), float("nan"), device=cuda)
+        assert call(engine, lib.tlibg_ttv_f32, q, na, pia, A, b, c_ref, stream) == 0
+        st = call(engine, lib.tlibg_ttv_f32_noalloc, q, na, pia, A, b, c_new, stream)
+        assert st == 0, engine._last_error()
+        torch.cuda.synchronize()
+        # the tolerance of the parity tests: 1e-5 of sum_k |a_ik b_k| per output
+        pl = engine.plan(q, na, pia)
+        P, nq, S = pl["P"], pl["nq"], pl["S"]
+        absn = torch.einsum("sip,i->sp", A.view(S, nq, P).abs().double(), b.abs().double())
+        err = ((c_new.double() - c_ref.double()).abs().view(S, P) / absn.clamp_min(1e-300)).max()
+        assert not torch.isnan(c_new).any(), f"round {round_}: unwritten outputs"
+        assert float(err) <= 1e-5, f"round {round_}: {float(err):.3e}"
+    assert engine.device_error() == 0
+
+
+def test_noalloc_refuses_oversize_scratch(engine, cuda):
+    import torch
+    lib = bind(engine)
+    # a problem whose split reduction needs more than the fixed array
+    pick = None
+    for P in (1 << 18, 1 << 19, 1 << 20):
+        for nq in (1 << 13, 1 << 14):
+            na, pia, q = [P, nq], [1, 2], 2
+            if split_scratch_bytes(engine, q, na, pia) > LIMIT:
+                pick = (na, pia, q)
+                break
+        if pick:
+            break
+    assert pick is not None
+    na, pia, q = pick
+    A = torch.empty(int(np.prod(na)), device=cuda)   # never read: the call is refused first
+    b = torch.empty(na[1], device=cuda)
+    c = torch.empty(na[0], device=cuda)
+    st = call(engine, lib.tlibg_ttv_f32_noalloc, q, na, pia, A, b, c,
+              torch.cuda.current_stream().cuda_stream)
+    assert st == engine.ERR_UNSUPPORTED
+    msg = engine._last_error()
+    assert "tlibg_ttv_f32_noalloc" in msg and str(LIMIT) in msg
+    # invalid calls get the reference's text, as on the regular entry point
+    keep = [engine._sizes(v) for v in ([4, 5], [1, 4], [1, 2], [7], [4], [1], [1])]
+    p = [engine._p(k) for k in keep]
+    st = lib.tlibg_ttv_f32_noalloc(2, 2, A.data_ptr(), p[0], p[1], p[2], b.data_ptr(), p[3],
+                                   c.data_ptr(), p[4], p[5], p[6], None)
+    assert st == engine.ERR_ARGUMENT
+    assert engine._last_error() == ("Error in tlib::tensor_times_vector: contraction dimension "
+                                    "of A and B are not equal.")

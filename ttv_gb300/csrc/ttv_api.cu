@@ -752,3 +752,79 @@ uint64_t tlibg_launch_count(void) { return g_launches.load(); }
 const char* tlibg_version(void) { return "tlibg 0.1 (sm_103a)"; }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free entry point
+// ============================================================================
+// Some callers cannot let this library allocate device memory: frameworks
+// whose caching allocator owns (and accounts for) every device byte, memory-
+// budgeted or multi-tenant processes, and latency-critical loops where the
+// implicit device synchronisation of cudaMalloc / cudaFree is not acceptable.
+// tlibg_ttv_f32_noalloc serves them: the only device memory it uses besides
+// the caller's a, b and c is the split-reduction scratch below, a fixed array
+// compiled into the library.  Every device that loads the library holds it
+// (TLIBG_NOALLOC_SCRATCH_BYTES) until the process exits.
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[TLIBG_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch, resolved once per device with that
+// device current.  In host code the array's name is only a host-side stand-in
+// for the symbol, never a device address, so kernels get this pointer.
+int noalloc_scratch(void** out)
+{
+    static std::mutex mu;
+    static std::map<int, void*> addr;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = addr.find(dev);
+    if (it != addr.end()) {
+        *out = it->second;
+        return TLIBG_OK;
+    }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr)
+        return cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress");
+    addr[dev] = p;
+    *out = p;
+    return TLIBG_OK;
+}
+
+}  // namespace
+
+extern "C" int tlibg_ttv_f32_noalloc(size_t q, size_t p, const float* a, const size_t* na,
+                                     const size_t* wa, const size_t* pia, const float* b,
+                                     const size_t* nb, float* c, const size_t* nc,
+                                     const size_t* wc, const size_t* pic, void* stream)
+{
+    Canon cn;
+    int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
+    if (st) return st;
+    DevInfo d = dev_info();
+    if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    Plan pl;
+    st = make_plan(F32, cn, a, b, nullptr, d.sms, &pl);
+    if (st) return st;
+    const size_t need = partial_bytes(pl);
+    if (need > (size_t)TLIBG_NOALLOC_SCRATCH_BYTES)
+        return fail(TLIBG_ERR_UNSUPPORTED,
+                    "tlibg_ttv_f32_noalloc: this problem's split reduction needs " + std::to_string(need) +
+                        " bytes of scratch, more than the fixed " +
+                        std::to_string((size_t)TLIBG_NOALLOC_SCRATCH_BYTES) +
+                        "-byte buffer; use tlibg_ttv_f32");
+    void* part = nullptr;
+    if (need) {
+        st = noalloc_scratch(&part);
+        if (st) return st;
+    }
+    // Nothing in the scratch needs to start at zero: the main kernel writes
+    // every partial slot the combine kernel then reads, within this call.
+    uint64_t launches = 0;
+    cudaError_t e = launch_plan(pl, a, b, c, part, static_cast<cudaStream_t>(stream), &launches);
+    g_launches += launches;
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return ok();
+}
