@@ -342,7 +342,69 @@ def run_ours(args, rank, world, local_rank):
             out["e2e"] = run_e2e(T, torch, prepared, A, Bv, dtypes, args)
         if not args.no_cpu and world == 1:
             out["cpu_baseline"] = run_cpu_baseline(prepared, args)
+        if not args.no_batch and args.workload != "case":
+            A.clear()
+            Bv.clear()
+            Cv.clear()
+            torch.cuda.empty_cache()
+            out["batched"] = run_batched(T, torch, dev, args)
     return out
+
+
+def run_batched(T, torch, dev, args, n=4096, seed=4096):
+    """Batched configuration: 4096 uneven fp32 TTVs (orders 3-5, extents log-uniform in
+    [8, 512], <= 2^22 elements each, random q and layout) per launch.  Learned-selected
+    persistent CUDA-graph launch vs the fixed rule vs one plain kernel launch per problem."""
+    from ttv_gb300 import batch as B
+    from ttv_gb300 import costmodel as CM
+    shapes = CM.random_shapes(n, seed)
+    sizes = [int(np.prod(na)) for na, _, _ in shapes]
+    outs = [s // na[q - 1] for s, (na, _, q) in zip(sizes, shapes)]
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    A = torch.rand(sum((s + 63) // 64 * 64 for s in sizes), generator=g, device=dev) * 2 - 1
+    bvec = torch.rand(512, generator=g, device=dev) * 2 - 1
+    C = torch.empty(sum((m + 63) // 64 * 64 for m in outs), device=dev)
+    probs = CM.problems_from_arena([(sh, 1) for sh in shapes], A, bvec, C)
+    nbytes = sum(4 * (s + m) for s, m in zip(sizes, outs))
+    model = B.load_cost_model()   # committed trained weights (installs them), or None
+    res = {"problems": n, "bytes_per_launch": nbytes, "model": "trained" if model is not None
+           else "absent (learned mode falls back to the fixed rule)"}
+    K = max(3, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(K):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
+
+    for name, sel in (("learned", B.SELECT_LEARNED), ("fixed_rule", B.SELECT_HEURISTIC)):
+        with B.Batch(probs, select=sel) as bt:
+            l0 = T.launch_count()
+            ms = timed(bt.launch)
+            res[name] = {"ms": round(ms, 3), "TTVs/s": round(n / ms * 1e3, 1),
+                         "GB/s": round(nbytes / ms / 1e6, 1),
+                         "gpu_launches_per_batch": (T.launch_count() - l0) // (K + 3)}
+    ms = timed(lambda: B.ttv_percall(probs))
+    res["plain_per_call"] = {"ms": round(ms, 3), "TTVs/s": round(n / ms * 1e3, 1),
+                             "GB/s": round(nbytes / ms / 1e6, 1)}
+    res["speedup_learned_vs_plain"] = round(res["plain_per_call"]["ms"] / res["learned"]["ms"], 3)
+    res["speedup_learned_vs_fixed_rule"] = round(res["fixed_rule"]["ms"] / res["learned"]["ms"], 3)
+    # accuracy of the learned launch on a sample of problems
+    import oracle
+    errs = []
+    for pr, (na, pia, q) in list(zip(probs, shapes))[:: max(1, n // 64)]:
+        P, nq, S = canonical({"na": na, "pia": pia, "q": q})
+        ref, absn = oracle.truth(S, nq, P, pr.a_view.cpu().numpy(), pr.b.cpu().numpy())
+        errs.append(oracle.rel_error(pr.c_view.cpu().numpy(), ref, absn))
+    res["max_rel_err_fp32"] = float(max(errs))
+    return res
 
 
 def accuracy_sample(T, torch, dev, A, Bv, Cv, prepared):
@@ -509,6 +571,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--detail", default=None, help="write per-TTV timings and plans (JSON)")
     ap.add_argument("--case", default=None,
                     help="one TTV instead of a sweep, e.g. 'na=645,645,128 pia=1,2,3 q=2 "

@@ -166,6 +166,85 @@ int tlibg_ttv_f32_noalloc(size_t q, size_t p,
                           float* c, const size_t* nc, const size_t* wc, const size_t* pic,
                           void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched TTVs: thousands of independent fp32 problems (uneven order, extents,
+ * q and layout) in one persistent launch fed by a device-side work queue,
+ * captured once in a CUDA graph and replayed.  No reference counterpart (the
+ * reference runs one call at a time); each problem has the argument meaning
+ * of ttv.h:54-60 and is validated like tlibg_ttv_f32.
+ * ------------------------------------------------------------------------- */
+typedef struct tlibg_problem {
+    size_t q, p;
+    const void* a; const size_t* na; const size_t* wa; const size_t* pia;
+    const void* b; const size_t* nb;
+    void* c; const size_t* nc; const size_t* wc; const size_t* pic;
+} tlibg_problem;
+
+#define TLIBG_SELECT_HEURISTIC 0  /* fixed rule of the engine                                 */
+#define TLIBG_SELECT_LEARNED   1  /* cost-model MLP scores every variant on the device         */
+#define TLIBG_SELECT_FIXED     2  /* every problem runs `variant`                              */
+#define TLIBG_SELECT_GIVEN     3  /* per-problem `variants` (e.g. from exhaustive tuning)      */
+#define TLIBG_NVARIANT 8
+
+typedef struct tlibg_batch_options {
+    int select;            /* TLIBG_SELECT_*; LEARNED without a model falls back to GIVEN, then HEURISTIC */
+    int variant;           /* TLIBG_SELECT_FIXED                                              */
+    int accumulate;        /* TLIBG_ACC_*                                                     */
+    int no_graph;          /* nonzero: launch the kernels directly instead of a CUDA graph    */
+    const int* variants;   /* one per problem (TLIBG_SELECT_GIVEN), or NULL                   */
+} tlibg_batch_options;
+
+typedef struct tlibg_batch tlibg_batch;
+
+/* Builds device descriptors (synchronises `stream` once) and, unless no_graph,
+ * instantiates the CUDA graph of one launch.  Problem buffers must stay valid
+ * for the lifetime of the batch. */
+int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count,
+                       const tlibg_batch_options* opt, void* stream, tlibg_batch** out);
+/* Runs every problem of the batch once (asynchronous on `stream`). */
+int tlibg_batch_launch(tlibg_batch* batch, void* stream);
+/* Changes the forced variant of a TLIBG_SELECT_FIXED batch created with
+ * no_graph (the autotuner's loop over variants). */
+int tlibg_batch_set_variant(tlibg_batch* batch, int variant);
+/* The variant each problem ran with in the last launch (synchronises). */
+int tlibg_batch_variants(tlibg_batch* batch, int* out, void* stream);
+int tlibg_batch_destroy(tlibg_batch* batch);
+/* create + launch + destroy (synchronous). */
+int tlibg_ttv_batch(int dtype, const tlibg_problem* probs, size_t count,
+                    const tlibg_batch_options* opt, void* stream);
+/* The plain alternative: one tlibg_ttv_ex launch per problem, in order. */
+int tlibg_ttv_percall(int dtype, const tlibg_problem* probs, size_t count, void* stream);
+/* Cost-model features of each problem (TLIBG_MLP_FEATURES floats per problem),
+ * its kernel family and the fixed rule's variant (kind / heuristic may be NULL). */
+int tlibg_batch_features(const tlibg_problem* probs, size_t count, float* feat, int* kind,
+                         int* heuristic);
+/* Reads and clears the batched executor's device error word. */
+unsigned int tlibg_batch_device_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Learned cost model: an MLP (TLIBG_MLP_IN inputs = features + one-hot
+ * variant, three hidden layers of 64 ReLU units, one output = predicted
+ * log2 cost per problem) trained by the engine's own CUDA kernels.  All
+ * buffers are device pointers unless stated.
+ * ------------------------------------------------------------------------- */
+#define TLIBG_MLP_FEATURES 8
+#define TLIBG_MLP_IN 16
+#define TLIBG_MLP_HIDDEN 64
+#define TLIBG_MLP_PARAMS 9473
+/* loss = (1/n) sum 0.5 (f(x)-y)^2 and its gradient (grad[TLIBG_MLP_PARAMS], loss[1]) */
+int tlibg_mlp_loss_grad(const float* params, const float* x, const float* y, size_t n, float* grad,
+                        float* loss, void* stream);
+/* one Adam step (step counts from 1) */
+int tlibg_mlp_adam(float* params, const float* grad, float* m, float* v, uint64_t step, float lr,
+                   float beta1, float beta2, float eps, void* stream);
+int tlibg_mlp_predict(const float* params, const float* x, size_t n, float* y, void* stream);
+/* minibatch Adam over `epochs` shuffled passes; epoch_loss (HOST, epochs floats) may be NULL */
+int tlibg_mlp_train(float* params, float* m, float* v, const float* x, const float* y, size_t n,
+                    int epochs, int batch, float lr, uint64_t seed, float* epoch_loss, void* stream);
+/* Installs (HOST array of TLIBG_MLP_PARAMS floats) or clears (NULL) the model
+ * TLIBG_SELECT_LEARNED uses for batches created afterwards. */
+int tlibg_set_cost_model(const float* params, size_t count);
+
 /* ---- diagnostics ---- */
 /* Copies the calling thread's last error text into buf (NUL-terminated,
  * truncated to len); returns the full text length. */

@@ -1,0 +1,190 @@
+"""Autotuner, training and evaluation of the learned variant selector.
+
+    python -m ttv_gb300.costmodel --train 20000 --test 2000      (on a GPU)
+
+1. ``random_shapes`` draws batched-TTV problems: order p uniform in {3,4,5},
+   every extent log-uniform in [8, 512] (rounded), re-drawn until the problem
+   has at most 2^22 elements, a random contraction mode and a random layout.
+2. ``tune`` times every kernel variant of each shape exhaustively: K copies
+   of the shape (K x bytes ~ 256 MB, 32 <= K <= 4096) run as one persistent
+   batch with that variant forced, L2 flushed before each timed launch,
+   CUDA-event timed; cost = time / K (microseconds per problem).
+3. ``train`` fits the MLP (features + one-hot variant -> log2 cost) with the
+   engine's own CUDA forward/backward/Adam kernels.
+4. ``evaluate`` measures regret against exhaustive tuning on held-out shapes,
+   for the learned choice and for the engine's fixed rule.
+
+Results go to ttv_gb300/data/: tuning_db.npz (features, times, fixed-rule
+variant, split) and cost_model.npz (parameters, loss curve, regret).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import batch as B
+
+DATA = B.DATA
+DB_PATH = os.path.join(DATA, "tuning_db.npz")
+
+
+def random_shapes(n, seed, max_elems=1 << 22, lo=8, hi=512, orders=(3, 4, 5)):
+    """Shapes of the batched configuration (rejection-resampled to <= max_elems)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        p = int(rng.choice(orders))
+        na = [int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) for _ in range(p)]
+        if int(np.prod(na)) > max_elems:
+            continue
+        q = int(rng.integers(1, p + 1))
+        pia = [int(x) + 1 for x in rng.permutation(p)]
+        out.append((na, pia, q))
+    return out
+
+
+def problems_from_arena(shapes_counts, A, b, C):
+    """Problems laid out back to back in device arenas A (inputs) and C (outputs);
+    every problem shares the vector arena b.  Offsets are 64-element aligned."""
+    import copy
+    probs = []
+    oa = oc = 0
+    a0, c0 = A.data_ptr(), C.data_ptr()
+    for (na, pia, q), k in shapes_counts:
+        N = int(np.prod(na))
+        M = N // na[q - 1]
+        first = B.Problem(q, na, pia, a0 + 4 * oa, b[:na[q - 1]], c0 + 4 * oc)
+        for j in range(k):
+            pr = first if j == 0 else copy.copy(first)   # metadata shared, buffers differ
+            pr.a, pr.c = a0 + 4 * oa, c0 + 4 * oc
+            pr.a_view, pr.c_view = A[oa:oa + N], C[oc:oc + M]
+            probs.append(pr)
+            oa += (N + 63) // 64 * 64
+            oc += (M + 63) // 64 * 64
+    assert oa <= A.numel() and oc <= C.numel()
+    return probs
+
+
+def copies_for(na, target_bytes=256 << 20, lo=32, hi=4096):
+    nbytes = 4 * int(np.prod(na))
+    return int(min(hi, max(lo, -(-target_bytes // nbytes))))
+
+
+def tune(shapes, reps=2, log_every=500, flush_bytes=256 << 20):
+    """Exhaustive timing of every variant of every shape: (features [n, 8], times [n, 8] us
+    per problem, fixed-rule variant [n])."""
+    import torch
+    dev = torch.device("cuda")
+    A = torch.rand(int(1.2 * (1 << 28)) // 4 * 4 + (1 << 22), device=dev) * 2 - 1
+    b = torch.rand(1024, device=dev) * 2 - 1
+    C = torch.empty(64 << 20, device=dev)
+    flush = torch.empty(flush_bytes // 4, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    feats = np.zeros((len(shapes), B.MLP_FEATURES), np.float32)
+    times = np.zeros((len(shapes), B.NVARIANT), np.float32)
+    heur = np.zeros(len(shapes), np.int32)
+    t0 = time.time()
+    for si, (na, pia, q) in enumerate(shapes):
+        k = copies_for(na)
+        probs = problems_from_arena([((na, pia, q), k)], A, b, C)
+        f, _kind, h = B.features(probs)
+        feats[si] = f[0]
+        heur[si] = h[0]
+        with B.Batch(probs, select=B.SELECT_FIXED, variant=0, no_graph=True) as bt:
+            for v in range(B.NVARIANT):
+                bt.set_variant(v)
+                best = float("inf")
+                for r in range(reps + 1):
+                    flush.zero_()
+                    e0.record()
+                    bt.launch()
+                    e1.record()
+                    e1.synchronize()
+                    if r:
+                        best = min(best, e0.elapsed_time(e1))
+                times[si, v] = best * 1e3 / k
+        if log_every and (si + 1) % log_every == 0:
+            print(f"tuned {si + 1}/{len(shapes)} shapes in {time.time() - t0:.0f} s", flush=True)
+    return feats, times, heur
+
+
+def training_set(feats, times):
+    x = B.mlp_inputs(feats)
+    y = np.log2(np.maximum(times, 1e-3)).ravel().astype(np.float32)
+    return x, y
+
+
+def train(feats, times, epochs=60, batch=512, lr=2e-3, seed=0):
+    import torch
+    x, y = training_set(feats, times)
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.from_numpy(y).cuda()
+    params = torch.from_numpy(B.init_params(seed)).cuda()
+    losses = B.mlp_train(params, dx, dy, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    return params.cpu().numpy(), losses
+
+
+def predict_variants(params, feats):
+    import torch
+    x = torch.from_numpy(B.mlp_inputs(feats)).cuda()
+    pred = B.mlp_predict(torch.from_numpy(np.asarray(params, np.float32)).cuda(), x)
+    return pred.cpu().numpy().reshape(len(feats), B.NVARIANT).argmin(axis=1)
+
+
+def regret(times, chosen):
+    """Aggregate time of the chosen variants over exhaustive tuning's best, minus one;
+    and the mean per-shape ratio minus one."""
+    idx = np.arange(len(times))
+    t_sel = times[idx, chosen].astype(np.float64)
+    t_best = times.min(axis=1).astype(np.float64)
+    return float(t_sel.sum() / t_best.sum() - 1.0), float(np.mean(t_sel / t_best) - 1.0)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=20000)
+    ap.add_argument("--test", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--out", default=DATA)
+    ap.add_argument("--reuse-db", action="store_true", help="train on an existing tuning_db.npz")
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    db_path = os.path.join(args.out, "tuning_db.npz")
+    if args.reuse_db and os.path.exists(db_path):
+        d = np.load(db_path)
+        feats, times, heur, split = d["features"], d["times"], d["heuristic"], d["is_test"]
+    else:
+        shapes = random_shapes(args.train + args.test, args.seed)
+        t0 = time.time()
+        feats, times, heur = tune(shapes)
+        print(f"tuning: {time.time() - t0:.1f} s for {len(shapes)} shapes x {B.NVARIANT} variants")
+        split = np.zeros(len(shapes), bool)
+        split[args.train:] = True
+        np.savez_compressed(db_path, features=feats, times=times, heuristic=heur, is_test=split,
+                            shapes=np.frombuffer(json.dumps(shapes).encode(), np.uint8))
+    tr, te = ~split, split
+    t0 = time.time()
+    params, losses = train(feats[tr], times[tr], epochs=args.epochs, seed=args.seed)
+    t_train = time.time() - t0
+    learned = predict_variants(params, feats[te])
+    r_learn = regret(times[te], learned)
+    r_heur = regret(times[te], heur[te])
+    r_fixed = {v: regret(times[te], np.full(te.sum(), v))[0] for v in range(B.NVARIANT)}
+    summary = {"train_shapes": int(tr.sum()), "test_shapes": int(te.sum()),
+               "train_seconds": round(t_train, 2), "final_loss": float(losses[-1]),
+               "regret_learned": r_learn, "regret_fixed_rule": r_heur,
+               "regret_single_variant": r_fixed,
+               "learned_picks_best": float(np.mean(learned == times[te].argmin(axis=1)))}
+    np.savez_compressed(os.path.join(args.out, "cost_model.npz"), params=params, losses=losses,
+                        summary=np.frombuffer(json.dumps(summary).encode(), np.uint8))
+    print(json.dumps(summary))
+
+
+if __name__ == "__main__":
+    main()

@@ -2,6 +2,7 @@
 // exact messages, the canonical-view planner, device scratch, dispatch and
 // the host-buffer path.  Declarations: include/tlibg.h.
 #include "../../include/tlibg.h"
+#include "ttv_internal.h"
 #include "ttv_kernels.cuh"
 
 #include <algorithm>
@@ -828,3 +829,46 @@ extern "C" int tlibg_ttv_f32_noalloc(size_t q, size_t p, const float* a, const s
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return ok();
 }
+
+// ============================================================================
+// internal interface for the other translation units (ttv_internal.h)
+// ============================================================================
+namespace tlibg {
+
+int internal_analyse(size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+                     const size_t* pia, const void* b, const size_t* nb, const void* c,
+                     const size_t* nc, const size_t* wc, const size_t* pic, CanonView* out)
+{
+    Canon cn;
+    const int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
+    if (st) return st;
+    out->P = cn.P;
+    out->nq = cn.nq;
+    out->S = cn.S;
+    out->ref_case = cn.ref_case;
+    return TLIBG_OK;
+}
+
+int internal_plan(int dtype, const CanonView& cv, const void* a, const void* b,
+                  const tlibg_options* opt, int sms, Plan* out)
+{
+    Canon cn;
+    cn.P = cv.P;
+    cn.nq = cv.nq;
+    cn.S = cv.S;
+    cn.ref_case = cv.ref_case;
+    return make_plan(dtype, cn, a, b, opt, sms, out);
+}
+
+int internal_sms()
+{
+    DevInfo d = dev_info();
+    return d.ok ? d.sms : 0;
+}
+
+int internal_fail(int code, const std::string& msg) { return fail(code, msg); }
+int internal_ok() { return ok(); }
+int internal_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
+void internal_count_launches(uint64_t n) { g_launches += n; }
+
+}  // namespace tlibg

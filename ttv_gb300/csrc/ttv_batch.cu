@@ -1,0 +1,912 @@
+// Batched TTVs in one persistent launch driven by a device-side work queue.
+//
+// A batch of independent fp32 problems (any order, extents, q and layout) is
+// turned into device descriptors once (tlibg_batch_create).  Every launch is
+// one short sequence, captured in a CUDA graph and replayed:
+//
+//   batch_select  (learned mode) the cost-model MLP scores every kernel
+//                 variant of every problem and keeps the cheapest
+//   batch_plan    one CTA: decodes each problem's variant into work units,
+//                 prefix-sums units and split-partial offsets, fills the
+//                 unit -> problem map and resets the queue
+//   batch_exec    persistent CTAs (SMs x occupancy) pop units from an atomic
+//                 counter; a unit is a block of rows (row form) or a tile of
+//                 the prefix over one segment of q (column form, b segment
+//                 staged by TMA); the CTA that completes a split problem's
+//                 last unit combines its partials in fixed segment order
+//
+// Variants (8): index v = 2*g + s.  Row form: lanes per row G = 4 << g;
+// column form: warps along q WI = 1 << g.  s = 1 splits q into up to 4
+// segments (two-phase, deterministic).
+#include "ttv_device.cuh"
+#include "ttv_internal.h"
+#include "ttv_mlp.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+namespace tlibg {
+
+static __device__ unsigned int g_batch_error = 0u;
+
+struct BPair {
+    float s, c;
+};
+
+struct BProb {
+    const float* a;
+    const float* b;
+    float* c;
+    uint64_t P, nq, S;
+    uint64_t seg_len;
+    uint64_t unit_begin;
+    uint64_t part_off;   // in BPair elements
+    float feat[NFEAT];
+    int kind;
+    int vec;
+    int variant;
+    int group;
+    uint32_t nseg;
+    uint32_t units;
+    uint32_t valid_mask;
+    unsigned int done;
+};
+
+struct BCtl {
+    unsigned long long head;
+    unsigned long long total;
+};
+
+constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
+constexpr int BCAP_F32 = BMAX_F32 + 4;
+
+__host__ __device__ inline void decode_variant(int kind, int v, uint64_t nq, int* group, uint32_t* nseg)
+{
+    const int gi = (v >> 1) & 3, si = v & 1;
+    *group = kind == KIND_ROW ? (4 << gi) : (1 << gi);
+    uint64_t ns = 1;
+    if (si) ns = nq >= 64 ? 4 : (nq >= 16 ? 2 : 1);
+    const uint64_t min_seg = kind == KIND_COL ? (nq + BMAX_F32 - 1) / BMAX_F32 : 1;
+    if (ns < min_seg) ns = min_seg;
+    if (ns > nq) ns = nq;
+    *nseg = (uint32_t)ns;
+}
+
+__host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uint64_t P, uint64_t nq,
+                                               uint64_t S, uint32_t nseg, uint64_t* seg_len)
+{
+    uint64_t sl = (nq + nseg - 1) / nseg;
+    if (kind == KIND_ROW) sl = (sl + vec - 1) / vec * vec;
+    *seg_len = sl;
+    const uint64_t ns = (nq + sl - 1) / sl;
+    if (kind == KIND_ROW) {
+        const uint64_t gpc = BLOCK / group;
+        return (S * ns + gpc - 1) / gpc;
+    }
+    const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * vec;
+    return (S * P + TO - 1) / TO * ns;
+}
+
+// --------------------------------------------------------------------------
+// selection: MLP score per (problem, variant), keep the argmin
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int n, const float* __restrict__ w,
+                                                    float log2_count)
+{
+    __shared__ float sw[MLP_PARAMS];
+    for (int p = threadIdx.x; p < MLP_PARAMS; p += blockDim.x) sw[p] = w[p];
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int pi = t / NVARIANT, v = t % NVARIANT;
+    float score = INFINITY;
+    if (pi < n && ((pr[pi].valid_mask >> v) & 1u)) {
+        float x[MLP_IN];
+#pragma unroll
+        for (int i = 0; i < NFEAT; ++i) x[i] = pr[pi].feat[i];
+        x[6] = log2_count / 16.f;
+#pragma unroll
+        for (int i = 0; i < NVARIANT; ++i) x[NFEAT + i] = (i == v) ? 1.f : 0.f;
+        score = mlp_forward<false>(sw, x, nullptr, nullptr, nullptr);
+    }
+    int best = v;
+    // argmin over the 8 lanes of this problem (ties: lowest variant)
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, score, off);
+        const int ob = __shfl_xor_sync(0xffffffffu, best, off);
+        if (os < score || (os == score && ob < best)) {
+            score = os;
+            best = ob;
+        }
+    }
+    if (pi < n && v == 0) pr[pi].variant = isinf(score) ? 0 : best;
+}
+
+__global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pr[i].variant = v;
+}
+
+// --------------------------------------------------------------------------
+// plan: units, prefix sums, unit -> problem map, queue reset (one CTA)
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl,
+                                                   uint32_t* __restrict__ unit_map)
+{
+    __shared__ unsigned long long s_units[32], s_parts[32];
+    __shared__ unsigned long long carry_u, carry_p;
+    if (threadIdx.x == 0) {
+        carry_u = 0;
+        carry_p = 0;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        unsigned long long u = 0, pe = 0;
+        if (i < n) {
+            BProb& P = pr[i];
+            int group;
+            uint32_t nseg;
+            decode_variant(P.kind, P.variant, P.nq, &group, &nseg);
+            uint64_t seg_len;
+            u = unit_count(P.kind, group, P.vec, P.P, P.nq, P.S, nseg, &seg_len);
+            nseg = (uint32_t)((P.nq + seg_len - 1) / seg_len);
+            P.group = group;
+            P.nseg = nseg;
+            P.seg_len = seg_len;
+            P.units = (uint32_t)u;
+            P.done = 0u;
+            pe = nseg > 1 ? (unsigned long long)nseg * P.S * P.P : 0ull;
+        }
+        // inclusive warp scans, then across warps
+        unsigned long long xu = u, xp = pe;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned long long yu = __shfl_up_sync(0xffffffffu, xu, off);
+            const unsigned long long yp = __shfl_up_sync(0xffffffffu, xp, off);
+            if (lane >= off) {
+                xu += yu;
+                xp += yp;
+            }
+        }
+        if (lane == 31) {
+            s_units[warp] = xu;
+            s_parts[warp] = xp;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long wu = lane < (int)(blockDim.x >> 5) ? s_units[lane] : 0ull;
+            unsigned long long wp = lane < (int)(blockDim.x >> 5) ? s_parts[lane] : 0ull;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned long long yu = __shfl_up_sync(0xffffffffu, wu, off);
+                const unsigned long long yp = __shfl_up_sync(0xffffffffu, wp, off);
+                if (lane >= off) {
+                    wu += yu;
+                    wp += yp;
+                }
+            }
+            s_units[lane] = wu;   // inclusive prefix over warps
+            s_parts[lane] = wp;
+        }
+        __syncthreads();
+        const unsigned long long before_u = carry_u + (warp ? s_units[warp - 1] : 0ull) + xu - u;
+        const unsigned long long before_p = carry_p + (warp ? s_parts[warp - 1] : 0ull) + xp - pe;
+        if (i < n) {
+            pr[i].unit_begin = before_u;
+            pr[i].part_off = before_p;
+            for (unsigned long long k = 0; k < u; ++k) unit_map[before_u + k] = (uint32_t)i;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            carry_u += s_units[(blockDim.x >> 5) - 1];
+            carry_p += s_parts[(blockDim.x >> 5) - 1];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctl->total = carry_u;
+        ctl->head = 0ull;
+    }
+}
+
+// --------------------------------------------------------------------------
+// the persistent executor
+// --------------------------------------------------------------------------
+template <int V, bool KAHAN>
+__device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G)
+{
+    const uint32_t lane = threadIdx.x & 31u, gl = lane & (uint32_t)(G - 1);
+    const uint64_t gpc = BLOCK / G;
+    const uint64_t items = P.S * P.nseg;
+    const uint64_t item = lu * gpc + threadIdx.x / G;
+    const bool valid = item < items;
+    constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
+    Acc<float, KAHAN> acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v].init();
+    uint64_t row = 0, seg = 0;
+    if (valid) {
+        row = item / P.nseg;
+        seg = item - row * P.nseg;
+        const uint64_t ib = seg * P.seg_len;
+        const uint64_t ie = min(P.nq, ib + P.seg_len);
+        const float* ap = P.a + row * P.nq + ib;
+        const float* bp = P.b + ib;
+        const uint64_t n = ie - ib, nv = n / V;
+        uint64_t kv = gl;
+        for (; kv + (U - 1) * G < nv; kv += U * G) {
+            float av[U][V], bv[U][V];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
+#pragma unroll
+                for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
+        }
+#pragma unroll 4
+        for (; kv < nv; kv += G) {
+            float av[V];
+            load_a<float, float, V>(ap + kv * V, av);
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
+        }
+        for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
+    }
+#pragma unroll
+    for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
+    for (int off = G >> 1; off > 0; off >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
+        const float oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
+        acc[0].merge(os, oc);
+    }
+    if (valid && gl == 0) P.c[row] = acc[0].value();
+}
+
+template <int V, bool KAHAN>
+__device__ __forceinline__ void row_unit_split(const BProb& P, uint64_t lu, int G, BPair* __restrict__ part)
+{
+    // identical walk to row_unit; partial sums go to part[seg * S + row]
+    const uint32_t lane = threadIdx.x & 31u, gl = lane & (uint32_t)(G - 1);
+    const uint64_t gpc = BLOCK / G;
+    const uint64_t items = P.S * P.nseg;
+    const uint64_t item = lu * gpc + threadIdx.x / G;
+    const bool valid = item < items;
+    constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
+    Acc<float, KAHAN> acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v].init();
+    uint64_t row = 0, seg = 0;
+    if (valid) {
+        row = item / P.nseg;
+        seg = item - row * P.nseg;
+        const uint64_t ib = seg * P.seg_len;
+        const uint64_t ie = min(P.nq, ib + P.seg_len);
+        const float* ap = P.a + row * P.nq + ib;
+        const float* bp = P.b + ib;
+        const uint64_t n = ie - ib, nv = n / V;
+        uint64_t kv = gl;
+        for (; kv + (U - 1) * G < nv; kv += U * G) {
+            float av[U][V], bv[U][V];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
+#pragma unroll
+                for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
+        }
+#pragma unroll 4
+        for (; kv < nv; kv += G) {
+            float av[V];
+            load_a<float, float, V>(ap + kv * V, av);
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
+        }
+        for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
+    }
+#pragma unroll
+    for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
+    for (int off = G >> 1; off > 0; off >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
+        const float oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
+        acc[0].merge(os, oc);
+    }
+    if (valid && gl == 0) {
+        BPair pr;
+        pr.s = acc[0].s;
+        pr.c = KAHAN ? acc[0].c : 0.f;
+        part[P.part_off + seg * P.S + row] = pr;
+    }
+}
+
+// column unit: tile of TO outputs over one segment; false if a staging wait expired
+template <int V, bool KAHAN>
+__device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, float* sb, float* red,
+                                         uint64_t* bar, uint32_t& phase, int* abort_flag,
+                                         BPair* __restrict__ part)
+{
+    const uint32_t WO = (BLOCK / 32) / WI;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t wi = warp % WI, wo = warp / WI;
+    const uint64_t TO = (uint64_t)WO * 32u * V;
+    const uint64_t outputs = P.S * P.P;
+    const uint64_t tiles = (outputs + TO - 1) / TO;
+    const uint64_t seg = lu / tiles, tile = lu - seg * tiles;
+    const uint64_t ib = seg * P.seg_len;
+    const uint64_t ie = min(P.nq, ib + P.seg_len);
+    if (!stage_b<float>(sb, P.b, ib, ie, bar, phase, abort_flag, &g_batch_error)) return false;
+    const uint32_t off = (uint32_t)((reinterpret_cast<uintptr_t>(P.b + ib) & 15u) / sizeof(float));
+    const float* bs = sb + off - ib;
+    constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
+
+    const uint64_t o0 = tile * TO + ((uint64_t)wo * 32u + lane) * V;
+    const bool valid = o0 < outputs;
+    Acc<float, KAHAN> acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v].init();
+    if (valid) {
+        const uint64_t s = o0 / P.P;
+        const uint64_t j = o0 - s * P.P;
+        const float* ap = P.a + (s * P.nq) * P.P + j;
+        uint64_t i = ib + wi;
+        for (; i + (U - 1) * WI < ie; i += U * WI) {
+            float av[U][V];
+#pragma unroll
+            for (int u = 0; u < U; ++u) load_a<float, float, V>(ap + (i + u * WI) * P.P, av[u]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float bb = bs[i + u * WI];
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
+            }
+        }
+#pragma unroll 4
+        for (; i < ie; i += WI) {
+            float av[V];
+            load_a<float, float, V>(ap + i * P.P, av);
+            const float bb = bs[i];
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
+        }
+    }
+    if (WI > 1) {
+        const uint32_t slot = wo * 32u + lane;
+        if (wi > 0) {
+            float* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                r[2 * v] = acc[v].s;
+                r[2 * v + 1] = acc[v].c;
+            }
+        }
+        __syncthreads();
+        if (wi == 0) {
+            for (uint32_t w = 1; w < (uint32_t)WI; ++w) {
+                const float* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].merge(r[2 * v], r[2 * v + 1]);
+            }
+        }
+        __syncthreads();
+    }
+    if (wi == 0 && valid) {
+        if (P.nseg == 1) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) P.c[o0 + v] = acc[v].value();
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                BPair pr;
+                pr.s = acc[v].s;
+                pr.c = KAHAN ? acc[v].c : 0.f;
+                part[P.part_off + seg * outputs + o0 + v] = pr;
+            }
+        }
+    }
+    return true;
+}
+
+template <bool KAHAN>
+__device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __restrict__ part)
+{
+    const uint64_t outputs = P.S * P.P;
+    for (uint64_t o = threadIdx.x; o < outputs; o += BLOCK) {
+        const BPair* pp = part + P.part_off + o;
+        float2 first = __ldcg(reinterpret_cast<const float2*>(pp));
+        Acc<float, KAHAN> acc;
+        acc.s = first.x;
+        acc.c = first.y;
+        for (uint32_t g = 1; g < P.nseg; ++g) {
+            const float2 q = __ldcg(reinterpret_cast<const float2*>(pp + (uint64_t)g * outputs));
+            acc.merge(q.x, q.y);
+        }
+        P.c[o] = acc.value();
+    }
+}
+
+template <bool KAHAN>
+__global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map,
+                                                    BCtl* ctl, BPair* __restrict__ part)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
+    float* sb = reinterpret_cast<float*>(smem_raw + 16);
+    float* red = sb + BCAP_F32;
+    __shared__ unsigned long long s_unit;
+    __shared__ int s_prob, s_last;
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total);
+    unsigned long long next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(&ctl->head, 1ull);
+    uint32_t phase = 0;
+    __syncthreads();
+
+    while (true) {
+        if (threadIdx.x == 0) {
+            s_unit = next;
+            if (next < total) {
+                s_prob = (int)unit_map[next];
+                next = atomicAdd(&ctl->head, 1ull);   // consumed on the next iteration
+            }
+        }
+        __syncthreads();
+        const unsigned long long u = s_unit;
+        if (u >= total) break;
+        const BProb& P = pr[s_prob];
+        const uint64_t lu = u - P.unit_begin;
+        bool ok = true;
+        if (P.kind == KIND_ROW) {
+            if (P.nseg == 1) {
+                switch (P.vec) {
+                case 4: row_unit<4, KAHAN>(P, lu, P.group); break;
+                case 2: row_unit<2, KAHAN>(P, lu, P.group); break;
+                default: row_unit<1, KAHAN>(P, lu, P.group); break;
+                }
+            } else {
+                switch (P.vec) {
+                case 4: row_unit_split<4, KAHAN>(P, lu, P.group, part); break;
+                case 2: row_unit_split<2, KAHAN>(P, lu, P.group, part); break;
+                default: row_unit_split<1, KAHAN>(P, lu, P.group, part); break;
+                }
+            }
+        } else {
+            switch (P.vec) {
+            case 4: ok = col_unit<4, KAHAN>(P, lu, P.group, sb, red, bar, phase, abort_flag, part); break;
+            case 2: ok = col_unit<2, KAHAN>(P, lu, P.group, sb, red, bar, phase, abort_flag, part); break;
+            default: ok = col_unit<1, KAHAN>(P, lu, P.group, sb, red, bar, phase, abort_flag, part); break;
+            }
+        }
+        if (!ok) return;   // every thread saw the same expired wait
+        if (P.nseg > 1) {
+            __syncthreads();   // this CTA's partial stores are issued
+            if (threadIdx.x == 0) {
+                __threadfence();
+                const unsigned int old = atomicAdd(&pr[s_prob].done, 1u);
+                s_last = (old + 1u == P.units);
+            }
+            __syncthreads();
+            if (s_last) {
+                __threadfence();
+                combine_problem<KAHAN>(P, part);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// --------------------------------------------------------------------------
+// host side
+// --------------------------------------------------------------------------
+namespace {
+
+std::mutex g_model_mu;
+std::vector<float> g_model;   // installed cost-model parameters (empty: none)
+
+size_t exec_smem_bytes()
+{
+    const size_t red_floats = (size_t)(8 - 1) * 1 * 32 * 2 * 4;   // largest: WI = 8, V = 4
+    return 16 + (size_t)BCAP_F32 * 4 + red_floats * 4;
+}
+
+int exec_ctas_per_sm(bool kahan)
+{
+    static int cache[2] = {-1, -1};
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    int& c = cache[kahan ? 1 : 0];
+    if (c >= 0) return c;
+    const void* fn = kahan ? reinterpret_cast<const void*>(batch_exec<true>)
+                           : reinterpret_cast<const void*>(batch_exec<false>);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, exec_smem_bytes()) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    c = std::max(1, n);
+    return c;
+}
+
+// widest load (elements) the layout and the pointers' alignment allow
+int batch_vec(int kind, const CanonView& cn, const void* a, const void* b)
+{
+    int vec = 4;
+    while (vec > 1 && !((kind == KIND_ROW ? cn.nq : cn.P) % vec == 0 &&
+                        (reinterpret_cast<uintptr_t>(a) % (vec * 4)) == 0 &&
+                        (kind == KIND_COL || (reinterpret_cast<uintptr_t>(b) % (vec * 4)) == 0)))
+        vec /= 2;
+    return vec;
+}
+
+// The fixed rule the engine uses without the cost model.
+int heuristic_variant(int kind, uint64_t P, uint64_t nq, uint64_t S, int vec)
+{
+    int g = 0, s = 0;
+    if (kind == KIND_ROW) {
+        const uint64_t nvec = (nq + vec - 1) / vec;
+        int G = 4;
+        while (G < 32 && (uint64_t)G * 8 <= nvec) G *= 2;   // >= 4 vector loads per lane
+        g = G == 4 ? 0 : G == 8 ? 1 : G == 16 ? 2 : 3;
+    } else {
+        const uint64_t outputs = S * P;
+        if (outputs < 2048 && nq >= 64) g = 3;
+        else if (outputs < 8192 && nq >= 32) g = 2;
+        else if (outputs < 32768 && nq >= 16) g = 1;
+        s = (outputs < 1024 && nq >= 256) ? 1 : 0;
+    }
+    return 2 * g + s;
+}
+
+}  // namespace
+}  // namespace tlibg
+
+using namespace tlibg;
+
+struct tlibg_batch {
+    int count = 0;
+    int select = TLIBG_SELECT_HEURISTIC;
+    int fixed_variant = 0;
+    bool kahan = true;
+    int grid = 0;
+    BProb* d_prob = nullptr;
+    BCtl* d_ctl = nullptr;
+    uint32_t* d_map = nullptr;
+    BPair* d_part = nullptr;
+    float* d_model = nullptr;
+    float log2_count = 0.f;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int enqueue(tlibg_batch* bt, cudaStream_t st)
+{
+    uint64_t n = 0;
+    if (bt->select == TLIBG_SELECT_LEARNED) {
+        const int threads = bt->count * NVARIANT;
+        batch_select<<<(threads + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_model, bt->log2_count);
+        ++n;
+    } else if (bt->select == TLIBG_SELECT_FIXED) {
+        batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
+        ++n;
+    }
+    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map);
+    const size_t smem = exec_smem_bytes();
+    if (bt->kahan)
+        batch_exec<true><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
+    else
+        batch_exec<false><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
+    n += 2;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
+    internal_count_launches(n);
+    return TLIBG_OK;
+}
+
+int launches_per_run(const tlibg_batch* bt)
+{
+    return (bt->select == TLIBG_SELECT_LEARNED || bt->select == TLIBG_SELECT_FIXED) ? 3 : 2;
+}
+
+void release(tlibg_batch* bt)
+{
+    if (!bt) return;
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->graph) cudaGraphDestroy(bt->graph);
+    if (bt->d_prob) cudaFree(bt->d_prob);
+    if (bt->d_ctl) cudaFree(bt->d_ctl);
+    if (bt->d_map) cudaFree(bt->d_map);
+    if (bt->d_part) cudaFree(bt->d_part);
+    if (bt->d_model) cudaFree(bt->d_model);
+    delete bt;
+}
+
+int create_fail(tlibg_batch* bt, int code, const std::string& msg)
+{
+    release(bt);
+    return internal_fail(code, msg);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tlibg_set_cost_model(const float* params, size_t count)
+{
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    if (!params) {
+        g_model.clear();
+        return internal_ok();
+    }
+    if (count != (size_t)MLP_PARAMS)
+        return internal_fail(TLIBG_ERR_ARGUMENT,
+                             "tlibg_set_cost_model: expected " + std::to_string(MLP_PARAMS) + " parameters");
+    g_model.assign(params, params + count);
+    return internal_ok();
+}
+
+int tlibg_batch_features(const tlibg_problem* pr, size_t count, float* feat, int* kind, int* heuristic)
+{
+    if ((!pr || !feat) && count) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_features: null argument");
+    for (size_t i = 0; i < count; ++i) {
+        const tlibg_problem& x = pr[i];
+        CanonView cn;
+        const int st = internal_analyse(x.q, x.p, x.a, x.na, x.wa, x.pia, x.b, x.nb, x.c, x.nc, x.wc, x.pic, &cn);
+        if (st) return st;
+        size_t k = 0;
+        while (x.pia[k] != x.q) ++k;
+        float* f = feat + i * NFEAT;
+        f[0] = (float)x.p / 8.f;
+        f[1] = x.p > 1 ? (float)k / (float)(x.p - 1) : 0.f;
+        f[2] = (float)std::log2((double)cn.P) / 24.f;
+        f[3] = (float)std::log2((double)cn.nq) / 24.f;
+        f[4] = (float)std::log2((double)cn.S) / 24.f;
+        f[5] = 0.f;   // fp32
+        f[6] = (float)std::log2((double)count) / 16.f;
+        f[7] = cn.P == 1 ? 0.f : 1.f;
+        const int kd = cn.P == 1 ? KIND_ROW : KIND_COL;
+        if (kind) kind[i] = kd;
+        if (heuristic) heuristic[i] = heuristic_variant(kd, cn.P, cn.nq, cn.S, batch_vec(kd, cn, x.a, x.b));
+    }
+    return internal_ok();
+}
+
+int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, const tlibg_batch_options* opt,
+                       void* stream, tlibg_batch** out)
+{
+    if (!out) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_create: null output handle");
+    *out = nullptr;
+    if (dtype != TLIBG_F32)
+        return internal_fail(TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: batches are fp32 (TLIBG_F32)");
+    if (!probs || count == 0 || count > ((size_t)1 << 24))
+        return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_create: need 1 to 2^24 problems");
+    const int sms = internal_sms();
+    if (!sms) return internal_fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    tlibg_batch* bt = new tlibg_batch();
+    bt->count = (int)count;
+    bt->select = opt ? opt->select : TLIBG_SELECT_HEURISTIC;
+    bt->fixed_variant = opt ? opt->variant : 0;
+    bt->kahan = !(opt && opt->accumulate == TLIBG_ACC_PLAIN);
+    const bool use_graph = !(opt && opt->no_graph);
+    const bool have_given = opt && opt->variants;
+    bt->log2_count = (float)std::log2((double)count);
+    if (bt->select < TLIBG_SELECT_HEURISTIC || bt->select > TLIBG_SELECT_GIVEN)
+        return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: unknown selection mode");
+    if (bt->select == TLIBG_SELECT_FIXED && (bt->fixed_variant < 0 || bt->fixed_variant >= NVARIANT))
+        return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: variant must be in 0..7");
+
+    std::vector<float> feat(count * NFEAT);
+    std::vector<int> kinds(count), heur(count);
+    int s = tlibg_batch_features(probs, count, feat.data(), kinds.data(), heur.data());
+    if (s) {
+        release(bt);
+        return s;
+    }
+    std::vector<float> model;
+    if (bt->select == TLIBG_SELECT_LEARNED) {
+        std::lock_guard<std::mutex> lk(g_model_mu);
+        model = g_model;
+    }
+    if (bt->select == TLIBG_SELECT_LEARNED && model.empty())
+        // no model installed: exhaustive-tuning results when given, else the fixed rule
+        bt->select = have_given ? TLIBG_SELECT_GIVEN : TLIBG_SELECT_HEURISTIC;
+    if (bt->select == TLIBG_SELECT_GIVEN && !have_given)
+        return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: TLIBG_SELECT_GIVEN needs variants");
+
+    // descriptors; unit map and partial scratch sized for the worst variant of each problem
+    std::vector<BProb> hp(count);
+    uint64_t total_units = 0, max_part = 0;
+    for (size_t i = 0; i < count; ++i) {
+        const tlibg_problem& x = probs[i];
+        CanonView cn;
+        internal_analyse(x.q, x.p, x.a, x.na, x.wa, x.pia, x.b, x.nb, x.c, x.nc, x.wc, x.pic, &cn);
+        BProb& b = hp[i];
+        std::memset(&b, 0, sizeof(b));
+        b.a = static_cast<const float*>(x.a);
+        b.b = static_cast<const float*>(x.b);
+        b.c = static_cast<float*>(x.c);
+        b.P = cn.P;
+        b.nq = cn.nq;
+        b.S = cn.S;
+        b.kind = kinds[i];
+        b.vec = batch_vec(b.kind, cn, x.a, x.b);
+        std::copy(feat.begin() + i * NFEAT, feat.begin() + (i + 1) * NFEAT, b.feat);
+        b.valid_mask = (1u << NVARIANT) - 1u;
+        b.variant = heur[i];
+        if (bt->select == TLIBG_SELECT_GIVEN) {
+            const int v = opt->variants[i];
+            if (v < 0 || v >= NVARIANT)
+                return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: variants must be in 0..7");
+            b.variant = v;
+        }
+        uint64_t mu = 0, mp = 0;
+        for (int v = 0; v < NVARIANT; ++v) {
+            int g;
+            uint32_t ns;
+            decode_variant(b.kind, v, b.nq, &g, &ns);
+            uint64_t sl;
+            mu = std::max(mu, unit_count(b.kind, g, b.vec, b.P, b.nq, b.S, ns, &sl));
+            const uint64_t nsr = (b.nq + sl - 1) / sl;
+            if (nsr > 1) mp = std::max(mp, nsr * b.S * b.P);
+        }
+        total_units += mu;
+        max_part += mp;
+    }
+    if (total_units >= ((uint64_t)1 << 32))
+        return create_fail(bt, TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: more than 2^32 work units");
+
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&bt->d_prob, count * sizeof(BProb))) != cudaSuccess ||
+        (e = cudaMalloc(&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
+        (e = cudaMalloc(&bt->d_map, std::max<uint64_t>(total_units, 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc(&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
+        (!model.empty() && (e = cudaMalloc(&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
+        cudaGetLastError();
+        return create_fail(bt, TLIBG_ERR_NOMEM, std::string("tlibg_batch_create: ") + cudaGetErrorString(e));
+    }
+    cudaMemcpyAsync(bt->d_prob, hp.data(), count * sizeof(BProb), cudaMemcpyHostToDevice, st);
+    if (!model.empty() && bt->select == TLIBG_SELECT_LEARNED)
+        cudaMemcpyAsync(bt->d_model, model.data(), MLP_PARAMS * sizeof(float), cudaMemcpyHostToDevice, st);
+    bt->grid = sms * exec_ctas_per_sm(bt->kahan);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        release(bt);
+        return internal_cuda_fail(e, "tlibg_batch_create");
+    }
+    if (use_graph) {
+        cudaStream_t cap = nullptr;
+        if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess) {
+            release(bt);
+            return internal_cuda_fail(e, "capture stream");
+        }
+        e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            s = enqueue(bt, cap);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+            if (!s && e2 == cudaSuccess) {
+                bt->graph = g;
+                e = cudaGraphInstantiate(&bt->exec, g, 0);
+            } else {
+                e = e2 != cudaSuccess ? e2 : cudaErrorUnknown;
+                if (g) cudaGraphDestroy(g);
+            }
+        }
+        cudaStreamDestroy(cap);
+        if (s) {
+            release(bt);
+            return s;
+        }
+        if (e != cudaSuccess) {
+            release(bt);
+            return internal_cuda_fail(e, "graph capture");
+        }
+    }
+    *out = bt;
+    return internal_ok();
+}
+
+int tlibg_batch_launch(tlibg_batch* bt, void* stream)
+{
+    if (!bt) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_launch: null batch");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (bt->exec) {
+        const cudaError_t e = cudaGraphLaunch(bt->exec, st);
+        if (e != cudaSuccess) return internal_cuda_fail(e, "graph launch");
+        internal_count_launches((uint64_t)launches_per_run(bt));
+        return internal_ok();
+    }
+    const int s = enqueue(bt, st);
+    return s ? s : internal_ok();
+}
+
+int tlibg_batch_set_variant(tlibg_batch* bt, int variant)
+{
+    if (!bt) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_set_variant: null batch");
+    if (bt->select != TLIBG_SELECT_FIXED || bt->exec)
+        return internal_fail(TLIBG_ERR_ARGUMENT,
+                             "tlibg_batch_set_variant: only for TLIBG_SELECT_FIXED batches built with no_graph");
+    if (variant < 0 || variant >= NVARIANT)
+        return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_set_variant: variant must be in 0..7");
+    bt->fixed_variant = variant;
+    return internal_ok();
+}
+
+int tlibg_batch_variants(tlibg_batch* bt, int* out, void* stream)
+{
+    if (!bt || !out) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_variants: null argument");
+    std::vector<BProb> hp(bt->count);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(hp.data(), bt->d_prob, bt->count * sizeof(BProb), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return internal_cuda_fail(e, "tlibg_batch_variants");
+    for (int i = 0; i < bt->count; ++i) out[i] = hp[i].variant;
+    return internal_ok();
+}
+
+int tlibg_batch_destroy(tlibg_batch* bt)
+{
+    if (bt) {
+        cudaDeviceSynchronize();
+        release(bt);
+    }
+    return internal_ok();
+}
+
+int tlibg_ttv_batch(int dtype, const tlibg_problem* probs, size_t count, const tlibg_batch_options* opt,
+                    void* stream)
+{
+    tlibg_batch* bt = nullptr;
+    tlibg_batch_options o{};
+    if (opt) o = *opt;
+    o.no_graph = 1;   // one launch: nothing to replay
+    int s = tlibg_batch_create(dtype, probs, count, &o, stream, &bt);
+    if (s) return s;
+    s = tlibg_batch_launch(bt, stream);
+    cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    release(bt);
+    return s;
+}
+
+int tlibg_ttv_percall(int dtype, const tlibg_problem* probs, size_t count, void* stream)
+{
+    if (!probs && count) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_ttv_percall: null problems");
+    for (size_t i = 0; i < count; ++i) {
+        const tlibg_problem& x = probs[i];
+        const int s = tlibg_ttv_ex(dtype, x.q, x.p, x.a, x.na, x.wa, x.pia, x.b, x.nb, x.c, x.nc, x.wc, x.pic,
+                                   nullptr, stream);
+        if (s) return s;
+    }
+    return internal_ok();
+}
+
+unsigned int tlibg_batch_device_error(void)
+{
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_batch_error, sizeof(v)) != cudaSuccess) return 0xffffffffu;
+    cudaMemcpyToSymbol(g_batch_error, &zero, sizeof(zero));
+    return v;
+}
+
+}  // extern "C"

@@ -1,0 +1,34 @@
+// Internal interface between the C-ABI translation units (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/tlibg.h"
+#include "ttv_kernels.cuh"
+
+namespace tlibg {
+
+struct CanonView {
+    uint64_t P = 1, nq = 1, S = 1;
+    int ref_case = 0;
+};
+
+// Validate a low-level call exactly like tlibg_ttv_* and reduce it to the
+// canonical (S, nq, P) view; sets the thread's last error on failure.
+int internal_analyse(size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+                     const size_t* pia, const void* b, const size_t* nb, const void* c,
+                     const size_t* nc, const size_t* wc, const size_t* pic, CanonView* out);
+// The single-call planner (heuristic).
+int internal_plan(int dtype, const CanonView& cn, const void* a, const void* b,
+                  const tlibg_options* opt, int sms, Plan* out);
+// Streaming multiprocessors of the current device (0 without a device).
+int internal_sms();
+int internal_fail(int code, const std::string& msg);
+int internal_ok();
+int internal_cuda_fail(cudaError_t e, const char* where);
+void internal_count_launches(uint64_t n);
+
+}  // namespace tlibg
