@@ -76,6 +76,16 @@ __host__ __device__ inline void decode_variant(int kind, int v, uint64_t nq, int
     *nseg = (uint32_t)ns;
 }
 
+// Row form: rounds of one row segment per lane group that make up a work unit,
+// so that a unit covers about 64 KB of A (per-unit queue overhead amortised).
+__host__ __device__ inline uint64_t rows_per_group(uint64_t seg_len, int group)
+{
+    const uint64_t gpc = BLOCK / group;
+    const uint64_t per_round = gpc * seg_len * 4;
+    uint64_t r = (65536 + per_round - 1) / per_round;
+    return r < 1 ? 1 : (r > 64 ? 64 : r);
+}
+
 __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uint64_t P, uint64_t nq,
                                                uint64_t S, uint32_t nseg, uint64_t* seg_len)
 {
@@ -84,8 +94,8 @@ __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uin
     *seg_len = sl;
     const uint64_t ns = (nq + sl - 1) / sl;
     if (kind == KIND_ROW) {
-        const uint64_t gpc = BLOCK / group;
-        return (S * ns + gpc - 1) / gpc;
+        const uint64_t per_unit = (BLOCK / group) * rows_per_group(sl, group);
+        return (S * ns + per_unit - 1) / per_unit;
     }
     const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * vec;
     return (S * P + TO - 1) / TO * ns;
@@ -220,116 +230,68 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
 // the persistent executor
 // --------------------------------------------------------------------------
 template <int V, bool KAHAN>
-__device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G)
+__device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPair* __restrict__ part)
 {
     const uint32_t lane = threadIdx.x & 31u, gl = lane & (uint32_t)(G - 1);
     const uint64_t gpc = BLOCK / G;
     const uint64_t items = P.S * P.nseg;
-    const uint64_t item = lu * gpc + threadIdx.x / G;
-    const bool valid = item < items;
+    const uint64_t R = rows_per_group(P.seg_len, G);
     constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
-    Acc<float, KAHAN> acc[V];
+    for (uint64_t r = 0; r < R; ++r) {
+        const uint64_t item = (lu * R + r) * gpc + threadIdx.x / G;
+        const bool valid = item < items;
+        Acc<float, KAHAN> acc[V];
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc[v].init();
-    uint64_t row = 0, seg = 0;
-    if (valid) {
-        row = item / P.nseg;
-        seg = item - row * P.nseg;
-        const uint64_t ib = seg * P.seg_len;
-        const uint64_t ie = min(P.nq, ib + P.seg_len);
-        const float* ap = P.a + row * P.nq + ib;
-        const float* bp = P.b + ib;
-        const uint64_t n = ie - ib, nv = n / V;
-        uint64_t kv = gl;
-        for (; kv + (U - 1) * G < nv; kv += U * G) {
-            float av[U][V], bv[U][V];
+        for (int v = 0; v < V; ++v) acc[v].init();
+        uint64_t row = 0, seg = 0;
+        if (valid) {
+            row = item / P.nseg;
+            seg = item - row * P.nseg;
+            const uint64_t ib = seg * P.seg_len;
+            const uint64_t ie = min(P.nq, ib + P.seg_len);
+            const float* ap = P.a + row * P.nq + ib;
+            const float* bp = P.b + ib;
+            const uint64_t n = ie - ib, nv = n / V;
+            uint64_t kv = gl;
+            for (; kv + (U - 1) * G < nv; kv += U * G) {
+                float av[U][V], bv[U][V];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
+                for (int u = 0; u < U; ++u) {
+                    load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
 #pragma unroll
-                for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
+                    for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
             }
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-#pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
-        }
 #pragma unroll 4
-        for (; kv < nv; kv += G) {
-            float av[V];
-            load_a<float, float, V>(ap + kv * V, av);
+            for (; kv < nv; kv += G) {
+                float av[V];
+                load_a<float, float, V>(ap + kv * V, av);
 #pragma unroll
-            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
-        }
-        for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
-    }
-#pragma unroll
-    for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
-    for (int off = G >> 1; off > 0; off >>= 1) {
-        const float os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
-        const float oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
-        acc[0].merge(os, oc);
-    }
-    if (valid && gl == 0) P.c[row] = acc[0].value();
-}
-
-template <int V, bool KAHAN>
-__device__ __forceinline__ void row_unit_split(const BProb& P, uint64_t lu, int G, BPair* __restrict__ part)
-{
-    // identical walk to row_unit; partial sums go to part[seg * S + row]
-    const uint32_t lane = threadIdx.x & 31u, gl = lane & (uint32_t)(G - 1);
-    const uint64_t gpc = BLOCK / G;
-    const uint64_t items = P.S * P.nseg;
-    const uint64_t item = lu * gpc + threadIdx.x / G;
-    const bool valid = item < items;
-    constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
-    Acc<float, KAHAN> acc[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) acc[v].init();
-    uint64_t row = 0, seg = 0;
-    if (valid) {
-        row = item / P.nseg;
-        seg = item - row * P.nseg;
-        const uint64_t ib = seg * P.seg_len;
-        const uint64_t ie = min(P.nq, ib + P.seg_len);
-        const float* ap = P.a + row * P.nq + ib;
-        const float* bp = P.b + ib;
-        const uint64_t n = ie - ib, nv = n / V;
-        uint64_t kv = gl;
-        for (; kv + (U - 1) * G < nv; kv += U * G) {
-            float av[U][V], bv[U][V];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
-#pragma unroll
-                for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
             }
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-#pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
+            for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
         }
-#pragma unroll 4
-        for (; kv < nv; kv += G) {
-            float av[V];
-            load_a<float, float, V>(ap + kv * V, av);
 #pragma unroll
-            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
+        for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
+        for (int off = G >> 1; off > 0; off >>= 1) {
+            const float os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
+            const float oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
+            acc[0].merge(os, oc);
         }
-        for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
-    }
-#pragma unroll
-    for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
-    for (int off = G >> 1; off > 0; off >>= 1) {
-        const float os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
-        const float oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
-        acc[0].merge(os, oc);
-    }
-    if (valid && gl == 0) {
-        BPair pr;
-        pr.s = acc[0].s;
-        pr.c = KAHAN ? acc[0].c : 0.f;
-        part[P.part_off + seg * P.S + row] = pr;
+        if (valid && gl == 0) {
+            if (P.nseg == 1) {
+                P.c[row] = acc[0].value();
+            } else {
+                BPair pr;
+                pr.s = acc[0].s;
+                pr.c = KAHAN ? acc[0].c : 0.f;
+                part[P.part_off + seg * P.S + row] = pr;
+            }
+        }
     }
 }
 
@@ -348,9 +310,12 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
     const uint64_t seg = lu / tiles, tile = lu - seg * tiles;
     const uint64_t ib = seg * P.seg_len;
     const uint64_t ie = min(P.nq, ib + P.seg_len);
-    if (!stage_b<float>(sb, P.b, ib, ie, bar, phase, abort_flag, &g_batch_error)) return false;
-    const uint32_t off = (uint32_t)((reinterpret_cast<uintptr_t>(P.b + ib) & 15u) / sizeof(float));
-    const float* bs = sb + off - ib;
+    // b is read through L1 (warp-uniform per row): no per-unit staging wait
+    const float* __restrict__ bs = P.b;
+    (void)sb;
+    (void)bar;
+    (void)phase;
+    (void)abort_flag;
     constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
 
     const uint64_t o0 = tile * TO + ((uint64_t)wo * 32u + lane) * V;
@@ -369,7 +334,7 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
             for (int u = 0; u < U; ++u) load_a<float, float, V>(ap + (i + u * WI) * P.P, av[u]);
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const float bb = bs[i + u * WI];
+                const float bb = __ldg(bs + i + u * WI);
 #pragma unroll
                 for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
             }
@@ -378,7 +343,7 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
         for (; i < ie; i += WI) {
             float av[V];
             load_a<float, float, V>(ap + i * P.P, av);
-            const float bb = bs[i];
+            const float bb = __ldg(bs + i);
 #pragma unroll
             for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
         }
@@ -445,8 +410,8 @@ __global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, cons
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
-    float* sb = reinterpret_cast<float*>(smem_raw + 16);
-    float* red = sb + BCAP_F32;
+    float* sb = nullptr;   // column units read b through L1 (no staging buffer)
+    float* red = reinterpret_cast<float*>(smem_raw + 16);
     __shared__ unsigned long long s_unit;
     __shared__ int s_prob, s_last;
 
@@ -476,18 +441,10 @@ __global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, cons
         const uint64_t lu = u - P.unit_begin;
         bool ok = true;
         if (P.kind == KIND_ROW) {
-            if (P.nseg == 1) {
-                switch (P.vec) {
-                case 4: row_unit<4, KAHAN>(P, lu, P.group); break;
-                case 2: row_unit<2, KAHAN>(P, lu, P.group); break;
-                default: row_unit<1, KAHAN>(P, lu, P.group); break;
-                }
-            } else {
-                switch (P.vec) {
-                case 4: row_unit_split<4, KAHAN>(P, lu, P.group, part); break;
-                case 2: row_unit_split<2, KAHAN>(P, lu, P.group, part); break;
-                default: row_unit_split<1, KAHAN>(P, lu, P.group, part); break;
-                }
+            switch (P.vec) {
+            case 4: row_unit<4, KAHAN>(P, lu, P.group, part); break;
+            case 2: row_unit<2, KAHAN>(P, lu, P.group, part); break;
+            default: row_unit<1, KAHAN>(P, lu, P.group, part); break;
             }
         } else {
             switch (P.vec) {
@@ -525,7 +482,7 @@ std::vector<float> g_model;   // installed cost-model parameters (empty: none)
 size_t exec_smem_bytes()
 {
     const size_t red_floats = (size_t)(8 - 1) * 1 * 32 * 2 * 4;   // largest: WI = 8, V = 4
-    return 16 + (size_t)BCAP_F32 * 4 + red_floats * 4;
+    return 16 + red_floats * 4;
 }
 
 int exec_ctas_per_sm(bool kahan)
@@ -560,20 +517,16 @@ int batch_vec(int kind, const CanonView& cn, const void* a, const void* b)
 // The fixed rule the engine uses without the cost model.
 int heuristic_variant(int kind, uint64_t P, uint64_t nq, uint64_t S, int vec)
 {
-    int g = 0, s = 0;
-    if (kind == KIND_ROW) {
-        const uint64_t nvec = (nq + vec - 1) / vec;
-        int G = 4;
-        while (G < 32 && (uint64_t)G * 8 <= nvec) G *= 2;   // >= 4 vector loads per lane
-        g = G == 4 ? 0 : G == 8 ? 1 : G == 16 ? 2 : 3;
-    } else {
+    // Row form: four lanes per row; column form: one warp row per tile unless the
+    // problem has few outputs and a long contraction; never split.
+    (void)vec;
+    int g = 0;
+    if (kind == KIND_COL) {
         const uint64_t outputs = S * P;
-        if (outputs < 2048 && nq >= 64) g = 3;
-        else if (outputs < 8192 && nq >= 32) g = 2;
-        else if (outputs < 32768 && nq >= 16) g = 1;
-        s = (outputs < 1024 && nq >= 256) ? 1 : 0;
+        if (outputs < 512 && nq >= 128) g = 2;
+        else if (outputs < 2048 && nq >= 64) g = 1;
     }
-    return 2 * g + s;
+    return 2 * g;
 }
 
 }  // namespace
