@@ -136,22 +136,33 @@ def test_metadata_helpers_match_reference(engine):
 
 
 def test_planner_kernel_family(engine):
-    # q fastest in the layout -> row kernel; otherwise the column kernel
-    assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
-    assert engine.plan(3, [64, 32, 16], [3, 2, 1])["kind"] == engine.KIND_ROW
-    assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_COL
-    pl = engine.plan(2, [256, 256, 256], [1, 2, 3])
+    # whole rows of the canonical view within a 16 KB stage -> the streamed kernel
+    assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_STREAM
+    assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_STREAM
+    assert engine.plan(2, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_STREAM
+    # long rows: the register kernels (q fastest -> row kernel, else column kernel)
+    assert engine.plan(1, [16384, 16384], [1, 2])["kind"] == engine.KIND_ROW
+    assert engine.plan(2, [16384, 16384], [1, 2])["kind"] == engine.KIND_COL
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL
+    # forced register kernels
+    R, Cn = engine.KIND_ROW, engine.KIND_COL
+    assert engine.plan(1, [64, 32, 16], [1, 2, 3], kind=R)["kind"] == R
+    assert engine.plan(3, [64, 32, 16], [3, 2, 1], kind=R)["kind"] == R
+    pl = engine.plan(2, [256, 256, 256], [1, 2, 3], kind=Cn)
     assert (pl["P"], pl["nq"], pl["S"]) == (256, 256, 256)
     assert pl["vec"] == 4 and pl["accumulate"] == engine.ACC_COMPENSATED
     # odd prefix: scalar loads; fp64: 2 per 16-byte load; bf16: 8
-    assert engine.plan(2, [25, 25, 25], [1, 2, 3])["vec"] == 1
-    assert engine.plan(2, [256, 256, 256], [1, 2, 3], dtype=engine.F64)["vec"] == 2
-    assert engine.plan(2, [256, 256, 256], [1, 2, 3], dtype=engine.BF16A)["vec"] == 8
+    assert engine.plan(2, [25, 25, 25], [1, 2, 3], kind=Cn)["vec"] == 1
+    assert engine.plan(2, [256, 256, 256], [1, 2, 3], dtype=engine.F64, kind=Cn)["vec"] == 2
+    assert engine.plan(2, [256, 256, 256], [1, 2, 3], dtype=engine.BF16A, kind=Cn)["vec"] == 8
+    with pytest.raises(engine.TTVError, match="streamed kernel"):
+        engine.plan(1, [16384, 16384], [1, 2], kind=engine.KIND_STREAM)
     # long contraction with a thin prefix is split, and segments fit the staged b
-    pl = engine.plan(2, [64, 1 << 22], [1, 2])
+    pl = engine.plan(2, [64, 1 << 22], [1, 2], kind=Cn)
     assert pl["split"] >= (1 << 22) // 4096
+    assert engine.plan(2, [64, 1 << 22], [1, 2])["split"] > 1   # streamed: split to fill the GPU
     # forced options are honoured or refused
-    assert engine.plan(2, [256, 256, 256], [1, 2, 3], group=2, split=3)["group"] == 2
+    assert engine.plan(2, [256, 256, 256], [1, 2, 3], kind=Cn, group=2, split=3)["group"] == 2
     with pytest.raises(engine.TTVError):
         engine.plan(1, [256, 256, 256], [1, 2, 3], kind=engine.KIND_COL)
 

@@ -167,6 +167,7 @@ def test_variant_sweep(engine, orc, torch_dev, na, pia, q):
         vmax = 16 // np.dtype(dt).itemsize
         groups = [1, 2, 4, 8, 16, 32] if P == 1 else [1, 2, 4, 8]
         vecs = [v for v in (1, 2, 4, 8) if v <= vmax and (nq if P == 1 else P) % v == 0]
+        kind = engine.KIND_ROW if P == 1 else engine.KIND_COL
         for g in groups:
             for v in vecs:
                 bmax = 16384 // np.dtype(dt).itemsize   # b elements staged per segment
@@ -175,8 +176,17 @@ def test_variant_sweep(engine, orc, torch_dev, na, pia, q):
                         continue
                     if split > nq:
                         continue
-                    check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, group=g,
-                          vec=v, split=split)
+                    check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
+                          group=g, vec=v, split=split)
+        # the TMA-streamed kernel, where whole rows fit a stage
+        L = nq if P == 1 else P
+        if L * np.dtype(dt).itemsize <= 16384 and (P == 1 or -(-P // 256) <= 8):
+            for g in ([1, 2, 4, 8, 16, 32] if P == 1 else [0]):
+                for split in ((0,) if P == 1 else (0, 1, 3, 17)):
+                    if split > nq:
+                        continue
+                    check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
+                          kind=engine.KIND_STREAM, group=g, split=split)
 
 
 def test_bf16_stored_a(engine, orc, torch_dev):

@@ -28,7 +28,7 @@ __all__ = [
     "TTVError", "UnsupportedError", "ttv", "ttv_ex", "ttv_host", "ttv_array", "ttvs", "plan",
     "output_shape", "output_layout", "strides", "k_order_layout", "inverse_mode",
     "library", "library_path", "launch_count", "device_error", "F32", "F64", "BF16A",
-    "ACC_COMPENSATED", "ACC_PLAIN", "KIND_ROW", "KIND_COL",
+    "ACC_COMPENSATED", "ACC_PLAIN", "KIND_ROW", "KIND_COL", "KIND_STREAM",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -36,7 +36,7 @@ LIB_PATH = os.path.join(HERE, "libttvgpu.so")
 
 F32, F64, BF16A = 0, 1, 2
 ACC_COMPENSATED, ACC_PLAIN = 0, 1
-KIND_ROW, KIND_COL = 0, 1
+KIND_ROW, KIND_COL, KIND_STREAM = 0, 1, 2
 OK, ERR_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = range(6)
 
 

@@ -290,6 +290,57 @@ int pow2_floor(uint64_t x)
     return r;
 }
 
+// Streamed kernel: A as rows of L contiguous elements, R rows per 16 KB chunk,
+// a static block of units per CTA (row form: rows; column form: (s, segment)).
+int make_stream_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
+{
+    const size_t ea = elem_size_a(pl.dtype);
+    pl.kind = KIND_STREAM;
+    pl.stream_col = cn.P > 1 ? 1 : 0;
+    pl.vec = 1;
+    pl.L = cn.P == 1 ? cn.nq : cn.P;
+    pl.R = std::max<uint64_t>(1, (uint64_t)STREAM_STAGE_BYTES / (pl.L * ea));
+    const int force_split = opt ? opt->split : 0;
+    const int force_group = opt ? opt->group : 0;
+    if (!pl.stream_col) {
+        // fp64 rows: at least 32 elements per lane, so the DADDs of the shuffle tree stay
+        // small next to the one DFMA per element (GB300's FP64 pipe is the bound there)
+        const uint64_t per_lane = pl.dtype == F64 ? 32 : 8;
+        int G = force_group > 0 ? force_group : std::min(32, std::max(1, pow2_floor(pl.L / per_lane)));
+        if (G < 1 || G > 32 || (G & (G - 1)))
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: lanes per row must be a power of two in 1..32");
+        pl.group = G;
+    } else {
+        pl.group = 1;
+        pl.RG = cn.P < (uint64_t)STREAM_CONSUMERS ? (int)(STREAM_CONSUMERS / cn.P) : 1;
+        pl.J = cn.P < (uint64_t)STREAM_CONSUMERS ? 1 : (int)cdiv(cn.P, STREAM_CONSUMERS);
+    }
+    const int cps = std::max(1, plan_ctas_per_sm(pl));
+    const uint64_t grid_max = (uint64_t)sms * cps;
+    uint64_t nseg = 1;
+    if (!pl.stream_col) {
+        pl.units = cn.S;
+    } else {
+        if (force_split > 0) {
+            nseg = (uint64_t)force_split;
+        } else if (cn.S < 2 * grid_max) {
+            nseg = cdiv(2 * grid_max, cn.S);
+            nseg = std::min<uint64_t>(nseg, std::max<uint64_t>(1, cn.nq / (2 * pl.R)));
+        }
+        nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
+        pl.seg_len = cdiv(cn.nq, nseg);
+        nseg = cdiv(cn.nq, pl.seg_len);
+        pl.units = cn.S * nseg;
+    }
+    pl.split = (int)nseg;
+    pl.units_per_cta = cdiv(pl.units, std::min<uint64_t>(grid_max, pl.units));
+    pl.grid = (int)cdiv(pl.units, pl.units_per_cta);
+    pl.f64_combine = (pl.dtype != F64) && pl.split > 1 && cn.nq > (uint64_t(1) << 20);
+    pl.smem = plan_smem_bytes(pl);
+    *out = pl;
+    return TLIBG_OK;
+}
+
 int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
               int sms, Plan* out)
 {
@@ -300,10 +351,16 @@ int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tl
     pl.S = cn.S;
     pl.kahan = (dtype == F64) ? 0 : ((opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1);
     pl.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
-    if (opt && opt->kind >= 0 && opt->kind != pl.kind)
+    const bool eligible = stream_eligible(dtype, cn.P, cn.nq);
+    if (opt && opt->kind == KIND_STREAM && !eligible)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the streamed kernel needs whole rows of the canonical view "
+                                        "(n_q when P == 1, else P) within one 16 KB stage");
+    if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
     const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
+    if ((opt && opt->kind == KIND_STREAM) || (eligible && !(opt && opt->kind >= 0)))
+        return make_stream_plan(pl, cn, opt, sms, out);
     const int vmax = (int)(16 / ea);
 
     // vector width: the widest load that keeps every access aligned
@@ -326,7 +383,9 @@ int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tl
     const int force_group = opt ? opt->group : 0;
     if (pl.kind == KIND_ROW) {
         const uint64_t nvec = cdiv(cn.nq, V);
-        int G = force_group > 0 ? force_group : std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / 4)));
+        const uint64_t vec_per_lane = dtype == F64 ? 16 : 4;   // fp64: keep shuffle-tree DADDs rare
+        int G = force_group > 0 ? force_group
+                                : std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / vec_per_lane)));
         if (G < 1 || G > 32 || (G & (G - 1)))
             return fail(TLIBG_ERR_ARGUMENT, "tlibg: lanes per row must be a power of two in 1..32");
         pl.group = G;

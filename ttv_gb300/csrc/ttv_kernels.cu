@@ -23,6 +23,7 @@
 #include "ttv_device.cuh"
 #include "ttv_kernels.cuh"
 
+#include <algorithm>
 #include <mutex>
 #include <unordered_map>
 
@@ -320,6 +321,12 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
     }
 }
 
+}  // namespace tlibg
+
+#include "ttv_stream.cuh"
+
+namespace tlibg {
+
 // --------------------------------------------------------------------------
 // host side: instantiation tables
 // --------------------------------------------------------------------------
@@ -347,8 +354,35 @@ static KernelFn pick_main(int kind, int vec)
     return nullptr;
 }
 
+typedef void (*StreamFn)(SArgs);
+
+static StreamFn stream_fn(const Plan& p)
+{
+    const bool col = p.stream_col != 0;
+    switch (p.dtype) {
+    case F32:
+        if (p.kahan) return col ? stream_kernel<float, float, true, true> : stream_kernel<float, float, true, false>;
+        return col ? stream_kernel<float, float, false, true> : stream_kernel<float, float, false, false>;
+    case F64:
+        return col ? stream_kernel<double, double, false, true> : stream_kernel<double, double, false, false>;
+    case BF16A:
+        if (p.kahan)
+            return col ? stream_kernel<uint16_t, float, true, true> : stream_kernel<uint16_t, float, true, false>;
+        return col ? stream_kernel<uint16_t, float, false, true> : stream_kernel<uint16_t, float, false, false>;
+    }
+    return nullptr;
+}
+
+bool stream_eligible(int dtype, uint64_t P, uint64_t nq)
+{
+    const uint64_t ea = dtype == F64 ? 8 : (dtype == BF16A ? 2 : 4);
+    if (P == 1) return nq * ea <= (uint64_t)STREAM_STAGE;
+    return P * ea <= (uint64_t)STREAM_STAGE && (P + STREAM_NT - 1) / STREAM_NT <= (uint64_t)STREAM_MAXJ;
+}
+
 static KernelFn main_kernel(const Plan& p)
 {
+    if (p.kind == KIND_STREAM) return reinterpret_cast<KernelFn>(stream_fn(p));
     switch (p.dtype) {
     case F32:
         return p.kahan ? pick_main<float, float, true>(p.kind, p.vec)
@@ -366,6 +400,12 @@ static size_t acc_size(int dtype) { return dtype == F64 ? 8 : 4; }
 
 size_t plan_smem_bytes(const Plan& p)
 {
+    if (p.kind == KIND_STREAM) {
+        const size_t es = acc_size(p.dtype);
+        size_t extra = 2 * (size_t)STREAM_NT * es;
+        if (!p.stream_col) extra = std::max(extra, (size_t)p.L * es);
+        return 128 + (size_t)STREAM_NS * STREAM_SLOT + extra;
+    }
     if (p.kind == KIND_ROW) return 0;
     const size_t es = acc_size(p.dtype);
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
@@ -397,9 +437,12 @@ int plan_ctas_per_sm(const Plan& p)
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(fn), BLOCK, smem) !=
-        cudaSuccess)
+    const int threads = p.kind == KIND_STREAM ? STREAM_THREADS : BLOCK;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(fn), threads, smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
         n = 0;
+    }
     std::lock_guard<std::mutex> lk(mu);
     cache[key] = n;
     return n;
@@ -410,6 +453,36 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
 {
     KernelFn fn = main_kernel(plan);
     if (!fn) return cudaErrorInvalidConfiguration;
+    if (plan.kind == KIND_STREAM) {
+        SArgs sa;
+        sa.a = a;
+        sa.b = b;
+        sa.out = c;
+        sa.partial = partial;
+        sa.S = plan.S;
+        sa.nq = plan.nq;
+        sa.P = plan.P;
+        sa.L = plan.L;
+        sa.R = plan.R;
+        sa.units = plan.units;
+        sa.units_per_cta = plan.units_per_cta;
+        sa.seg_len = plan.seg_len;
+        sa.nseg = (uint32_t)plan.split;
+        sa.G = (uint32_t)plan.group;
+        sa.RG = (uint32_t)plan.RG;
+        sa.J = (uint32_t)plan.J;
+        const size_t smem = plan_smem_bytes(plan);
+        StreamFn sf = stream_fn(plan);
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(reinterpret_cast<const void*>(sf), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        sf<<<plan.grid, STREAM_THREADS, smem, stream>>>(sa);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        if (launches) ++*launches;
+        if (plan.split > 1) return launch_combine(plan, partial, c, stream, launches);
+        return cudaSuccess;
+    }
     KArgs k;
     k.a = a;
     k.b = b;
@@ -434,7 +507,14 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (launches) ++*launches;
-    if (plan.split > 1) {
+    if (plan.split > 1) return launch_combine(plan, partial, c, stream, launches);
+    return cudaSuccess;
+}
+
+cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_t stream, uint64_t* launches)
+{
+    cudaError_t err;
+    {
         const uint64_t outputs = plan.S * plan.P;
         int g = (int)((outputs + BLOCK - 1) / BLOCK);
         if (g > 152 * 16) g = 152 * 16;

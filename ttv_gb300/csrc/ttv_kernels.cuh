@@ -7,10 +7,12 @@
 namespace tlibg {
 
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
-enum Kind { KIND_ROW = 0, KIND_COL = 1 };
+enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
+constexpr int STREAM_STAGE_BYTES = 16384;   // streamed kernel: bytes of A per shared-memory stage
+constexpr int STREAM_CONSUMERS = 256;       // streamed kernel: consumer threads per CTA
 
 // One planned launch of a canonical problem C[s, j] = sum_i A[s, i, j] b[i],
 // A dense (S, nq, P) row-major, C dense (S, P).
@@ -28,7 +30,14 @@ struct Plan {
     int grid = 1;
     size_t smem = 0;
     bool f64_combine = false;    // combine split partials in fp64 (fp32 storage, nq > 2^20)
+    // streamed kernel (kind == KIND_STREAM): A as rows of L elements, R rows per chunk
+    int stream_col = 0;          // 0: row form (P == 1), 1: column form
+    uint64_t L = 0, R = 0, units = 0, units_per_cta = 0;
+    int RG = 1, J = 1;
 };
+
+// Whether the streamed kernel can take a problem (whole rows fit a stage).
+bool stream_eligible(int dtype, uint64_t P, uint64_t nq);
 
 struct KArgs {
     const void* a;
@@ -50,6 +59,9 @@ size_t partial_bytes(const Plan& p);
 // launch error.  Adds the number of launched kernels to *launches.
 cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c, void* partial,
                         cudaStream_t stream, uint64_t* launches);
+
+// Second phase of a split plan: C[o] = sum over segments of the partials.
+cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_t stream, uint64_t* launches);
 
 // Dynamic shared memory and the occupancy-derived CTAs per SM of a plan's
 // main kernel (cached per instantiation).
