@@ -136,10 +136,13 @@ def test_metadata_helpers_match_reference(engine):
 
 
 def test_planner_kernel_family(engine):
-    # whole rows of the canonical view within a 16 KB stage -> the streamed kernel
+    # q-fastest rows within a 16 KB stage -> the streamed kernel (row form)
     assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_STREAM
-    assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_STREAM
-    assert engine.plan(2, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_STREAM
+    assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_STREAM
+    assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_COL
+    # its column form on request
+    assert engine.plan(2, [645, 645, 645], [1, 2, 3], kind=engine.KIND_STREAM)["kind"] == \
+        engine.KIND_STREAM
     # long rows: the register kernels (q fastest -> row kernel, else column kernel)
     assert engine.plan(1, [16384, 16384], [1, 2])["kind"] == engine.KIND_ROW
     assert engine.plan(2, [16384, 16384], [1, 2])["kind"] == engine.KIND_COL
@@ -160,7 +163,7 @@ def test_planner_kernel_family(engine):
     # long contraction with a thin prefix is split, and segments fit the staged b
     pl = engine.plan(2, [64, 1 << 22], [1, 2], kind=Cn)
     assert pl["split"] >= (1 << 22) // 4096
-    assert engine.plan(2, [64, 1 << 22], [1, 2])["split"] > 1   # streamed: split to fill the GPU
+    assert engine.plan(2, [64, 1 << 22], [1, 2], kind=engine.KIND_STREAM)["split"] > 1
     # forced options are honoured or refused
     assert engine.plan(2, [256, 256, 256], [1, 2, 3], kind=Cn, group=2, split=3)["group"] == 2
     with pytest.raises(engine.TTVError):

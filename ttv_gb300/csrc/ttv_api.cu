@@ -359,7 +359,9 @@ int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tl
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
     const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
-    if ((opt && opt->kind == KIND_STREAM) || (eligible && !(opt && opt->kind >= 0)))
+    // default: the streamed kernel for q-fastest rows that fit a stage (its column form
+    // stays available on request); the register kernels for everything else
+    if ((opt && opt->kind == KIND_STREAM) || (eligible && cn.P == 1 && !(opt && opt->kind >= 0)))
         return make_stream_plan(pl, cn, opt, sms, out);
     const int vmax = (int)(16 / ea);
 

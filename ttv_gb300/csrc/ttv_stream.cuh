@@ -201,8 +201,17 @@ __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
                 Acc<T, KAHAN> acc;
                 acc.init();
                 if (valid) {
+                    // each group starts its walk at a row-dependent offset, so groups reading
+                    // rows a power-of-two apart do not land on the same shared-memory banks
                     const TA* rp = rows + rr * k.L;
-                    for (uint64_t e = gl; e < k.L; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
+                    const uint64_t rot = ((r0 + rr) * G) % k.L;
+                    uint64_t e = gl + rot;
+                    if (e >= k.L) e -= k.L;
+                    for (uint64_t t = gl; t < k.L; t += G) {
+                        acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
+                        e += G;
+                        if (e >= k.L) e -= k.L;
+                    }
                 }
                 for (uint32_t off = G >> 1; off > 0; off >>= 1) {
                     const T os = __shfl_xor_sync(0xffffffffu, acc.s, off);
