@@ -192,6 +192,7 @@ typedef struct tlibg_batch_options {
     int accumulate;        /* TLIBG_ACC_*                                                     */
     int no_graph;          /* nonzero: launch the kernels directly instead of a CUDA graph    */
     const int* variants;   /* one per problem (TLIBG_SELECT_GIVEN), or NULL                   */
+    int record_costs;      /* nonzero: the executor sums each problem's SM clock cycles       */
 } tlibg_batch_options;
 
 typedef struct tlibg_batch tlibg_batch;
@@ -206,6 +207,10 @@ int tlibg_batch_launch(tlibg_batch* batch, void* stream);
 /* Changes the forced variant of a TLIBG_SELECT_FIXED batch created with
  * no_graph (the autotuner's loop over variants). */
 int tlibg_batch_set_variant(tlibg_batch* batch, int variant);
+/* SM clock cycles each problem's work units took in the last launch of a
+ * batch created with record_costs (the autotuner's per-problem cost inside
+ * a mixed batch; synchronises). */
+int tlibg_batch_costs(tlibg_batch* batch, uint64_t* cycles, void* stream);
 /* The variant each problem ran with in the last launch (synchronises). */
 int tlibg_batch_variants(tlibg_batch* batch, int* out, void* stream);
 int tlibg_batch_destroy(tlibg_batch* batch);

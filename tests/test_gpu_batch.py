@@ -155,3 +155,26 @@ def test_one_shot_and_errors(engine, orc, cuda):
         B.Batch([probs[1], bad])
     with pytest.raises(engine.TTVError, match="variant must be in 0..7"):
         B.Batch(probs, select=B.SELECT_FIXED, variant=9)
+
+
+def test_recorded_costs(engine, orc, cuda):
+    """A recording batch returns every problem's SM cycles and the same results."""
+    import torch
+    from ttv_gb300 import batch as B
+    probs, host = make_batch(torch, cuda, 64, seed=14)
+    with B.Batch(probs, select=B.SELECT_FIXED, variant=0, no_graph=True,
+                 record_costs=True) as bt:
+        bt.launch()
+        torch.cuda.synchronize()
+        c1 = bt.costs()
+        check_all(orc, probs, host)
+        reset(probs)
+        bt.set_variant(2)
+        bt.launch()
+        torch.cuda.synchronize()
+        c2 = bt.costs()
+        check_all(orc, probs, host)
+    assert (c1 > 0).all() and (c2 > 0).all()
+    with B.Batch(probs) as bt:   # not recording: costs stay zero
+        bt.launch()
+        assert (bt.costs() == 0).all()

@@ -382,3 +382,30 @@ def test_launch_counter(engine, torch_dev):
     engine.ttv(q, 2, torch.ones(1024, device=dev), na, wa, pia, torch.ones(32, device=dev), [32],
                torch.empty(32, device=dev), nc, wc, pic, sync=True)
     assert engine.launch_count() > before
+
+
+def test_fp64_emulation_window_and_fallback(engine, orc, torch_dev):
+    """fp64 calls accumulate in double-float on the FP32/INT32 pipes when every
+    exponent is inside [2^-60, 2^61) and fall back to native DFMA outside it:
+    wide-range values, zeros and subnormals, every kernel family, against the
+    oracle (1e-13) and against the native-DFMA mode."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(64)
+    for na, pia, q in (([300, 200, 50], [1, 2, 3], 2), ([64, 48, 300], [1, 2, 3], 1),
+                       ([2000, 400], [2, 1], 2), ([16, 4096, 8], [1, 2, 3], 2)):
+        N = int(np.prod(na))
+        a = rng.uniform(-1, 1, N) * 10.0 ** rng.uniform(-40, 40, N)
+        a[rng.integers(0, N, N // 50)] = 0.0
+        a[rng.integers(0, N, N // 100)] = 5e-310                      # subnormal
+        b = rng.uniform(-1, 1, na[q - 1]) * 10.0 ** rng.uniform(-5, 5, na[q - 1])
+        P, nq, S = orc.canonical(na, pia, q)
+        truth = orc.truth(S, nq, P, a, b)
+        for kind in (-1, engine.KIND_ROW if P == 1 else engine.KIND_COL):
+            c_emu, _ = check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind)
+            c_nat, _ = check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
+                             accumulate=engine.ACC_PLAIN)
+        # in-window data: emulated and native agree to the double-float error
+        a2 = rng.uniform(-1, 1, N)
+        truth2 = orc.truth(S, nq, P, a2, b)
+        c_emu, e_emu = check(orc, engine, torch, dev, q, na, pia, a2, b, truth=truth2)
+        assert e_emu <= 1e-13

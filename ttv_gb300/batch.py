@@ -37,7 +37,8 @@ class _Problem(C.Structure):
 
 class _BatchOptions(C.Structure):
     _fields_ = [("select", C.c_int), ("variant", C.c_int), ("accumulate", C.c_int),
-                ("no_graph", C.c_int), ("variants", C.POINTER(C.c_int))]
+                ("no_graph", C.c_int), ("variants", C.POINTER(C.c_int)),
+                ("record_costs", C.c_int)]
 
 
 _bound = False
@@ -54,6 +55,7 @@ def _lib():
         L.tlibg_batch_launch.argtypes = [_vp, _vp]
         L.tlibg_batch_variants.argtypes = [_vp, C.POINTER(C.c_int), _vp]
         L.tlibg_batch_set_variant.argtypes = [_vp, C.c_int]
+        L.tlibg_batch_costs.argtypes = [_vp, C.POINTER(C.c_uint64), _vp]
         L.tlibg_batch_destroy.argtypes = [_vp]
         L.tlibg_ttv_batch.argtypes = [C.c_int, P, C.c_size_t, C.POINTER(_BatchOptions), _vp]
         L.tlibg_ttv_percall.argtypes = [C.c_int, P, C.c_size_t, _vp]
@@ -103,9 +105,9 @@ def _array(problems):
     return arr
 
 
-def _opts(select, variant, accumulate, no_graph, variants):
+def _opts(select, variant, accumulate, no_graph, variants, record=False):
     keep = None
-    o = _BatchOptions(select, variant, accumulate, int(bool(no_graph)), None)
+    o = _BatchOptions(select, variant, accumulate, int(bool(no_graph)), None, int(bool(record)))
     if variants is not None:
         keep = (C.c_int * len(variants))(*[int(v) for v in variants])
         o.variants = C.cast(keep, C.POINTER(C.c_int))
@@ -116,10 +118,11 @@ class Batch:
     """Descriptors of many problems plus the CUDA graph of one launch."""
 
     def __init__(self, problems, select=SELECT_HEURISTIC, variant=0, accumulate=0,
-                 no_graph=False, variants=None, stream=None):
+                 no_graph=False, variants=None, stream=None, record_costs=False):
         self.problems = list(problems)
         self._arr = _array(self.problems)
-        self._opt, self._vkeep = _opts(select, variant, accumulate, no_graph, variants)
+        self._opt, self._vkeep = _opts(select, variant, accumulate, no_graph, variants,
+                                       record_costs)
         h = _vp()
         st = _lib().tlibg_batch_create(0, self._arr, len(self.problems), C.byref(self._opt),
                                        _stream(stream), C.byref(h))
@@ -132,6 +135,13 @@ class Batch:
     def set_variant(self, v):
         """Change the forced variant of a SELECT_FIXED batch built with no_graph."""
         _raise(_lib().tlibg_batch_set_variant(self._h, int(v)))
+
+    def costs(self, stream=None):
+        """SM clock cycles of each problem in the last launch (record_costs batches)."""
+        out = np.zeros(len(self.problems), np.uint64)
+        _raise(_lib().tlibg_batch_costs(self._h, out.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                        _stream(stream)))
+        return out
 
     def variants(self, stream=None):
         out = (C.c_int * len(self.problems))()

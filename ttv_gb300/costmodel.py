@@ -5,10 +5,11 @@
 1. ``random_shapes`` draws batched-TTV problems: order p uniform in {3,4,5},
    every extent log-uniform in [8, 512] (rounded), re-drawn until the problem
    has at most 2^22 elements, a random contraction mode and a random layout.
-2. ``tune`` times every kernel variant of each shape exhaustively: K copies
-   of the shape (K x bytes ~ 256 MB, 32 <= K <= 4096) run as one persistent
-   batch with that variant forced, L2 flushed before each timed launch,
-   CUDA-event timed; cost = time / K (microseconds per problem).
+2. ``tune_mixed`` times every kernel variant of each shape exhaustively inside
+   mixed batches (random sizes 64..4096): each batch runs once per forced
+   variant, L2 flushed before each recorded launch, and the persistent
+   executor sums every problem's SM clock cycles; cost = microseconds per
+   problem.  (``tune``: the older K-copies method, launch time / K.)
 3. ``train`` fits the MLP (features + one-hot variant -> log2 cost) with the
    engine's own CUDA forward/backward/Adam kernels.
 4. ``evaluate`` measures regret against exhaustive tuning on held-out shapes,
@@ -113,6 +114,66 @@ def tune(shapes, reps=2, log_every=500, flush_bytes=256 << 20):
     return feats, times, heur
 
 
+def tune_mixed(shapes, seed=0, reps=2, lo=64, hi=4096, log_every=5000,
+               flush_bytes=256 << 20, arena_elems=3 << 30):
+    """Exhaustive timing of every variant of every shape inside mixed batches.
+
+    Shapes are taken in consecutive batches whose sizes are drawn log-uniformly in
+    [lo, hi]; each batch runs once per variant with that variant forced on every
+    problem, L2 flushed before each recorded launch, and the executor sums each
+    problem's SM clock cycles (``Batch.costs``).  Cost = min over reps, in
+    microseconds at the 2070 MHz maximum SM clock.  The batch-size feature is the
+    size of the batch the problem was timed in."""
+    import torch
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(seed)
+    A = torch.empty(arena_elems, device=dev)
+    A.uniform_(-1, 1)
+    b = torch.rand(1024, device=dev) * 2 - 1
+    C = torch.empty(arena_elems // 8, device=dev)
+    flush = torch.empty(flush_bytes // 4, device=dev)
+    feats = np.zeros((len(shapes), B.MLP_FEATURES), np.float32)
+    times = np.zeros((len(shapes), B.NVARIANT), np.float32)
+    heur = np.zeros(len(shapes), np.int32)
+    batch_of = np.zeros(len(shapes), np.int32)
+    t0 = time.time()
+    i = nb = 0
+    while i < len(shapes):
+        want = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        chunk, tot_a, tot_c = [], 0, 0
+        for sh in shapes[i:i + want]:
+            N = int(np.prod(sh[0]))
+            na_a = (N + 63) // 64 * 64
+            na_c = (N // sh[0][sh[2] - 1] + 63) // 64 * 64
+            if tot_a + na_a > A.numel() or tot_c + na_c > C.numel():
+                break
+            chunk.append(sh)
+            tot_a += na_a
+            tot_c += na_c
+        idx = np.arange(i, i + len(chunk))
+        probs = problems_from_arena([(sh, 1) for sh in chunk], A, b, C)
+        f, _kind, h = B.features(probs)
+        feats[idx], heur[idx], batch_of[idx] = f, h, nb
+        with B.Batch(probs, select=B.SELECT_FIXED, variant=0, no_graph=True,
+                     record_costs=True) as bt:
+            for v in range(B.NVARIANT):
+                bt.set_variant(v)
+                bt.launch()
+                best = None
+                for _ in range(reps):
+                    flush.zero_()
+                    bt.launch()
+                    c = bt.costs().astype(np.float64)
+                    best = c if best is None else np.minimum(best, c)
+                times[idx, v] = best / 2070.0
+        i += len(chunk)
+        nb += 1
+        if log_every and i // log_every != (i - len(chunk)) // log_every:
+            print(f"tuned {i}/{len(shapes)} shapes in {nb} mixed batches, {time.time() - t0:.0f} s",
+                  flush=True)
+    return feats, times, heur
+
+
 def training_set(feats, times):
     x = B.mlp_inputs(feats)
     y = np.log2(np.maximum(times, 1e-3)).ravel().astype(np.float32)
@@ -153,6 +214,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--out", default=DATA)
     ap.add_argument("--reuse-db", action="store_true", help="train on an existing tuning_db.npz")
+    ap.add_argument("--mode", choices=["mixed", "copies"], default="mixed",
+                    help="mixed: per-problem cycles inside mixed batches (default); copies: K "
+                         "copies of each shape, launch time / K")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     db_path = os.path.join(args.out, "tuning_db.npz")
@@ -162,7 +226,10 @@ def main():
     else:
         shapes = random_shapes(args.train + args.test, args.seed)
         t0 = time.time()
-        feats, times, heur = tune(shapes)
+        if args.mode == "mixed":
+            feats, times, heur = tune_mixed(shapes, seed=args.seed)
+        else:
+            feats, times, heur = tune(shapes)
         print(f"tuning: {time.time() - t0:.1f} s for {len(shapes)} shapes x {B.NVARIANT} variants")
         split = np.zeros(len(shapes), bool)
         split[args.train:] = True

@@ -349,7 +349,8 @@ int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tl
     pl.P = cn.P;
     pl.nq = cn.nq;
     pl.S = cn.S;
-    pl.kahan = (dtype == F64) ? 0 : ((opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1);
+    // compensated: fp32 Kahan, fp64 double-float emulation; plain: fp32 FMA, fp64 DFMA
+    pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
     pl.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
     const bool eligible = stream_eligible(dtype, cn.P, cn.nq);
     if (opt && opt->kind == KIND_STREAM && !eligible)

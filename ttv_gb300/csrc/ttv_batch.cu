@@ -54,11 +54,13 @@ struct BProb {
     uint32_t units;
     uint32_t valid_mask;
     unsigned int done;
+    unsigned long long cycles;   // SM clock cycles spent on this problem's units (recording launches)
 };
 
 struct BCtl {
     unsigned long long head;
     unsigned long long total;
+    int record;                  // nonzero: accumulate per-problem unit cycles
 };
 
 constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
@@ -172,6 +174,7 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
             P.seg_len = seg_len;
             P.units = (uint32_t)u;
             P.done = 0u;
+            P.cycles = 0ull;
             pe = nseg > 1 ? (unsigned long long)nseg * P.S * P.P : 0ull;
         }
         // inclusive warp scans, then across warps
@@ -421,6 +424,8 @@ __global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, cons
         fence_mbar_init();
     }
     const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total);
+    const int record = *reinterpret_cast<volatile int*>(&ctl->record);
+    long long t_unit = 0;
     unsigned long long next = 0;
     if (threadIdx.x == 0) next = atomicAdd(&ctl->head, 1ull);
     uint32_t phase = 0;
@@ -437,6 +442,7 @@ __global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, cons
         __syncthreads();
         const unsigned long long u = s_unit;
         if (u >= total) break;
+        if (record && threadIdx.x == 0) t_unit = clock64();
         const BProb& P = pr[s_prob];
         const uint64_t lu = u - P.unit_begin;
         bool ok = true;
@@ -468,6 +474,8 @@ __global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, cons
             }
         }
         __syncthreads();
+        if (record && threadIdx.x == 0)
+            atomicAdd(&pr[s_prob].cycles, (unsigned long long)(clock64() - t_unit));
     }
 }
 
@@ -740,6 +748,8 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         return create_fail(bt, TLIBG_ERR_NOMEM, std::string("tlibg_batch_create: ") + cudaGetErrorString(e));
     }
     cudaMemcpyAsync(bt->d_prob, hp.data(), count * sizeof(BProb), cudaMemcpyHostToDevice, st);
+    BCtl hctl{0ull, 0ull, (opt && opt->record_costs) ? 1 : 0};
+    cudaMemcpyAsync(bt->d_ctl, &hctl, sizeof(BCtl), cudaMemcpyHostToDevice, st);
     if (!model.empty() && bt->select == TLIBG_SELECT_LEARNED)
         cudaMemcpyAsync(bt->d_model, model.data(), MLP_PARAMS * sizeof(float), cudaMemcpyHostToDevice, st);
     bt->grid = sms * exec_ctas_per_sm(bt->kahan);
@@ -815,6 +825,18 @@ int tlibg_batch_variants(tlibg_batch* bt, int* out, void* stream)
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return internal_cuda_fail(e, "tlibg_batch_variants");
     for (int i = 0; i < bt->count; ++i) out[i] = hp[i].variant;
+    return internal_ok();
+}
+
+int tlibg_batch_costs(tlibg_batch* bt, uint64_t* cycles, void* stream)
+{
+    if (!bt || !cycles) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_costs: null argument");
+    std::vector<BProb> hp(bt->count);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(hp.data(), bt->d_prob, bt->count * sizeof(BProb), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return internal_cuda_fail(e, "tlibg_batch_costs");
+    for (int i = 0; i < bt->count; ++i) cycles[i] = hp[i].cycles;
     return internal_ok();
 }
 

@@ -90,6 +90,95 @@ template <typename T, bool KAHAN> struct Acc {
         }
     }
     __device__ __forceinline__ T value() const { return KAHAN ? (s - c) : s; }
+    __device__ __forceinline__ void fold() {}
+};
+
+// --------------------------------------------------------------------------
+// fp64 products accumulated on the FP32 / INT32 pipes.
+//
+// GB300 executes about two DFMA per SM per clock (1.25 TFLOP/s), below the
+// one-per-element rate an HBM-bound fp64 TTV needs.  Each double x with
+// exponent in [2^-60, 2^61) is split exactly into x = hi + lo, hi = x cut to
+// its top 24 significand bits, lo = the remaining 29 bits scaled (integer
+// ops, one int->float conversion, one power-of-two multiply).  The product
+// a*b = hi_a*hi_b + (hi_a*lo_b + lo_a*hi_b + lo_a*lo_b) keeps hi_a*hi_b
+// exact through Dekker's TwoProduct (one FMA gives its rounding error) and
+// the small terms in fp32; the running sum is a double-float (hi, lo) updated
+// with Knuth's TwoSum and a fast renormalisation.  Relative error per product
+// about 2^-47, per addition about 2^-47 of the sum.  Elements outside the
+// exponent window (and non-finite or subnormal ones) take a native DFMA into
+// a separate double accumulator.  fold() turns the state into one double, in
+// `s`, before any cross-lane or cross-warp reduction.
+// --------------------------------------------------------------------------
+struct DSplit {
+    float hi, lo;
+    bool ok;
+};
+
+__device__ __forceinline__ DSplit split_double(double x)
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi32 = (uint32_t)(bits >> 32), lo32 = (uint32_t)bits;
+    const uint32_t e = (hi32 >> 20) & 0x7ffu;
+    const uint32_t sign = hi32 & 0x80000000u;
+    DSplit r;
+    const bool zero = ((hi32 & 0x7fffffffu) | lo32) == 0u;
+    r.ok = zero || (e >= 1023u - 60u && e <= 1023u + 60u);
+    const uint32_t m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+    const uint32_t ee = r.ok && !zero ? e : 1023u;   // keep the bit patterns below well formed
+    r.hi = zero ? 0.f : __uint_as_float(sign | ((ee - 1023u + 127u) << 23) | m23);
+    const float rest = (float)(lo32 & 0x1fffffffu);                    // low 29 significand bits
+    const float scale = __uint_as_float((ee - 1075u + 127u) << 23);    // 2^(e - 1075)
+    const float lo = rest * scale;
+    r.lo = zero ? 0.f : (sign ? -lo : lo);
+    return r;
+}
+
+struct AccDF {
+    double s, c;    // folded value (after fold()); c stays 0
+    float hi, lo;   // double-float running sum
+    double d;       // native DFMA accumulator for out-of-window elements
+    __device__ __forceinline__ void init()
+    {
+        s = 0.0;
+        c = 0.0;
+        hi = 0.f;
+        lo = 0.f;
+        d = 0.0;
+    }
+    __device__ __forceinline__ void add_split(const DSplit& a, const DSplit& b, double ad, double bd)
+    {
+        if (a.ok && b.ok) {
+            const float p = a.hi * b.hi;
+            const float pe = fmaf(a.hi, b.hi, -p);                              // exact error of p
+            const float t = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.lo, b.lo, pe)));
+            const float sum = hi + p;                                           // TwoSum(hi, p)
+            const float v = sum - hi;
+            float err = (hi - (sum - v)) + (p - v);
+            err += lo + t;
+            hi = sum + err;                                                     // renormalise
+            lo = err - (hi - sum);
+        } else {
+            d = fma(ad, bd, d);
+        }
+    }
+    __device__ __forceinline__ void fma_add(double a, double b) { add_split(split_double(a), split_double(b), a, b); }
+    __device__ __forceinline__ void fold()
+    {
+        s = ((double)hi + (double)lo) + d;
+        c = 0.0;
+    }
+    __device__ __forceinline__ void merge(double os, double) { s = s + os; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+// Accumulator of a kernel instantiation: fp32 plain / Kahan, fp64 native
+// DFMA (KAHAN == false) or double-float emulation (KAHAN == true).
+template <typename T, bool KAHAN> struct AccSel {
+    typedef Acc<T, KAHAN> type;
+};
+template <> struct AccSel<double, true> {
+    typedef AccDF type;
 };
 
 // --------------------------------------------------------------------------

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 namespace tlibg {
@@ -72,6 +73,21 @@ __device__ __forceinline__ void load_b(const T* p, T (&out)[V])
     }
 }
 
+// acc[v] += av[v] * bb for the V outputs of one thread; the double-float
+// accumulator splits the shared bb once.
+template <int V, typename AccT, typename T>
+__device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb)
+{
+    if constexpr (std::is_same<AccT, AccDF>::value) {
+        const DSplit bs = split_double(bb);
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].add_split(split_double(av[v]), bs, av[v], bb);
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
+    }
+}
+
 // --------------------------------------------------------------------------
 // row kernel: P == 1
 // --------------------------------------------------------------------------
@@ -91,7 +107,7 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
     for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
         const uint64_t item = wbase + lane / G;
         const bool valid = item < k.items;
-        Acc<T, KAHAN> acc[V];
+        typename AccSel<T, KAHAN>::type acc[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].init();
         uint64_t row = 0, seg = 0;
@@ -135,6 +151,8 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
                 acc[0].fma_add(av[0], __ldg(bp + e));
             }
         }
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].fold();
 #pragma unroll
         for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
         for (uint32_t off = G >> 1; off > 0; off >>= 1) {
@@ -206,7 +224,7 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
 
         const uint64_t o0 = tile * TO + (uint64_t(wo) * 32u + lane) * V;
         const bool valid = o0 < outputs;
-        Acc<T, KAHAN> acc[V];
+        typename AccSel<T, KAHAN>::type acc[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].init();
         if (valid) {
@@ -219,21 +237,17 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
 #pragma unroll
                 for (int u = 0; u < U; ++u) load_a<TA, T, V>(ap + (i + u * WI) * k.P, av[u]);
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const T bb = bs[i + u * WI];
-#pragma unroll
-                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
-                }
+                for (int u = 0; u < U; ++u) row_fma<V>(acc, av[u], bs[i + u * WI]);
             }
 #pragma unroll 4
             for (; i < ie; i += WI) {
                 T av[V];
                 load_a<TA, T, V>(ap + i * k.P, av);
-                const T bb = bs[i];
-#pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
+                row_fma<V>(acc, av, bs[i]);
             }
         }
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].fold();
         if (WI > 1) {
             // warps stacked along i hand their partials to warp row wi == 0
             const uint32_t slot = wo * 32u + lane;
@@ -364,6 +378,7 @@ static StreamFn stream_fn(const Plan& p)
         if (p.kahan) return col ? stream_kernel<float, float, true, true> : stream_kernel<float, float, true, false>;
         return col ? stream_kernel<float, float, false, true> : stream_kernel<float, float, false, false>;
     case F64:
+        if (p.kahan) return col ? stream_kernel<double, double, true, true> : stream_kernel<double, double, true, false>;
         return col ? stream_kernel<double, double, false, true> : stream_kernel<double, double, false, false>;
     case BF16A:
         if (p.kahan)
@@ -388,7 +403,8 @@ static KernelFn main_kernel(const Plan& p)
         return p.kahan ? pick_main<float, float, true>(p.kind, p.vec)
                        : pick_main<float, float, false>(p.kind, p.vec);
     case F64:
-        return pick_main<double, double, false>(p.kind, p.vec);
+        return p.kahan ? pick_main<double, double, true>(p.kind, p.vec)
+                       : pick_main<double, double, false>(p.kind, p.vec);
     case BF16A:
         return p.kahan ? pick_main<uint16_t, float, true>(p.kind, p.vec)
                        : pick_main<uint16_t, float, false>(p.kind, p.vec);

@@ -198,21 +198,19 @@ __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
             for (uint64_t rb = 0; rb < nrows; rb += ngrp) {   // warp-uniform trip count
                 const uint64_t rr = rb + grp;
                 const bool valid = rr < nrows;
-                Acc<T, KAHAN> acc;
+                typename AccSel<T, KAHAN>::type acc;
                 acc.init();
                 if (valid) {
-                    // each group starts its walk at a row-dependent offset, so groups reading
-                    // rows a power-of-two apart do not land on the same shared-memory banks
+                    // Power-of-two rows: each group starts at a row-dependent offset (a
+                    // multiple of G) and wraps, so groups reading rows a power of two apart
+                    // do not share shared-memory banks.  Other lengths walk straight.
                     const TA* rp = rows + rr * k.L;
-                    const uint64_t rot = ((r0 + rr) * G) % k.L;
-                    uint64_t e = gl + rot;
-                    if (e >= k.L) e -= k.L;
-                    for (uint64_t t = gl; t < k.L; t += G) {
-                        acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
-                        e += G;
-                        if (e >= k.L) e -= k.L;
-                    }
+                    const uint32_t Lr = (uint32_t)k.L;
+                    const uint32_t rot = (Lr & (Lr - 1)) == 0 ? (uint32_t)((rr * G) & (Lr - 1)) : 0u;
+                    for (uint32_t e = rot + gl; e < Lr; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
+                    for (uint32_t e = gl; e < rot; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
                 }
+                acc.fold();
                 for (uint32_t off = G >> 1; off > 0; off >>= 1) {
                     const T os = __shfl_xor_sync(0xffffffffu, acc.s, off);
                     const T oc = __shfl_xor_sync(0xffffffffu, acc.c, off);
@@ -233,7 +231,7 @@ __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
     const uint32_t rg = RG > 1 ? ct / (uint32_t)P : 0;
     const uint32_t j0 = RG > 1 ? ct % (uint32_t)P : ct;
     const bool active = RG > 1 ? (ct < RG * (uint32_t)P) : true;
-    Acc<T, KAHAN> acc[STREAM_MAXJ];
+    typename AccSel<T, KAHAN>::type acc[STREAM_MAXJ];
 #pragma unroll
     for (int jj = 0; jj < STREAM_MAXJ; ++jj) acc[jj].init();
     bool failed = false;   // after an expired wait: walk on (named barriers) without work
@@ -270,6 +268,8 @@ __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
             // item (s, segment) complete: reduce row groups in fixed order, write
             const uint64_t item = w.unit;
             const uint64_t seg = item - s * k.nseg;
+#pragma unroll
+            for (int jj = 0; jj < STREAM_MAXJ; ++jj) acc[jj].fold();
             if (RG > 1) {
                 T* red = sbuf;
                 if (active) {
