@@ -75,11 +75,18 @@ def asym_cases():
     return cases
 
 
+def precision_cases():
+    return [{"dtype": "f32", "na": [64, 1 << 22], "pia": [1, 2], "q": 2},
+            {"dtype": "f32", "na": [16, 1 << 20, 16], "pia": [1, 2, 3], "q": 2}]
+
+
 WORKLOADS = {
     "sym": (sym_cases, "symmetric sweep: p=2..7, n=floor(2^(28/p)), every q, first- and "
                        "last-order layouts, fp32+fp64 (108 TTVs of ~2^28 elements)"),
     "asym": (asym_cases, "asymmetric sweep: p=2..10, n1=2^(28-2(p-1)), n_k=4, every q, "
                          "first-order, fp32 (54 TTVs of 2^28 elements)"),
+    "precision": (precision_cases, "precision and long contraction: 64x2^22 and 16x2^20x16, "
+                                   "q=2, fp32"),
 }
 
 
@@ -183,6 +190,18 @@ def traffic_per_element(kernel):
     return None
 
 
+def aggregate(ms_total, bytes_step, steps, world, dist=None, device=None):
+    """Max of the timed region over ranks, and the whole-job throughput: every
+    rank processed bytes_step per step (replicas, no data-path collective)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(ms_total)], dtype=torch.float64,
+                         device=device if device is not None else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    return ms_total, world * bytes_step * steps / (ms_total / 1e3) / 1e9
+
+
 # --------------------------------------------------------------------------
 # the engine arm
 # --------------------------------------------------------------------------
@@ -267,13 +286,8 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         barrier()
     launches = T.launch_count() - launches0
-    ms_total = t0.elapsed_time(t1)
-    if dist is not None:
-        tt = torch.tensor([ms_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_total = float(tt.item())
     bytes_step = sum(p[3] for p in prepared)
-    value = world * bytes_step * K / (ms_total / 1e3) / 1e9
+    ms_total, value = aggregate(t0.elapsed_time(t1), bytes_step, K, world, dist, dev)
     ms_step = ms_total / K
 
     # per-kernel breakdown from the per-case events (same timed region)
@@ -409,6 +423,71 @@ def run_batched(T, torch, dev, args, n=4096, seed=4096):
     return res
 
 
+def run_precision(args):
+    """Precision and long contraction: 64 x 2^22 and 16 x 2^20 x 16 fp32, contraction over
+    the long mode, A = N(0,1) * 10^U(-3,3), b = U[-1,1]; fp32 compensated (default),
+    fp32 plain accumulation, bf16-stored A; error vs the oracle's fp64 truth and GB/s."""
+    import torch
+    import oracle
+    import ttv_gb300 as T
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(5)
+    problems = [([64, 1 << 22], [1, 2], 2), ([16, 1 << 20, 16], [1, 2, 3], 2)]
+    res = {}
+    tot = {"compensated": [0, 0.0], "plain": [0, 0.0], "bf16a": [0, 0.0]}
+    K = max(3, args.steps)
+    for na, pia, q in problems:
+        N = int(np.prod(na))
+        a = (rng.standard_normal(N) * 10.0 ** rng.uniform(-3, 3, N)).astype(np.float32)
+        b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)
+        P, nq, S = canonical({"na": na, "pia": pia, "q": q})
+        ref, absn = oracle.truth(S, nq, P, a, b)
+        wa = T.strides(na, pia)
+        nc, pic = T.output_shape(na, q), T.output_layout(pia, q)
+        wc = T.strides(nc, pic)
+        da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+        dab = torch.from_numpy(a).to(torch.bfloat16).to(dev).view(torch.int16)
+        dc = torch.empty(int(np.prod(nc)), device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        key = "x".join(str(n) for n in na)
+        res[key] = {}
+        for name, A_, dt, acc, nbytes in (("compensated", da, T.F32, T.ACC_COMPENSATED, 4 * N),
+                                          ("plain", da, T.F32, T.ACC_PLAIN, 4 * N),
+                                          ("bf16a", dab, T.BF16A, T.ACC_COMPENSATED, 2 * N)):
+            def call():
+                T.ttv(q, len(na), A_, na, wa, pia, db, [nq], dc, nc, wc, pic, dtype=dt,
+                      accumulate=acc)
+            for _ in range(3):
+                call()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(K):
+                call()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / K
+            algo = nbytes + 4 * int(np.prod(nc))
+            err = oracle.rel_error(dc.cpu().numpy(), ref, absn)
+            res[key][name] = {"max_rel_err": err, "GB/s": round(algo / ms / 1e6, 1),
+                              "ms": round(ms, 4)}
+            tot[name][0] += algo
+            tot[name][1] += ms
+    gbs = {k: round(v[0] / v[1] / 1e6, 1) for k, v in tot.items()}
+    peak, _ = measured_peak()
+    return {"metric": METRIC, "value": gbs["compensated"], "unit": "GB/s", "n_gpus": 1,
+            "steps": K, "warmup": 3, "ms_per_step": round(tot["compensated"][1], 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "precision and long contraction: 64x2^22 (q=2) and "
+                                   "16x2^20x16 (q=2), A = N(0,1)*10^U(-3,3), b = U[-1,1]",
+                       "l2": "inputs larger than L2 (no flush)"},
+            "roofline": {"bound": "hbm", "achieved": gbs["compensated"], "peak": peak,
+                         "unit": "GB/s", "frac": round(gbs["compensated"] / peak, 4)},
+            "variants_GBps": gbs, "precision": res,
+            "bars": {"fp32": 1e-5, "bf16a": "2e-3 vs the fp32 A (rounding of A: 2^-8 per element)"}}
+
+
 def accuracy_sample(T, torch, dev, A, Bv, Cv, prepared):
     """max rel error vs the oracle's fp64 truth on one case per order (fp32)."""
     import oracle
@@ -519,7 +598,7 @@ def run_reference(args):
     oracle.build(with_ref=False) if not os.path.exists(oracle.LIB_PATH) else None
     cases = WORKLOADS[args.workload][0]()
     # bounded per-step sample of the workload: every 3rd TTV of the sweep
-    sample = cases[::3]
+    sample = cases[::3] if len(cases) > 6 else cases
     data = cpu_inputs(sample)
     for _ in range(args.warmup):
         run_cpu_sweep(sample[:2], data, 1)
@@ -595,6 +674,10 @@ def main():
         print(json.dumps(run_reference(args)), flush=True)
         return
 
+    if args.workload == "precision":
+        if rank == 0:
+            print(json.dumps(run_precision(args)), flush=True)
+        return
     if world > 1:
         import torch
         import torch.distributed as dist

@@ -44,8 +44,9 @@ extern "C" {
 #define TLIBG_BF16A  2   /* A bfloat16 (raw 16-bit patterns), b and C float    */
 
 /* ---- accumulation ---- */
-#define TLIBG_ACC_COMPENSATED 0  /* fp32: per-thread Kahan partials (default)  */
-#define TLIBG_ACC_PLAIN       1  /* fp32: plain FMA accumulation               */
+#define TLIBG_ACC_COMPENSATED  0  /* fp32: per-thread Kahan partials (default); fp64: DFMA  */
+#define TLIBG_ACC_PLAIN        1  /* fp32: plain FMA accumulation; fp64: DFMA               */
+#define TLIBG_ACC_DOUBLE_FLOAT 2  /* fp64: double-float accumulation on the FP32/INT32 pipes */
 
 /* ---- kernel families chosen by the planner ---- */
 #define TLIBG_KIND_ROW 0   /* q is the fastest layout mode (prefix P == 1): lane-group dot products */
@@ -122,6 +123,11 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p,
  * except the one-time device-property query). */
 int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pia,
                const tlibg_options* opt, tlibg_plan_info* out);
+
+/* Installs autotuned options for canonical problems (type, P, n_q, S): later
+ * calls whose options leave every kernel choice to the planner (or pass NULL)
+ * use them.  opt == NULL removes the hint; with P = n_q = S = 0, all hints. */
+int tlibg_plan_hint(int dtype, uint64_t P, uint64_t nq, uint64_t S, const tlibg_options* opt);
 
 /* ---------------------------------------------------------------------------
  * Metadata helpers (host only, no device needed).

@@ -385,8 +385,8 @@ def test_launch_counter(engine, torch_dev):
 
 
 def test_fp64_emulation_window_and_fallback(engine, orc, torch_dev):
-    """fp64 calls accumulate in double-float on the FP32/INT32 pipes when every
-    exponent is inside [2^-60, 2^61) and fall back to native DFMA outside it:
+    """fp64 with ACC_DOUBLE_FLOAT accumulates in double-float on the FP32/INT32 pipes
+    when every exponent is inside [2^-60, 2^61) and falls back to native DFMA outside:
     wide-range values, zeros and subnormals, every kernel family, against the
     oracle (1e-13) and against the native-DFMA mode."""
     torch, dev = torch_dev
@@ -401,11 +401,12 @@ def test_fp64_emulation_window_and_fallback(engine, orc, torch_dev):
         P, nq, S = orc.canonical(na, pia, q)
         truth = orc.truth(S, nq, P, a, b)
         for kind in (-1, engine.KIND_ROW if P == 1 else engine.KIND_COL):
-            c_emu, _ = check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind)
-            c_nat, _ = check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
-                             accumulate=engine.ACC_PLAIN)
-        # in-window data: emulated and native agree to the double-float error
+            check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
+                  accumulate=engine.ACC_DOUBLE_FLOAT)
+            check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind)
+        # in-window data: the emulation stays within the fp64 bar
         a2 = rng.uniform(-1, 1, N)
         truth2 = orc.truth(S, nq, P, a2, b)
-        c_emu, e_emu = check(orc, engine, torch, dev, q, na, pia, a2, b, truth=truth2)
+        _, e_emu = check(orc, engine, torch, dev, q, na, pia, a2, b, truth=truth2,
+                         accumulate=engine.ACC_DOUBLE_FLOAT)
         assert e_emu <= 1e-13

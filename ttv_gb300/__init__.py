@@ -28,14 +28,14 @@ __all__ = [
     "TTVError", "UnsupportedError", "ttv", "ttv_ex", "ttv_host", "ttv_array", "ttvs", "plan",
     "output_shape", "output_layout", "strides", "k_order_layout", "inverse_mode",
     "library", "library_path", "launch_count", "device_error", "F32", "F64", "BF16A",
-    "ACC_COMPENSATED", "ACC_PLAIN", "KIND_ROW", "KIND_COL", "KIND_STREAM",
+    "ACC_COMPENSATED", "ACC_PLAIN", "ACC_DOUBLE_FLOAT", "KIND_ROW", "KIND_COL", "KIND_STREAM",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libttvgpu.so")
 
 F32, F64, BF16A = 0, 1, 2
-ACC_COMPENSATED, ACC_PLAIN = 0, 1
+ACC_COMPENSATED, ACC_PLAIN, ACC_DOUBLE_FLOAT = 0, 1, 2
 KIND_ROW, KIND_COL, KIND_STREAM = 0, 1, 2
 OK, ERR_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = range(6)
 

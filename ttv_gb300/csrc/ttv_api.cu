@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -341,16 +342,61 @@ int make_stream_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms
     return TLIBG_OK;
 }
 
+// Plan hints installed by the autotuner: (type, P, n_q, S) -> options used when
+// the caller leaves every kernel choice to the planner.
+std::mutex g_hint_mu;
+std::map<std::tuple<int, uint64_t, uint64_t, uint64_t>, tlibg_options> g_hints;
+
+bool default_choices(const tlibg_options* opt)
+{
+    return !opt || (opt->kind < 0 && opt->group == 0 && opt->vec == 0 && opt->split == 0 &&
+                    opt->accumulate == TLIBG_ACC_COMPENSATED);
+}
+
+int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
+                    int sms, Plan* out);
+
 int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
               int sms, Plan* out)
+{
+    if (default_choices(opt)) {
+        tlibg_options hinted;
+        bool found = false;
+        {
+            std::lock_guard<std::mutex> lk(g_hint_mu);
+            auto it = g_hints.find(std::make_tuple(dtype, cn.P, cn.nq, cn.S));
+            if (it != g_hints.end()) {
+                hinted = it->second;
+                found = true;
+            }
+        }
+        if (found) {
+            hinted.sync = opt ? opt->sync : 0;
+            Plan tmp;
+            // a hint that no longer applies (e.g. narrower alignment) falls back to the rules
+            if (make_plan_inner(dtype, cn, a, b, &hinted, sms, &tmp) == TLIBG_OK) {
+                *out = tmp;
+                return TLIBG_OK;
+            }
+        }
+    }
+    return make_plan_inner(dtype, cn, a, b, opt, sms, out);
+}
+
+int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
+                    int sms, Plan* out)
 {
     Plan pl;
     pl.dtype = dtype;
     pl.P = cn.P;
     pl.nq = cn.nq;
     pl.S = cn.S;
-    // compensated: fp32 Kahan, fp64 double-float emulation; plain: fp32 FMA, fp64 DFMA
-    pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
+    // fp32: Kahan unless plain is asked for; fp64: native DFMA unless the double-float
+    // emulation on the FP32/INT32 pipes is asked for (TLIBG_ACC_DOUBLE_FLOAT)
+    if (dtype == F64)
+        pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
+    else
+        pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
     pl.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
     const bool eligible = stream_eligible(dtype, cn.P, cn.nq);
     if (opt && opt->kind == KIND_STREAM && !eligible)
@@ -789,6 +835,20 @@ size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode)
             return r + 1;
         }
     return 0;
+}
+
+int tlibg_plan_hint(int dtype, uint64_t P, uint64_t nq, uint64_t S, const tlibg_options* opt)
+{
+    std::lock_guard<std::mutex> lk(g_hint_mu);
+    if (!opt) {
+        if (P == 0 && nq == 0 && S == 0) g_hints.clear();
+        else g_hints.erase(std::make_tuple(dtype, P, nq, S));
+        return ok();
+    }
+    if (dtype != F32 && dtype != F64 && dtype != BF16A)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg_plan_hint: unknown element type");
+    g_hints[std::make_tuple(dtype, P, nq, S)] = *opt;
+    return ok();
 }
 
 size_t tlibg_last_error(char* buf, size_t len)

@@ -73,15 +73,24 @@ __device__ __forceinline__ void load_b(const T* p, T (&out)[V])
     }
 }
 
-// acc[v] += av[v] * bb for the V outputs of one thread; the double-float
-// accumulator splits the shared bb once.
+// acc[v] += av[v] * bb for the V outputs of one thread.  With the fp64
+// double-float accumulator the work is mixed: half the products take a native
+// DFMA (even outputs, or even unrolled rows when V == 1) and half the FP32 /
+// INT32 emulation, so neither the FP64 pipe nor the issue slots alone bound
+// the kernel; the shared bb is split once.
 template <int V, typename AccT, typename T>
-__device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb)
+__device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, int u = 0)
 {
     if constexpr (std::is_same<AccT, AccDF>::value) {
         const DSplit bs = split_double(bb);
 #pragma unroll
-        for (int v = 0; v < V; ++v) acc[v].add_split(split_double(av[v]), bs, av[v], bb);
+        for (int v = 0; v < V; ++v) {
+            const bool native = V > 1 ? ((v & 1) == 0) : ((u & 1) == 0);
+            if (native)
+                acc[v].d = fma(av[v], bb, acc[v].d);
+            else
+                acc[v].add_split(split_double(av[v]), bs, av[v], bb);
+        }
     } else {
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
@@ -237,7 +246,7 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
 #pragma unroll
                 for (int u = 0; u < U; ++u) load_a<TA, T, V>(ap + (i + u * WI) * k.P, av[u]);
 #pragma unroll
-                for (int u = 0; u < U; ++u) row_fma<V>(acc, av[u], bs[i + u * WI]);
+                for (int u = 0; u < U; ++u) row_fma<V>(acc, av[u], bs[i + u * WI], u);
             }
 #pragma unroll 4
             for (; i < ie; i += WI) {
