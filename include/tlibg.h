@@ -129,6 +129,14 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
  * use them.  opt == NULL removes the hint; with P = n_q = S = 0, all hints. */
 int tlibg_plan_hint(int dtype, uint64_t P, uint64_t nq, uint64_t S, const tlibg_options* opt);
 
+/* Validation only: the checks of the compute entry points (ttv.h:64-89 and
+ * tensor_times_vector.h:147-168, in that order, same messages) on the metadata
+ * alone, with no data pointers, no device and no launch.  Lets a host wrapper
+ * that knows its buffers' sizes check them against the layout once the
+ * reference's own checks have passed. */
+int tlibg_validate(size_t q, size_t p, const size_t* na, const size_t* wa, const size_t* pia,
+                   const size_t* nb, const size_t* nc, const size_t* wc, const size_t* pic);
+
 /* ---------------------------------------------------------------------------
  * Metadata helpers (host only, no device needed).
  * Replace: detail::generate_output_shape (shape.h:103-158),
@@ -225,7 +233,9 @@ int tlibg_ttv_batch(int dtype, const tlibg_problem* probs, size_t count,
                     const tlibg_batch_options* opt, void* stream);
 /* The plain alternative: one tlibg_ttv_ex launch per problem, in order. */
 int tlibg_ttv_percall(int dtype, const tlibg_problem* probs, size_t count, void* stream);
-/* Cost-model features of each problem (TLIBG_MLP_FEATURES floats per problem),
+/* Cost-model features of each problem (TLIBG_MLP_FEATURES floats per problem:
+ * p/8, position of q in the layout/(p-1), log2 P/24, log2 n_q/24, log2 S/24,
+ * dtype (0 = fp32), log2 batch size/16, widest legal load/4),
  * its kernel family and the fixed rule's variant (kind / heuristic may be NULL). */
 int tlibg_batch_features(const tlibg_problem* probs, size_t count, float* feat, int* kind,
                          int* heuristic);
@@ -253,8 +263,10 @@ int tlibg_mlp_predict(const float* params, const float* x, size_t n, float* y, v
 int tlibg_mlp_train(float* params, float* m, float* v, const float* x, const float* y, size_t n,
                     int epochs, int batch, float lr, uint64_t seed, float* epoch_loss, void* stream);
 /* Installs (HOST array of TLIBG_MLP_PARAMS floats) or clears (NULL) the model
- * TLIBG_SELECT_LEARNED uses for batches created afterwards. */
-int tlibg_set_cost_model(const float* params, size_t count);
+ * TLIBG_SELECT_LEARNED uses for batches created afterwards.  A problem leaves
+ * the fixed rule's variant only when the model predicts the new one costs
+ * less than (1 - margin) of it. */
+int tlibg_set_cost_model(const float* params, size_t count, float margin);
 
 /* ---- diagnostics ---- */
 /* Copies the calling thread's last error text into buf (NUL-terminated,

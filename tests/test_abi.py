@@ -136,9 +136,15 @@ def test_metadata_helpers_match_reference(engine):
 
 
 def test_planner_kernel_family(engine):
-    # q-fastest rows within a 16 KB stage -> the streamed kernel (row form)
-    assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_STREAM
+    # q-fastest rows: aligned -> register row kernel; unaligned and within a 16 KB
+    # stage -> the streamed kernel (row form); long unaligned fp64 rows -> row kernel
+    assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
     assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_STREAM
+    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_STREAM
+    assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
+    # fp64 column kernel: the DFMA / double-float mix by default
+    assert engine.plan(2, [64, 32, 16], [1, 2, 3], dtype=engine.F64)["accumulate"] == \
+        engine.ACC_COMPENSATED
     assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_COL
     # its column form on request
     assert engine.plan(2, [645, 645, 645], [1, 2, 3], kind=engine.KIND_STREAM)["kind"] == \
@@ -223,3 +229,32 @@ def test_ttvs_contraction_order(engine, monkeypatch):
         engine.ttvs(1, A, B, "sideways")
     with pytest.raises(ValueError, match="number of input vectors"):
         engine.ttvs(1, A, B[:2])
+
+
+def test_validate_only_entry_point(engine):
+    """tlibg_validate runs the reference's checks on metadata alone."""
+    L, sz = engine.library(), engine._sizes
+    ok = [sz(v) for v in ([4, 5, 6], [1, 4, 20], [1, 2, 3], [5], [4, 6], [1, 4], [1, 2])]
+    assert L.tlibg_validate(2, 3, *[engine._p(k) for k in ok]) == 0
+    bad = list(ok)
+    bad[3] = sz([7])
+    assert L.tlibg_validate(2, 3, *[engine._p(k) for k in bad]) == 1
+    assert "contraction dimension of A and B are not equal" in engine._last_error()
+
+
+def test_undersized_tensors_are_refused_before_launch(engine):
+    """Tensors smaller than their layout addresses never reach a kernel; the
+    reference's own messages still come first."""
+    torch = pytest.importorskip("torch")
+    na, pia, q = [4, 5, 6], [1, 2, 3], 2
+    wa = engine.strides(na, pia)
+    nc, pic = engine.output_shape(na, q), engine.output_layout(pia, q)
+    wc = engine.strides(nc, pic)
+    a, b, c = torch.zeros(120), torch.zeros(5), torch.zeros(24)
+    for small in ("a", "b", "c"):
+        args = {"a": a, "b": b, "c": c}
+        args[small] = args[small][:-1]
+        with pytest.raises(engine.TTVError, match=f"buffer {small} holds"):
+            engine.ttv(q, 3, args["a"], na, wa, pia, args["b"], [5], args["c"], nc, wc, pic)
+    with pytest.raises(engine.TTVError, match="contraction dimension of A and B are not equal"):
+        engine.ttv(q, 3, a[:1], na, wa, pia, b, [4], c, nc, wc, pic)

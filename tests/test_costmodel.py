@@ -49,6 +49,7 @@ def test_features_and_fixed_rule_on_cpu(engine):
     f, kind, heur = B.features(probs)
     assert f.shape == (3, 8)
     # problem 0: P = 16, nq = 32, S = 64, q at layout position 1 of 0..2
+    # (fake pointers 256/512/1024 are 16-byte aligned and P % 4 == 0: loads of 4)
     np.testing.assert_allclose(f[0], [3 / 8, 0.5, 4 / 24, 5 / 24, 6 / 24, 0, np.log2(3) / 16, 1],
                                rtol=1e-6)
     assert list(kind) == [1, 0, 0]   # column, row (q first), row (q first in layout 3,2,1)
@@ -131,8 +132,9 @@ def test_learned_selection_beats_fixed_rule(engine, cuda):
     d = np.load(CM.DB_PATH)
     te = d["is_test"]
     feats, times, heur = d["features"][te], d["times"][te], d["heuristic"][te]
-    params = np.load(B.MODEL_PATH)["params"]
-    learned = CM.predict_variants(params, feats)   # the engine's inference kernel
+    m = np.load(B.MODEL_PATH)
+    params, margin = m["params"], (float(m["margin"]) if "margin" in m else 0.0)
+    learned = CM.predict_variants(params, feats, heur, margin)   # the engine's inference kernel
     r_learn, _ = CM.regret(times, learned)
     r_heur, _ = CM.regret(times, heur)
     assert r_learn < r_heur, (r_learn, r_heur)

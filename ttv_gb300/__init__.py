@@ -94,6 +94,8 @@ def library() -> C.CDLL:
         L.tlibg_ttv_ex.argtypes = [C.c_int] + sig + [C.POINTER(Options), _vp]
         L.tlibg_ttv_host.restype = C.c_int
         L.tlibg_ttv_host.argtypes = [C.c_int] + sig + [C.POINTER(Options)]
+        L.tlibg_validate.restype = C.c_int
+        L.tlibg_validate.argtypes = [_sz, _sz, _psz, _psz, _psz, _psz, _psz, _psz, _psz]
         L.tlibg_plan.restype = C.c_int
         L.tlibg_plan.argtypes = [C.c_int, _sz, _sz, _psz, _psz, C.POINTER(Options),
                                  C.POINTER(PlanInfo)]
@@ -183,6 +185,7 @@ def ttv(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, *, dtype=None, stream=None,
     if dtype is None:
         dtype = _dtype_of(a)
     keep = [_sizes(v) for v in (na, wa, pia, nb, nc, wc, pic)]
+    _check_buffers(dtype, q, p, keep, a, b, c)
     o = _options(**opts)
     st = library().tlibg_ttv_ex(dtype, q, p, _ptr(a), _p(keep[0]), _p(keep[1]), _p(keep[2]),
                                 _ptr(b), _p(keep[3]), _ptr(c), _p(keep[4]), _p(keep[5]),
@@ -192,6 +195,37 @@ def ttv(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, *, dtype=None, stream=None,
 
 
 ttv_ex = ttv
+
+_ELEM_BYTES = {F32: (4, 4, 4), F64: (8, 8, 8), BF16A: (2, 4, 4)}
+
+
+def _addressed(n, w):
+    """Elements a dense tensor with extents n and strides w spans (0 if empty)."""
+    if any(int(x) == 0 for x in n):
+        return 0
+    return 1 + sum((int(x) - 1) * int(s) for x, s in zip(n, w))
+
+
+def _check_buffers(dtype, q, p, keep, a, b, c):
+    """Refuse tensors smaller than the memory their layout addresses, before
+    any launch: the kernels trust the metadata as the reference does.  Runs
+    after the reference's own checks (same messages, same order) and only for
+    sized buffers (torch tensors); raw addresses are the caller's contract."""
+    bufs = [(name, t) for name, t in (("a", a), ("b", b), ("c", c)) if hasattr(t, "numel")]
+    if not bufs or dtype not in _ELEM_BYTES:
+        return
+    na, wa, pia, nb, nc, wc, pic = keep
+    if len(na) < p or len(wa) < p or len(nb) < 1 or (p > 1 and (len(nc) < p - 1 or len(wc) < p - 1)):
+        return   # malformed metadata: the C ABI reports it
+    _raise(library().tlibg_validate(q, p, _p(na), _p(wa), _p(pia), _p(nb), _p(nc), _p(wc), _p(pic)))
+    need = {"a": _addressed(na[:p], wa[:p]), "b": int(nb[0]),
+            "c": _addressed(nc[:p - 1], wc[:p - 1])}
+    esz = dict(zip("abc", _ELEM_BYTES[dtype]))
+    for name, t in bufs:
+        have = t.numel() * t.element_size()
+        if have < need[name] * esz[name]:
+            raise TTVError(f"tlibg: buffer {name} holds {have} bytes, its layout addresses "
+                           f"{need[name] * esz[name]}")
 
 
 def ttv_host(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, *, dtype=None, **opts):

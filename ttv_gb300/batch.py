@@ -16,8 +16,8 @@ import os
 
 import numpy as np
 
-from . import _last_error, _options, _p, _raise, _sizes, library, output_layout, output_shape, \
-    strides
+from . import F32, _check_buffers, _last_error, _options, _p, _raise, _sizes, library, \
+    output_layout, output_shape, strides
 
 SELECT_HEURISTIC, SELECT_LEARNED, SELECT_FIXED, SELECT_GIVEN = 0, 1, 2, 3
 NVARIANT = 8
@@ -69,7 +69,7 @@ def _lib():
         L.tlibg_mlp_predict.argtypes = [_vp, _vp, C.c_size_t, _vp, _vp]
         L.tlibg_mlp_train.argtypes = [_vp, _vp, _vp, _vp, _vp, C.c_size_t, C.c_int, C.c_int,
                                       C.c_float, C.c_uint64, fp, _vp]
-        L.tlibg_set_cost_model.argtypes = [fp, C.c_size_t]
+        L.tlibg_set_cost_model.argtypes = [fp, C.c_size_t, C.c_float]
         _bound = True
     return L
 
@@ -92,6 +92,7 @@ class Problem:
         wc = strides(nc, pic)
         self._keep = [_sizes(v) for v in (self.na, wa, self.pia, [self.na[self.q - 1]], nc, wc,
                                           pic)]
+        _check_buffers(F32, self.q, len(self.na), self._keep, a, b, c)
 
     def _struct(self):
         k = self._keep
@@ -198,22 +199,26 @@ def batch_device_error() -> int:
 # --------------------------------------------------------------------------
 # cost model
 # --------------------------------------------------------------------------
-def set_cost_model(params):
-    """Install (numpy float32 [9473]) or clear (None) the model SELECT_LEARNED uses."""
+def set_cost_model(params, margin=0.0):
+    """Install (numpy float32 [9473]) or clear (None) the model SELECT_LEARNED uses;
+    a problem leaves the fixed rule only for a predicted gain beyond ``margin``."""
     if params is None:
-        _raise(_lib().tlibg_set_cost_model(None, 0))
+        _raise(_lib().tlibg_set_cost_model(None, 0, 0.0))
         return
     p = np.ascontiguousarray(params, dtype=np.float32)
-    _raise(_lib().tlibg_set_cost_model(p.ctypes.data_as(C.POINTER(C.c_float)), p.size))
+    _raise(_lib().tlibg_set_cost_model(p.ctypes.data_as(C.POINTER(C.c_float)), p.size,
+                                       float(margin)))
 
 
 def load_cost_model(path=MODEL_PATH, install=True):
     """The committed trained weights (None if absent); installs them by default."""
     if not os.path.exists(path):
         return None
-    params = np.load(path)["params"].astype(np.float32)
+    d = np.load(path)
+    params = d["params"].astype(np.float32)
+    margin = float(d["margin"]) if "margin" in d else 0.0
     if install:
-        set_cost_model(params)
+        set_cost_model(params, margin)
     return params
 
 

@@ -190,11 +190,28 @@ def train(feats, times, epochs=60, batch=512, lr=2e-3, seed=0):
     return params.cpu().numpy(), losses
 
 
-def predict_variants(params, feats):
+def predict_scores(params, feats):
+    """Predicted log2 cost of every variant of every shape (the engine's inference kernel)."""
     import torch
     x = torch.from_numpy(B.mlp_inputs(feats)).cuda()
     pred = B.mlp_predict(torch.from_numpy(np.asarray(params, np.float32)).cuda(), x)
-    return pred.cpu().numpy().reshape(len(feats), B.NVARIANT).argmin(axis=1)
+    return pred.cpu().numpy().reshape(len(feats), B.NVARIANT)
+
+
+def choose(scores, heuristic, margin):
+    """The batch selection rule: argmin of the predicted cost, unless it does not beat
+    the fixed rule's variant by the relative margin."""
+    best = scores.argmin(axis=1)
+    idx = np.arange(len(scores))
+    keep = ~(scores[idx, best] < scores[idx, heuristic] + np.log2(1.0 - margin))
+    return np.where(keep, heuristic, best)
+
+
+def predict_variants(params, feats, heuristic=None, margin=0.0):
+    scores = predict_scores(params, feats)
+    if heuristic is None:
+        return scores.argmin(axis=1)
+    return choose(scores, heuristic, margin)
 
 
 def regret(times, chosen):
@@ -236,19 +253,31 @@ def main():
         np.savez_compressed(db_path, features=feats, times=times, heuristic=heur, is_test=split,
                             shapes=np.frombuffer(json.dumps(shapes).encode(), np.uint8))
     tr, te = ~split, split
+    # the last tenth of the training shapes picks the selection margin
+    tr_idx = np.where(tr)[0]
+    fit, val = tr_idx[: len(tr_idx) * 9 // 10], tr_idx[len(tr_idx) * 9 // 10:]
     t0 = time.time()
-    params, losses = train(feats[tr], times[tr], epochs=args.epochs, seed=args.seed)
+    params, losses = train(feats[fit], times[fit], epochs=args.epochs, seed=args.seed)
     t_train = time.time() - t0
-    learned = predict_variants(params, feats[te])
+    val_scores = predict_scores(params, feats[val])
+    margins = [0.0, 0.05, 0.1, 0.15, 0.2, 0.3, 0.5]
+    val_regret = {m: regret(times[val], choose(val_scores, heur[val], m))[0] for m in margins}
+    margin = min(margins, key=lambda m: val_regret[m])
+    learned = predict_variants(params, feats[te], heur[te], margin)
     r_learn = regret(times[te], learned)
+    r_argmin = regret(times[te], predict_variants(params, feats[te]))
     r_heur = regret(times[te], heur[te])
     r_fixed = {v: regret(times[te], np.full(te.sum(), v))[0] for v in range(B.NVARIANT)}
-    summary = {"train_shapes": int(tr.sum()), "test_shapes": int(te.sum()),
+    summary = {"train_shapes": int(len(fit)), "validation_shapes": int(len(val)),
+               "test_shapes": int(te.sum()),
                "train_seconds": round(t_train, 2), "final_loss": float(losses[-1]),
-               "regret_learned": r_learn, "regret_fixed_rule": r_heur,
-               "regret_single_variant": r_fixed,
-               "learned_picks_best": float(np.mean(learned == times[te].argmin(axis=1)))}
+               "margin": margin, "validation_regret_by_margin": val_regret,
+               "regret_learned": r_learn, "regret_learned_plain_argmin": r_argmin,
+               "regret_fixed_rule": r_heur, "regret_single_variant": r_fixed,
+               "learned_picks_best": float(np.mean(learned == times[te].argmin(axis=1))),
+               "learned_leaves_fixed_rule": float(np.mean(learned != heur[te]))}
     np.savez_compressed(os.path.join(args.out, "cost_model.npz"), params=params, losses=losses,
+                        margin=np.float32(margin),
                         summary=np.frombuffer(json.dumps(summary).encode(), np.uint8))
     print(json.dumps(summary))
 

@@ -394,10 +394,13 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     // fp32: Kahan unless plain is asked for; fp64: native DFMA unless the double-float
     // emulation on the FP32/INT32 pipes is asked for (TLIBG_ACC_DOUBLE_FLOAT)
     if (dtype == F64)
-        pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
+        pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1
+                   : (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0
+                   : (cn.P > 1 ? 1 : 0);   // default: the mix in the column kernel (measured faster)
     else
         pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
     pl.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
+    const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
     const bool eligible = stream_eligible(dtype, cn.P, cn.nq);
     if (opt && opt->kind == KIND_STREAM && !eligible)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: the streamed kernel needs whole rows of the canonical view "
@@ -405,10 +408,17 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
-    const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
-    // default: the streamed kernel for q-fastest rows that fit a stage (its column form
-    // stays available on request); the register kernels for everything else
-    if ((opt && opt->kind == KIND_STREAM) || (eligible && cn.P == 1 && !(opt && opt->kind >= 0)))
+    // default for q-fastest rows: the register row kernel when rows allow 16-byte loads;
+    // the streamed kernel (alignment-agnostic) for unaligned rows that fit a stage,
+    // except long fp64 rows, which the register kernel streams at the FP64 rate anyway.
+    // The streamed column form stays available on request.
+    bool rows_aligned = false;
+    {
+        const size_t vb = 16 / ea;
+        rows_aligned = cn.nq % vb == 0 && aligned(a, 16) && aligned(b, 16);
+    }
+    const bool stream_default = eligible && cn.P == 1 && !rows_aligned && !(dtype == F64 && cn.nq >= 256);
+    if ((opt && opt->kind == KIND_STREAM) || (stream_default && !(opt && opt->kind >= 0)))
         return make_stream_plan(pl, cn, opt, sms, out);
     const int vmax = (int)(16 / ea);
 
@@ -431,10 +441,16 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     const int force_split = opt ? opt->split : 0;
     const int force_group = opt ? opt->group : 0;
     if (pl.kind == KIND_ROW) {
+        // Lanes per row, measured on GB300: fp32 about 16 vector loads per lane (at least
+        // 2 lanes); fp64 up to 64 elements per lane so the shuffle-tree DADDs stay rare,
+        // but two lanes for rows of at most 8 vectors.
         const uint64_t nvec = cdiv(cn.nq, V);
-        const uint64_t vec_per_lane = dtype == F64 ? 16 : 4;   // fp64: keep shuffle-tree DADDs rare
-        int G = force_group > 0 ? force_group
-                                : std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / vec_per_lane)));
+        int Gdef;
+        if (dtype == F64)
+            Gdef = nvec <= 8 ? 2 : std::min(8, pow2_floor(std::max<uint64_t>(1, nvec / 64)));
+        else
+            Gdef = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / 16))));
+        int G = force_group > 0 ? force_group : Gdef;
         if (G < 1 || G > 32 || (G & (G - 1)))
             return fail(TLIBG_ERR_ARGUMENT, "tlibg: lanes per row must be a power of two in 1..32");
         pl.group = G;
@@ -467,19 +483,23 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         auto tiles_for = [&](int wi) { return cdiv(outputs, (uint64_t)((BLOCK / 32) / wi) * 32 * V); };
         pl.group = WI;
         int cps = std::max(1, plan_ctas_per_sm(pl));
-        const uint64_t want = (uint64_t)sms * cps * 8;   // items for good balance of the blocked split
+        // Measured on GB300 (tuner sweeps): one warp row per tile and no split are best
+        // whenever the tiles alone cover the grid; otherwise stack warps along q, then
+        // split q until about two items per CTA.
+        const uint64_t grid_full = (uint64_t)sms * cps;
         if (force_group <= 0) {
-            while (WI < 8 && tiles_for(WI) < want && cn.nq >= (uint64_t)WI * 2 * 4) WI *= 2;
+            while (WI < 8 && tiles_for(WI) < grid_full && cn.nq >= (uint64_t)WI * 2 * 4) WI *= 2;
             pl.group = WI;
             cps = std::max(1, plan_ctas_per_sm(pl));
         }
+        const uint64_t want = 2 * (uint64_t)sms * cps;
         const uint64_t tiles = tiles_for(WI);
         uint64_t nseg = cdiv(cn.nq, bmax);
         if (force_split > 0) {
             nseg = std::max<uint64_t>(nseg, (uint64_t)force_split);
             if ((uint64_t)force_split < cdiv(cn.nq, bmax))
                 return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced split leaves a segment longer than the staged b buffer");
-        } else if (tiles * nseg < want) {
+        } else if (tiles < (uint64_t)sms * cps && tiles * nseg < want) {
             const uint64_t min_len = (uint64_t)WI * 4 * 4;
             nseg = std::max<uint64_t>(nseg, std::min<uint64_t>(cdiv(want, tiles), std::max<uint64_t>(1, cn.nq / min_len)));
         }
@@ -607,6 +627,17 @@ int tlibg_ttv_ex(int dtype, size_t q, size_t p, const void* a, const size_t* na,
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: unknown element type");
     return run_device(dtype, q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, opt,
                       static_cast<cudaStream_t>(stream));
+}
+
+int tlibg_validate(size_t q, size_t p, const size_t* na, const size_t* wa, const size_t* pia,
+                   const size_t* nb, const size_t* nc, const size_t* wc, const size_t* pic)
+{
+    // the data pointers only take part in null checks: stand-ins let the
+    // metadata checks run in the reference's order without touching memory
+    static const char stand_in = 0;
+    Canon cn;
+    const int st = analyse(q, p, &stand_in, na, wa, pia, &stand_in, nb, &stand_in, nc, wc, pic, &cn);
+    return st ? st : ok();
 }
 
 int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pia,

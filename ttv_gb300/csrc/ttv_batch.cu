@@ -53,6 +53,7 @@ struct BProb {
     uint32_t nseg;
     uint32_t units;
     uint32_t valid_mask;
+    int heuristic;               // the fixed rule's variant (kept unless the model beats it by the margin)
     unsigned int done;
     unsigned long long cycles;   // SM clock cycles spent on this problem's units (recording launches)
 };
@@ -107,7 +108,7 @@ __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uin
 // selection: MLP score per (problem, variant), keep the argmin
 // --------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int n, const float* __restrict__ w,
-                                                    float log2_count)
+                                                    float log2_count, float log2_keep)
 {
     __shared__ float sw[MLP_PARAMS];
     for (int p = threadIdx.x; p < MLP_PARAMS; p += blockDim.x) sw[p] = w[p];
@@ -119,12 +120,14 @@ __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int 
         float x[MLP_IN];
 #pragma unroll
         for (int i = 0; i < NFEAT; ++i) x[i] = pr[pi].feat[i];
-        x[6] = log2_count / 16.f;
 #pragma unroll
         for (int i = 0; i < NVARIANT; ++i) x[NFEAT + i] = (i == v) ? 1.f : 0.f;
         score = mlp_forward<false>(sw, x, nullptr, nullptr, nullptr);
     }
     int best = v;
+    const int h = pi < n ? pr[pi].heuristic : 0;
+    // the fixed rule's predicted cost, broadcast within the problem's 8 lanes
+    const float h_score = __shfl_sync(0xffffffffu, score, (threadIdx.x & ~7u) + (unsigned)h);
     // argmin over the 8 lanes of this problem (ties: lowest variant)
 #pragma unroll
     for (int off = 4; off > 0; off >>= 1) {
@@ -135,7 +138,9 @@ __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int 
             best = ob;
         }
     }
-    if (pi < n && v == 0) pr[pi].variant = isinf(score) ? 0 : best;
+    // deviate from the fixed rule only for a predicted gain beyond the margin
+    if (pi < n && v == 0) pr[pi].variant = (isinf(score) || !(score < h_score + log2_keep)) ? h : best;
+    (void)log2_count;
 }
 
 __global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
@@ -486,6 +491,7 @@ namespace {
 
 std::mutex g_model_mu;
 std::vector<float> g_model;   // installed cost-model parameters (empty: none)
+float g_model_margin = 0.f;   // minimum predicted relative gain to leave the fixed rule
 
 size_t exec_smem_bytes()
 {
@@ -554,6 +560,7 @@ struct tlibg_batch {
     BPair* d_part = nullptr;
     float* d_model = nullptr;
     float log2_count = 0.f;
+    float log2_keep = 0.f;   // log2(1 - margin)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -565,7 +572,8 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
     uint64_t n = 0;
     if (bt->select == TLIBG_SELECT_LEARNED) {
         const int threads = bt->count * NVARIANT;
-        batch_select<<<(threads + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_model, bt->log2_count);
+        batch_select<<<(threads + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_model, bt->log2_count,
+                                                            bt->log2_keep);
         ++n;
     } else if (bt->select == TLIBG_SELECT_FIXED) {
         batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
@@ -612,13 +620,16 @@ int create_fail(tlibg_batch* bt, int code, const std::string& msg)
 
 extern "C" {
 
-int tlibg_set_cost_model(const float* params, size_t count)
+int tlibg_set_cost_model(const float* params, size_t count, float margin)
 {
     std::lock_guard<std::mutex> lk(g_model_mu);
     if (!params) {
         g_model.clear();
         return internal_ok();
     }
+    if (!(margin >= 0.f && margin < 1.f))
+        return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_set_cost_model: margin must be in [0, 1)");
+    g_model_margin = margin;
     if (count != (size_t)MLP_PARAMS)
         return internal_fail(TLIBG_ERR_ARGUMENT,
                              "tlibg_set_cost_model: expected " + std::to_string(MLP_PARAMS) + " parameters");
@@ -644,8 +655,8 @@ int tlibg_batch_features(const tlibg_problem* pr, size_t count, float* feat, int
         f[4] = (float)std::log2((double)cn.S) / 24.f;
         f[5] = 0.f;   // fp32
         f[6] = (float)std::log2((double)count) / 16.f;
-        f[7] = cn.P == 1 ? 0.f : 1.f;
         const int kd = cn.P == 1 ? KIND_ROW : KIND_COL;
+        f[7] = (float)batch_vec(kd, cn, x.a, x.b) / 4.f;   // widest legal load (alignment)
         if (kind) kind[i] = kd;
         if (heuristic) heuristic[i] = heuristic_variant(kd, cn.P, cn.nq, cn.S, batch_vec(kd, cn, x.a, x.b));
     }
@@ -689,6 +700,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
     if (bt->select == TLIBG_SELECT_LEARNED) {
         std::lock_guard<std::mutex> lk(g_model_mu);
         model = g_model;
+        bt->log2_keep = (float)std::log2(1.0 - (double)g_model_margin);
     }
     if (bt->select == TLIBG_SELECT_LEARNED && model.empty())
         // no model installed: exhaustive-tuning results when given, else the fixed rule
@@ -716,6 +728,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         std::copy(feat.begin() + i * NFEAT, feat.begin() + (i + 1) * NFEAT, b.feat);
         b.valid_mask = (1u << NVARIANT) - 1u;
         b.variant = heur[i];
+        b.heuristic = heur[i];
         if (bt->select == TLIBG_SELECT_GIVEN) {
             const int v = opt->variants[i];
             if (v < 0 || v >= NVARIANT)

@@ -126,6 +126,7 @@ def main():
     tdt = {"f32": torch.float32, "f64": torch.float64}
     maxN = max(int(np.prod(c["na"])) for c in cases)
     maxM = max(int(np.prod(c["na"])) // c["na"][c["q"] - 1] for c in cases)
+    maxQ = max(c["na"][c["q"] - 1] for c in cases)
     bufs = {}
     results = []
     tot_def = tot_best = 0.0
@@ -133,7 +134,7 @@ def main():
         dt = cs["dtype"]
         if dt not in bufs:
             bufs[dt] = (torch.rand(maxN, device=dev, dtype=tdt[dt]) * 2 - 1,
-                        torch.rand(1 << 15, device=dev, dtype=tdt[dt]) * 2 - 1,
+                        torch.rand(maxQ, device=dev, dtype=tdt[dt]) * 2 - 1,
                         torch.empty(maxM, device=dev, dtype=tdt[dt]))
         A, b, c = bufs[dt]
         code = F64 if dt == "f64" else F32
