@@ -51,6 +51,9 @@ extern "C" {
 /* ---- kernel families chosen by the planner ---- */
 #define TLIBG_KIND_ROW 0   /* q is the fastest layout mode (prefix P == 1): lane-group dot products */
 #define TLIBG_KIND_COL 1   /* q is a middle or outer mode: coalesced column GEMV over the prefix    */
+#define TLIBG_KIND_STREAM 2        /* TMA-streamed rows (whole rows of <= 16 KB), any alignment     */
+#define TLIBG_KIND_COL_REALIGN 3   /* column GEMV with 16-byte loads realigned by warp shuffles,    */
+                                   /*   for prefixes whose rows are not 16-byte aligned (fp32/fp64) */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */

@@ -152,7 +152,17 @@ def test_planner_kernel_family(engine):
     # long rows: the register kernels (q fastest -> row kernel, else column kernel)
     assert engine.plan(1, [16384, 16384], [1, 2])["kind"] == engine.KIND_ROW
     assert engine.plan(2, [16384, 16384], [1, 2])["kind"] == engine.KIND_COL
-    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL
+    # rows of the prefix not 16-byte aligned: shuffle-realigned loads once rows span 4 KB
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL_REALIGN
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == \
+        engine.KIND_COL_REALIGN
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["vec"] == 4
+    assert engine.plan(2, [25, 25, 25], [1, 2, 3])["kind"] == engine.KIND_COL
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.BF16A)["kind"] == engine.KIND_COL
+    assert engine.plan(2, [25, 25, 25], [1, 2, 3], kind=engine.KIND_COL_REALIGN)["kind"] == \
+        engine.KIND_COL_REALIGN
+    with pytest.raises(engine.TTVError, match="realigning column kernel"):
+        engine.plan(1, [25, 25, 25], [1, 2, 3], kind=engine.KIND_COL_REALIGN)
     # forced register kernels
     R, Cn = engine.KIND_ROW, engine.KIND_COL
     assert engine.plan(1, [64, 32, 16], [1, 2, 3], kind=R)["kind"] == R
@@ -258,3 +268,17 @@ def test_undersized_tensors_are_refused_before_launch(engine):
             engine.ttv(q, 3, args["a"], na, wa, pia, args["b"], [5], args["c"], nc, wc, pic)
     with pytest.raises(engine.TTVError, match="contraction dimension of A and B are not equal"):
         engine.ttv(q, 3, a[:1], na, wa, pia, b, [4], c, nc, wc, pic)
+
+
+def test_element_misaligned_pointers_refused(engine):
+    """Pointers not aligned to their element type never reach a kernel."""
+    sz = engine._sizes
+    meta = [sz(v) for v in ([4, 5, 6], [1, 4, 20], [1, 2, 3], [5], [4, 6], [1, 4], [1, 2])]
+    L = engine.library()
+    o = engine._options()
+    for dt, a, b, c in ((engine.F32, 18, 32, 64), (engine.F64, 20, 32, 64), (engine.F64, 64, 36, 64),
+                        (engine.F32, 64, 32, 66)):
+        st = L.tlibg_ttv_ex(dt, 2, 3, a, *[engine._p(k) for k in meta[:3]], b, engine._p(meta[3]), c,
+                            *[engine._p(k) for k in meta[4:]], C.byref(o), None)
+        assert st == engine.ERR_UNSUPPORTED, (dt, a, b, c, st)
+        assert "aligned to their element sizes" in engine._last_error()

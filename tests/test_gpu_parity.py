@@ -400,7 +400,8 @@ def test_fp64_emulation_window_and_fallback(engine, orc, torch_dev):
         b = rng.uniform(-1, 1, na[q - 1]) * 10.0 ** rng.uniform(-5, 5, na[q - 1])
         P, nq, S = orc.canonical(na, pia, q)
         truth = orc.truth(S, nq, P, a, b)
-        for kind in (-1, engine.KIND_ROW if P == 1 else engine.KIND_COL):
+        kinds = (-1, engine.KIND_ROW) if P == 1 else (-1, engine.KIND_COL, engine.KIND_COL_REALIGN)
+        for kind in kinds:
             check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
                   accumulate=engine.ACC_DOUBLE_FLOAT)
             check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind)
@@ -410,3 +411,47 @@ def test_fp64_emulation_window_and_fallback(engine, orc, torch_dev):
         _, e_emu = check(orc, engine, torch, dev, q, na, pia, a2, b, truth=truth2,
                          accumulate=engine.ACC_DOUBLE_FLOAT)
         assert e_emu <= 1e-13
+
+
+REALIGN_SHAPES = [
+    ([645, 33, 7], [1, 2, 3], 2),        # P = 645: windows straddle rows and slabs
+    ([1001, 9, 5], [1, 2, 3], 2),        # odd P, short contraction
+    ([2, 3, 1023, 5], [1, 2, 3, 4], 4),  # P = 6138 = 2 (mod 4)
+    ([25, 25, 25, 25], [1, 2, 3, 4], 3),  # P = 625, S = 25
+    ([7, 50, 3], [1, 2, 3], 2),          # P < one window: scalar path only
+    ([129, 5000, 2], [1, 2, 3], 2),      # long contraction: split b stages
+    ([1000, 17, 3], [1, 2, 3], 2),       # aligned P: misalignment 0 throughout
+    ([5, 3, 700], [3, 1, 2], 3),         # layout permuted: P = 700 * 5
+]
+
+
+@pytest.mark.parametrize("na,pia,q", REALIGN_SHAPES)
+def test_realigned_column_kernel(engine, orc, torch_dev, na, pia, q):
+    """The column kernel with shuffle-realigned 16-byte loads: every warp-row
+    count and split, A at element offsets 0-3, fp32 (compensated and plain) and
+    fp64 (native and double-float)."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(sum(na) * 7 + q)
+    P, nq, S = orc.canonical(na, pia, q)
+    wa, nc, wc, pic = meta(engine, na, pia, q)
+    N, M = int(np.prod(na)), int(np.prod(nc))
+    for dt in (np.float32, np.float64):
+        tdt = torch.float32 if dt == np.float32 else torch.float64
+        a = rng.uniform(-1, 1, N + 3).astype(dt)
+        b = rng.uniform(-1, 1, nq).astype(dt)
+        da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+        dc = torch.empty(M, dtype=tdt, device=dev)
+        bmax = 16384 // np.dtype(dt).itemsize
+        accs = (engine.ACC_COMPENSATED, engine.ACC_PLAIN) if dt == np.float32 else \
+            (engine.ACC_PLAIN, engine.ACC_DOUBLE_FLOAT)
+        for oa in (0, 1, 2, 3):
+            truth = orc.truth(S, nq, P, a[oa:oa + N], b)
+            for g, split, acc in itertools.product((1, 2, 4, 8), (0, 1, 3, 17), accs):
+                if (0 < split < -(-nq // bmax)) or split > nq:
+                    continue
+                dc.fill_(float("nan"))
+                engine.ttv(q, len(na), da[oa:oa + N], na, wa, pia, db, [nq], dc, nc, wc, pic,
+                           kind=engine.KIND_COL_REALIGN, group=g, split=split, accumulate=acc,
+                           sync=True)
+                err = orc.rel_error(dc.cpu().numpy(), *truth)
+                assert err <= TOL[dt], (na, pia, q, dt, oa, g, split, acc, err)

@@ -405,7 +405,12 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     if (opt && opt->kind == KIND_STREAM && !eligible)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: the streamed kernel needs whole rows of the canonical view "
                                         "(n_q when P == 1, else P) within one 16 KB stage");
-    if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != pl.kind)
+    const bool realign_ok = cn.P > 1 && dtype != BF16A;
+    if (opt && opt->kind == KIND_COL_REALIGN && !realign_ok)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the realigning column kernel needs prefix P > 1 and "
+                                        "fp32 or fp64 A");
+    if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
+        opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
     // default for q-fastest rows: the register row kernel when rows allow 16-byte loads;
@@ -431,10 +436,21 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
             return cn.nq % v == 0 && aligned(a, v * ea) && aligned(b, std::min<size_t>(16, v * et));
         return cn.P % v == 0 && aligned(a, v * ea);
     };
-    if (opt && opt->vec > 0) {
+    if (opt && opt->kind == KIND_COL_REALIGN) {
+        if (opt->vec > 0 && opt->vec != vmax)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: the realigning column kernel loads 16 bytes per vector");
+        V = vmax;
+        pl.kind = KIND_COL_REALIGN;
+    } else if (opt && opt->vec > 0) {
         if (!vec_ok(V)) return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced vector width violates alignment");
     } else {
         while (V > 1 && !vec_ok(V)) V /= 2;
+        // rows that are not 16-byte aligned and long enough that windows of 32
+        // vectors rarely straddle two rows: realigned 16-byte loads
+        if (V < vmax && realign_ok && !(opt && opt->kind >= 0) && cn.P * ea >= 4096) {
+            V = vmax;
+            pl.kind = KIND_COL_REALIGN;
+        }
     }
     pl.vec = V;
 
@@ -560,12 +576,23 @@ int get_scratch(cudaStream_t stream, size_t bytes, void** out)
     return TLIBG_OK;
 }
 
+// Every kernel addresses A, b and C per element (and wider): pointers must
+// be aligned to their element types, as a C or C++ caller's own are.
+int check_elem_align(int dtype, const void* a, const void* b, const void* c)
+{
+    if (!aligned(a, elem_size_a(dtype)) || !aligned(b, elem_size_t(dtype)) || !aligned(c, elem_size_t(dtype)))
+        return fail(TLIBG_ERR_UNSUPPORTED, "tlibg: a, b and c must be aligned to their element sizes");
+    return TLIBG_OK;
+}
+
 int run_device(int dtype, size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
                const size_t* pia, const void* b, const size_t* nb, void* c, const size_t* nc,
                const size_t* wc, const size_t* pic, const tlibg_options* opt, cudaStream_t stream)
 {
     Canon cn;
     int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
+    if (st) return st;
+    st = check_elem_align(dtype, a, b, c);
     if (st) return st;
     DevInfo d = dev_info();
     if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
@@ -956,6 +983,8 @@ extern "C" int tlibg_ttv_f32_noalloc(size_t q, size_t p, const float* a, const s
 {
     Canon cn;
     int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
+    if (st) return st;
+    st = check_elem_align(F32, a, b, c);
     if (st) return st;
     DevInfo d = dev_info();
     if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");

@@ -4,7 +4,8 @@
 // turned into device descriptors once (tlibg_batch_create).  Every launch is
 // one short sequence, captured in a CUDA graph and replayed:
 //
-//   batch_select  (learned mode) the cost-model MLP scores every kernel
+//   batch_select  (learned mode, once at creation: the scores depend only on
+//                 the descriptors) the cost-model MLP scores every kernel
 //                 variant of every problem and keeps the cheapest
 //   batch_plan    one CTA: decodes each problem's variant into work units,
 //                 prefix-sums units and split-partial offsets, fills the
@@ -570,12 +571,7 @@ namespace {
 int enqueue(tlibg_batch* bt, cudaStream_t st)
 {
     uint64_t n = 0;
-    if (bt->select == TLIBG_SELECT_LEARNED) {
-        const int threads = bt->count * NVARIANT;
-        batch_select<<<(threads + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_model, bt->log2_count,
-                                                            bt->log2_keep);
-        ++n;
-    } else if (bt->select == TLIBG_SELECT_FIXED) {
+    if (bt->select == TLIBG_SELECT_FIXED) {
         batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
         ++n;
     }
@@ -594,7 +590,7 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
 
 int launches_per_run(const tlibg_batch* bt)
 {
-    return (bt->select == TLIBG_SELECT_LEARNED || bt->select == TLIBG_SELECT_FIXED) ? 3 : 2;
+    return bt->select == TLIBG_SELECT_FIXED ? 3 : 2;
 }
 
 void release(tlibg_batch* bt)
@@ -645,6 +641,8 @@ int tlibg_batch_features(const tlibg_problem* pr, size_t count, float* feat, int
         CanonView cn;
         const int st = internal_analyse(x.q, x.p, x.a, x.na, x.wa, x.pia, x.b, x.nb, x.c, x.nc, x.wc, x.pic, &cn);
         if (st) return st;
+        if ((reinterpret_cast<uintptr_t>(x.a) | reinterpret_cast<uintptr_t>(x.b) | reinterpret_cast<uintptr_t>(x.c)) & 3u)
+            return internal_fail(TLIBG_ERR_UNSUPPORTED, "tlibg: a, b and c must be aligned to their element sizes");
         size_t k = 0;
         while (x.pia[k] != x.q) ++k;
         float* f = feat + i * NFEAT;
@@ -766,6 +764,18 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
     if (!model.empty() && bt->select == TLIBG_SELECT_LEARNED)
         cudaMemcpyAsync(bt->d_model, model.data(), MLP_PARAMS * sizeof(float), cudaMemcpyHostToDevice, st);
     bt->grid = sms * exec_ctas_per_sm(bt->kahan);
+    if (bt->select == TLIBG_SELECT_LEARNED) {
+        // the scores depend only on the descriptors and the model: select once,
+        // every launch replays plan + exec with the chosen variants
+        const int threads = bt->count * NVARIANT;
+        batch_select<<<(threads + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_model, bt->log2_count,
+                                                            bt->log2_keep);
+        internal_count_launches(1);
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            release(bt);
+            return internal_cuda_fail(e, "batch select");
+        }
+    }
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
         release(bt);
         return internal_cuda_fail(e, "tlibg_batch_create");

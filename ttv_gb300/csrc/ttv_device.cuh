@@ -90,6 +90,7 @@ template <typename T, bool KAHAN> struct Acc {
         }
     }
     __device__ __forceinline__ T value() const { return KAHAN ? (s - c) : s; }
+    __device__ __forceinline__ void renorm() {}
     __device__ __forceinline__ void fold() {}
 };
 
@@ -98,17 +99,21 @@ template <typename T, bool KAHAN> struct Acc {
 //
 // GB300 executes about two DFMA per SM per clock (1.25 TFLOP/s), below the
 // one-per-element rate an HBM-bound fp64 TTV needs.  Each double x with
-// exponent in [2^-60, 2^61) is split exactly into x = hi + lo, hi = x cut to
-// its top 24 significand bits, lo = the remaining 29 bits scaled (integer
-// ops, one int->float conversion, one power-of-two multiply).  The product
-// a*b = hi_a*hi_b + (hi_a*lo_b + lo_a*hi_b + lo_a*lo_b) keeps hi_a*hi_b
-// exact through Dekker's TwoProduct (one FMA gives its rounding error) and
-// the small terms in fp32; the running sum is a double-float (hi, lo) updated
-// with Knuth's TwoSum and a fast renormalisation.  Relative error per product
-// about 2^-47, per addition about 2^-47 of the sum.  Elements outside the
-// exponent window (and non-finite or subnormal ones) take a native DFMA into
-// a separate double accumulator.  fold() turns the state into one double, in
-// `s`, before any cross-lane or cross-warp reduction.
+// exponent in [2^-60, 2^61) is split into x = hi + lo with integer ops only:
+// hi = x cut to its top 24 significand bits (one funnel shift moves the
+// significand into float position, one add rebiases the exponent modulo 256,
+// one bit-select restores the sign); lo = the remaining 29 bits converted to
+// float (rounded to 24 bits, so |x - hi - lo| <= 2^-48 |x|) times
+// +-2^(e-1075), whose bit pattern is hi's sign and exponent minus 52.  The
+// product a*b = hi_a*hi_b + (hi_a*lo_b + lo_a*hi_b) keeps hi_a*hi_b exact
+// through Dekker's TwoProduct (one FMA gives its rounding error); lo_a*lo_b
+// (below 2^-48 of the product) is dropped.  The running sum is a double-float
+// (hi, lo): Knuth's TwoSum adds each product to hi exactly and the error goes
+// to lo; renorm() (every few products, and before fold()) moves lo's excess
+// back into hi so lo's own rounding stays near 2^-48 of the sum.  Elements
+// outside the exponent window (zeros, subnormals, non-finite values) take a
+// native DFMA into a separate double accumulator.  fold() turns the state
+// into one double, in `s`, before any cross-lane or cross-warp reduction.
 // --------------------------------------------------------------------------
 struct DSplit {
     float hi, lo;
@@ -117,20 +122,17 @@ struct DSplit {
 
 __device__ __forceinline__ DSplit split_double(double x)
 {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const uint32_t hi32 = (uint32_t)(bits >> 32), lo32 = (uint32_t)bits;
-    const uint32_t e = (hi32 >> 20) & 0x7ffu;
-    const uint32_t sign = hi32 & 0x80000000u;
+    const uint32_t hi32 = (uint32_t)__double2hiint(x), lo32 = (uint32_t)__double2loint(x);
     DSplit r;
-    const bool zero = ((hi32 & 0x7fffffffu) | lo32) == 0u;
-    r.ok = zero || (e >= 1023u - 60u && e <= 1023u + 60u);
-    const uint32_t m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
-    const uint32_t ee = r.ok && !zero ? e : 1023u;   // keep the bit patterns below well formed
-    r.hi = zero ? 0.f : __uint_as_float(sign | ((ee - 1023u + 127u) << 23) | m23);
-    const float rest = (float)(lo32 & 0x1fffffffu);                    // low 29 significand bits
-    const float scale = __uint_as_float((ee - 1075u + 127u) << 23);    // 2^(e - 1075)
-    const float lo = rest * scale;
-    r.lo = zero ? 0.f : (sign ? -lo : lo);
+    // biased exponent e in [963, 1083]: 2^-60 <= |x| < 2^61
+    r.ok = ((hi32 & 0x7ff00000u) - (963u << 20)) < (121u << 20);
+    // top 32 bits of (hi32:lo32) << 3 hold e mod 256 and 23 significand bits;
+    // float exponent e - 896 == (e mod 256) + 128 (mod 256) inside the window
+    const uint32_t top = __funnelshift_l(lo32, hi32, 3) + (128u << 23);
+    const uint32_t hb = (top & 0x7fffffffu) | (hi32 & 0x80000000u);
+    r.hi = __uint_as_float(hb);
+    const float scale = __uint_as_float((hb & 0xff800000u) - (52u << 23));   // +-2^(e-1075)
+    r.lo = (float)(lo32 & 0x1fffffffu) * scale;
     return r;
 }
 
@@ -146,25 +148,35 @@ struct AccDF {
         lo = 0.f;
         d = 0.0;
     }
+    // One product into the running sum, without renormalisation: callers
+    // renorm() at least every 8 products.
     __device__ __forceinline__ void add_split(const DSplit& a, const DSplit& b, double ad, double bd)
     {
         if (a.ok && b.ok) {
             const float p = a.hi * b.hi;
-            const float pe = fmaf(a.hi, b.hi, -p);                              // exact error of p
-            const float t = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.lo, b.lo, pe)));
+            const float t = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
             const float sum = hi + p;                                           // TwoSum(hi, p)
             const float v = sum - hi;
-            float err = (hi - (sum - v)) + (p - v);
-            err += lo + t;
-            hi = sum + err;                                                     // renormalise
-            lo = err - (hi - sum);
+            lo += ((hi - (sum - v)) + (p - v)) + t;
+            hi = sum;
         } else {
             d = fma(ad, bd, d);
         }
     }
-    __device__ __forceinline__ void fma_add(double a, double b) { add_split(split_double(a), split_double(b), a, b); }
+    __device__ __forceinline__ void renorm()
+    {
+        const float sum = hi + lo;
+        lo -= sum - hi;
+        hi = sum;
+    }
+    __device__ __forceinline__ void fma_add(double a, double b)
+    {
+        add_split(split_double(a), split_double(b), a, b);
+        renorm();
+    }
     __device__ __forceinline__ void fold()
     {
+        renorm();
         s = ((double)hi + (double)lo) + d;
         c = 0.0;
     }

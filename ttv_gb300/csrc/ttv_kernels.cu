@@ -97,6 +97,33 @@ __device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, 
     }
 }
 
+// acc[v] += av[v] * bv[v] (row form: b varies with the element).  The fp64
+// double-float accumulator mixes the same way: even vector slots (or even
+// unrolled loads when V == 1) on the DFMA pipe, odd ones emulated.
+template <int V, typename AccT, typename T>
+__device__ __forceinline__ void vec_fma(AccT (&acc)[V], const T (&av)[V], const T (&bv)[V], int u = 0)
+{
+    if constexpr (std::is_same<AccT, AccDF>::value) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const bool native = V > 1 ? ((v & 1) == 0) : ((u & 1) == 0);
+            if (native)
+                acc[v].d = fma(av[v], bv[v], acc[v].d);
+            else
+                acc[v].add_split(split_double(av[v]), split_double(bv[v]), av[v], bv[v]);
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bv[v]);
+    }
+}
+
+template <int V, typename AccT> __device__ __forceinline__ void renorm_all(AccT (&acc)[V])
+{
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v].renorm();
+}
+
 // --------------------------------------------------------------------------
 // row kernel: P == 1
 // --------------------------------------------------------------------------
@@ -142,17 +169,16 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
                     load_b<T, V>(bp + (kv + u * G) * V, bv[u]);
                 }
 #pragma unroll
-                for (int u = 0; u < U; ++u)
-#pragma unroll
-                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
+                for (int u = 0; u < U; ++u) vec_fma<V>(acc, av[u], bv[u], u);
+                renorm_all<V>(acc);
             }
 #pragma unroll 4
             for (; kv < nv; kv += G) {
                 T av[V], bv[V];
                 load_a<TA, T, V>(ap + kv * V, av);
                 load_b<T, V>(bp + kv * V, bv);
-#pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bv[v]);
+                vec_fma<V>(acc, av, bv);
+                renorm_all<V>(acc);
             }
             for (uint64_t e = nv * V + gl; e < n; e += G) {
                 T av[1];
@@ -247,6 +273,7 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
                 for (int u = 0; u < U; ++u) load_a<TA, T, V>(ap + (i + u * WI) * k.P, av[u]);
 #pragma unroll
                 for (int u = 0; u < U; ++u) row_fma<V>(acc, av[u], bs[i + u * WI], u);
+                renorm_all<V>(acc);
             }
 #pragma unroll 4
             for (; i < ie; i += WI) {
@@ -254,6 +281,7 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
                 load_a<TA, T, V>(ap + i * k.P, av);
                 row_fma<V>(acc, av, bs[i]);
             }
+            renorm_all<V>(acc);
         }
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fold();
@@ -347,6 +375,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 }  // namespace tlibg
 
 #include "ttv_stream.cuh"
+#include "ttv_realign.cuh"
 
 namespace tlibg {
 
@@ -359,6 +388,10 @@ template <typename TA, typename T, bool KAHAN>
 static KernelFn pick_main(int kind, int vec)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
+    if (kind == KIND_COL_REALIGN) {
+        if constexpr (std::is_same<TA, T>::value) return col_realign_kernel<T, KAHAN>;
+        else return nullptr;
+    }
     if (kind == KIND_ROW) {
         switch (vec) {
         case 1: return row_kernel<TA, T, 1, KAHAN>;
@@ -521,7 +554,7 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     k.items_per_cta = plan.items_per_cta;
     k.nseg = (uint32_t)plan.split;
     k.group = (uint32_t)plan.group;
-    if (plan.kind == KIND_COL) {
+    if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {
         const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec;
         k.ntiles = (plan.S * plan.P + TO - 1) / TO;
     } else {

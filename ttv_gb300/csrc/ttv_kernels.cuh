@@ -7,7 +7,7 @@
 namespace tlibg {
 
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
-enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2 };
+enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
@@ -19,8 +19,8 @@ constexpr int STREAM_CONSUMERS = 256;       // streamed kernel: consumer threads
 struct Plan {
     int dtype = F32;
     int kind = KIND_COL;
-    int group = 1;        // ROW: lanes per output row; COL: warps along the contracted mode
-    int vec = 1;          // elements per vector load
+    int group = 1;        // ROW: lanes per output row; COL / COL_REALIGN: warps along the contracted mode
+    int vec = 1;          // elements per vector load (COL_REALIGN: 16 bytes, realigned by shuffles)
     int split = 1;        // segments of the contracted mode
     int kahan = 1;        // compensated fp32 accumulation
     uint64_t P = 1, nq = 1, S = 1;

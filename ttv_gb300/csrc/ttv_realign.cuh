@@ -1,0 +1,215 @@
+// Column kernel for prefixes whose rows are not 16-byte aligned (included by
+// ttv_kernels.cu).
+//
+// When P is not a multiple of the 16-byte vector width (V = 4 fp32, 2 fp64),
+// or A starts at an odd element offset, the rows A[s, i, :] start at
+// different offsets inside their 16-byte blocks and the plain column kernel
+// falls back to scalar loads.  Here a warp owns a window of 32*V consecutive
+// outputs of one row of one slab and, for every row i, loads the 33 aligned
+// 16-byte vectors that cover the window: lane L the L-th, lane 31 also the
+// 33rd when the window is misaligned.  The lane's V elements are its own
+// vector shifted by the row's misalignment r (warp-uniform, 0..V-1) with the
+// start of its right neighbour's vector, fetched by one warp shuffle per
+// element.  Every load is a full 16-byte load and contains at least one
+// element of the window, so no access leaves A's allocation.  Windows that
+// straddle two slabs or end past a row (the last window of each row) take
+// scalar loads.  Work items, the b stage, the warps stacked along q and the
+// split reduction are those of the column kernel.
+#pragma once
+
+namespace tlibg {
+
+// o[v] = window element v of a lane: (c ++ n)[v + r] for r in 0..V-1, with
+// compile-time indices only (no local-memory arrays).
+template <typename T, int V>
+__device__ __forceinline__ void realign_vec(const T (&c)[V], const T (&n)[V], uint32_t r, T (&o)[V])
+{
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        T x = c[v];
+#pragma unroll
+        for (int k = 1; k < V; ++k) {
+            const T y = (v + k < V) ? c[v + k] : n[v + k - V];
+            x = (r == (uint32_t)k) ? y : x;
+        }
+        o[v] = x;
+    }
+}
+
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
+{
+    constexpr int V = 16 / (int)sizeof(T);
+    constexpr int U = 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
+    T* sb = reinterpret_cast<T*>(smem_raw + 16);
+    constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));
+
+    const uint32_t WI = k.group;
+    const uint32_t WO = (BLOCK / 32) / WI;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t wi = warp % WI, wo = warp / WI;
+    const uint64_t TO = uint64_t(WO) * 32u * V;
+    const uint64_t P = k.P;
+    const uint64_t outputs = k.S * P;
+    const T* __restrict__ A = static_cast<const T*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    // A's element offset inside its 16-byte block
+    const uint32_t amis = (uint32_t)((reinterpret_cast<uintptr_t>(A) & 15u) / sizeof(T));
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    uint32_t phase = 0;
+    uint64_t staged_seg = ~uint64_t(0);
+    uint32_t off = 0;
+    const uint64_t first = uint64_t(blockIdx.x) * k.items_per_cta;
+    const uint64_t last = min(k.items, first + k.items_per_cta);
+
+    for (uint64_t item = first; item < last; ++item) {
+        const uint64_t seg = item / k.ntiles;
+        const uint64_t tile = item - seg * k.ntiles;
+        const uint64_t ib = seg * k.seg_len;
+        const uint64_t ie = min(k.nq, ib + k.seg_len);
+        if (seg != staged_seg) {
+            __syncthreads();   // every reader of the previous segment is done
+            if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
+            staged_seg = seg;
+            off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+        }
+        const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+
+        const uint64_t ow = tile * TO + uint64_t(wo) * 32u * V;   // the warp's window
+        const uint64_t o0 = ow + uint64_t(lane) * V;
+        typename AccSel<T, KAHAN>::type acc[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].init();
+        if (ow < outputs) {
+            const uint64_t sw = ow / P;
+            const uint64_t jw = ow - sw * P;
+            if (jw + 32u * V <= P) {
+                // whole window inside row (sw, i, .): realigned vector loads
+                const uint64_t base = sw * k.nq * P + jw;   // element index of A[sw, 0, jw]
+                uint64_t i = ib + wi;
+                for (; i + (U - 1) * WI < ie; i += U * WI) {
+                    T cur[U][V], ext[U][V] = {};
+                    uint32_t r[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const uint64_t e = base + (i + u * WI) * P;
+                        r[u] = (uint32_t)((amis + e) & (V - 1));
+                        const T* vp = A + (int64_t)(e - r[u]);   // 16-byte aligned, in A's first block at worst
+                        load_a<T, T, V>(vp + lane * V, cur[u]);
+                        if (lane == 31u && r[u] != 0u) load_a<T, T, V>(vp + 32u * V, ext[u]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        T nxt[V], av[V];
+#pragma unroll
+                        for (int v = 0; v < V; ++v) {
+                            const T t = __shfl_down_sync(0xffffffffu, cur[u][v], 1);
+                            nxt[v] = lane == 31u ? ext[u][v] : t;
+                        }
+                        realign_vec<T, V>(cur[u], nxt, r[u], av);
+                        row_fma<V>(acc, av, bs[i + u * WI], u);
+                    }
+                    renorm_all<V>(acc);
+                }
+                for (; i < ie; i += WI) {
+                    T cur[V], ext[V] = {}, nxt[V], av[V];
+                    const uint64_t e = base + i * P;
+                    const uint32_t rr = (uint32_t)((amis + e) & (V - 1));
+                    const T* vp = A + (int64_t)(e - rr);
+                    load_a<T, T, V>(vp + lane * V, cur);
+                    if (lane == 31u && rr != 0u) load_a<T, T, V>(vp + 32u * V, ext);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        const T t = __shfl_down_sync(0xffffffffu, cur[v], 1);
+                        nxt[v] = lane == 31u ? ext[v] : t;
+                    }
+                    realign_vec<T, V>(cur, nxt, rr, av);
+                    row_fma<V>(acc, av, bs[i]);
+                }
+                renorm_all<V>(acc);
+            } else {
+                // window straddles two slabs or ends past the row: scalar loads
+                uint64_t ofs[V];
+                bool ok[V];
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    const uint64_t o = o0 + v;
+                    ok[v] = o < outputs;
+                    const uint64_t s = ok[v] ? o / P : 0;
+                    ofs[v] = s * k.nq * P + (o - s * P);
+                }
+                for (uint64_t i = ib + wi; i < ie; i += WI) {
+                    const T bb = bs[i];
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        if (ok[v]) {
+                            T av[1];
+                            load_a<T, T, 1>(A + ofs[v] + i * P, av);
+                            acc[v].fma_add(av[0], bb);
+                        }
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].fold();
+        if (WI > 1) {
+            // warps stacked along i hand their partials to warp row wi == 0
+            const uint32_t slot = wo * 32u + lane;
+            if (wi > 0) {
+                T* rp = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    rp[2 * v] = acc[v].s;
+                    rp[2 * v + 1] = acc[v].c;
+                }
+            }
+            __syncthreads();
+            if (wi == 0) {
+                for (uint32_t w = 1; w < WI; ++w) {
+                    const T* rp = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].merge(rp[2 * v], rp[2 * v + 1]);
+                }
+            }
+            __syncthreads();
+        }
+        if (wi == 0) {
+            if (k.nseg == 1) {
+                T* out = static_cast<T*>(k.out) + o0;
+                if (o0 + V <= outputs && (reinterpret_cast<uintptr_t>(out) & 15u) == 0) {
+                    T vals[V];
+#pragma unroll
+                    for (int v = 0; v < V; ++v) vals[v] = acc[v].value();
+                    *reinterpret_cast<uint4*>(out) = *reinterpret_cast<const uint4*>(vals);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        if (o0 + v < outputs) out[v] = acc[v].value();
+                }
+            } else {
+                Pair<T>* pp = static_cast<Pair<T>*>(k.partial) + seg * outputs;
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    if (o0 + v < outputs) {
+                        Pair<T> pr;
+                        pr.s = acc[v].s;
+                        pr.c = KAHAN ? acc[v].c : T(0);
+                        pp[o0 + v] = pr;
+                    }
+            }
+        }
+    }
+}
+
+}  // namespace tlibg

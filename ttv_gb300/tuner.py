@@ -21,8 +21,8 @@ import sys
 
 import numpy as np
 
-from . import F32, F64, KIND_COL, KIND_ROW, KIND_STREAM, ACC_DOUBLE_FLOAT, _options, \
-    library, output_layout, output_shape, plan, strides, ttv
+from . import F32, F64, KIND_COL, KIND_COL_REALIGN, KIND_ROW, KIND_STREAM, ACC_DOUBLE_FLOAT, \
+    _options, library, output_layout, output_shape, plan, strides, ttv
 
 L2_FLUSH_BYTES = 256 << 20
 
@@ -31,23 +31,26 @@ def candidates(dtype, P, nq, S):
     """Option dicts worth timing for a canonical problem."""
     out = [{}]   # the planner's own choice
     es = 8 if dtype == F64 else 4
+    accs = (0, ACC_DOUBLE_FLOAT) if dtype == F64 else (0,)
     if P == 1:
         for g in (1, 2, 4, 8, 16, 32):
-            out.append({"kind": KIND_ROW, "group": g})
+            for acc in accs:
+                out.append({"kind": KIND_ROW, "group": g, "accumulate": acc})
         if nq * es <= 16384:
             for g in (0, 2, 4, 8, 16, 32):
                 out.append({"kind": KIND_STREAM, "group": g})
     else:
-        for wi in (1, 2, 4, 8):
-            for split in (0, 1, 2, 4, 16):
-                if split and split > nq:
-                    continue
-                if split and split < -(-nq // (16384 // es)):
-                    continue
-                out.append({"kind": KIND_COL, "group": wi, "split": split})
-        if dtype == F64:
+        min_split = -(-nq // (16384 // es))
+        kinds = (KIND_COL, KIND_COL_REALIGN) if P % (16 // es) else (KIND_COL,)
+        for kind in kinds:
             for wi in (1, 2, 4, 8):
-                out.append({"kind": KIND_COL, "group": wi, "accumulate": ACC_DOUBLE_FLOAT})
+                for split in (0, 1, 2, 4, 16):
+                    if split and (split > nq or split < min_split):
+                        continue
+                    for acc in accs:
+                        out.append({"kind": kind, "group": wi, "split": split, "accumulate": acc})
+        if P * es <= 16384 and -(-P // 256) <= 8:
+            out.append({"kind": KIND_STREAM})
     return out
 
 
