@@ -421,7 +421,7 @@ REALIGN_SHAPES = [
     ([7, 50, 3], [1, 2, 3], 2),          # P < one window: scalar path only
     ([129, 5000, 2], [1, 2, 3], 2),      # long contraction: split b stages
     ([1000, 17, 3], [1, 2, 3], 2),       # aligned P: misalignment 0 throughout
-    ([5, 3, 700], [3, 1, 2], 3),         # layout permuted: P = 700 * 5
+    ([5, 3, 700], [3, 1, 2], 2),         # layout permuted: P = 700 * 5, n_q = 3
 ]
 
 
