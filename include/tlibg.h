@@ -44,9 +44,13 @@ extern "C" {
 #define TLIBG_BF16A  2   /* A bfloat16 (raw 16-bit patterns), b and C float    */
 
 /* ---- accumulation ---- */
-#define TLIBG_ACC_COMPENSATED  0  /* fp32: per-thread Kahan partials (default); fp64: DFMA  */
-#define TLIBG_ACC_PLAIN        1  /* fp32: plain FMA accumulation; fp64: DFMA               */
-#define TLIBG_ACC_DOUBLE_FLOAT 2  /* fp64: double-float accumulation on the FP32/INT32 pipes */
+#define TLIBG_ACC_COMPENSATED  0  /* default.  fp32: per-thread Kahan partials.  fp64: register   */
+                                  /*   kernels mix native DFMA (half the products) with double-  */
+                                  /*   float accumulation on the FP32/INT32 pipes; the streamed   */
+                                  /*   kernel uses DFMA                                            */
+#define TLIBG_ACC_PLAIN        1  /* fp32: plain FMA accumulation; fp64: native DFMA only          */
+#define TLIBG_ACC_DOUBLE_FLOAT 2  /* fp64: the mix in the register kernels, double-float for every */
+                                  /*   in-window product in the streamed kernel                    */
 
 /* ---- kernel families chosen by the planner ---- */
 #define TLIBG_KIND_ROW 0   /* q is the fastest layout mode (prefix P == 1): lane-group dot products */

@@ -152,10 +152,12 @@ def test_planner_kernel_family(engine):
     # long rows: the register kernels (q fastest -> row kernel, else column kernel)
     assert engine.plan(1, [16384, 16384], [1, 2])["kind"] == engine.KIND_ROW
     assert engine.plan(2, [16384, 16384], [1, 2])["kind"] == engine.KIND_COL
-    # rows of the prefix not 16-byte aligned: shuffle-realigned loads once rows span 4 KB
+    # fp32 rows of the prefix not 16-byte aligned: shuffle-realigned loads from 4 KB rows
+    # (2 KB with a short contraction); fp64 keeps scalar 8-byte loads
     assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL_REALIGN
-    assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == \
-        engine.KIND_COL_REALIGN
+    assert engine.plan(3, [25, 25, 25, 25], [1, 2, 3, 4])["kind"] == engine.KIND_COL_REALIGN
+    assert engine.plan(2, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_COL
     assert engine.plan(3, [645, 645, 645], [1, 2, 3])["vec"] == 4
     assert engine.plan(2, [25, 25, 25], [1, 2, 3])["kind"] == engine.KIND_COL
     assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.BF16A)["kind"] == engine.KIND_COL

@@ -391,12 +391,12 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     pl.P = cn.P;
     pl.nq = cn.nq;
     pl.S = cn.S;
-    // fp32: Kahan unless plain is asked for; fp64: native DFMA unless the double-float
-    // emulation on the FP32/INT32 pipes is asked for (TLIBG_ACC_DOUBLE_FLOAT)
+    // fp32: Kahan unless plain is asked for.  fp64: the register kernels mix native
+    // DFMA with double-float emulation on the FP32/INT32 pipes (measured faster than
+    // DFMA alone on GB300); the streamed kernel uses native DFMA unless the emulation
+    // is asked for (TLIBG_ACC_DOUBLE_FLOAT); TLIBG_ACC_PLAIN is native DFMA everywhere.
     if (dtype == F64)
-        pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1
-                   : (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0
-                   : (cn.P > 1 ? 1 : 0);   // default: the mix in the column kernel (measured faster)
+        pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
     else
         pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
     pl.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
@@ -423,8 +423,10 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         rows_aligned = cn.nq % vb == 0 && aligned(a, 16) && aligned(b, 16);
     }
     const bool stream_default = eligible && cn.P == 1 && !rows_aligned && !(dtype == F64 && cn.nq >= 256);
-    if ((opt && opt->kind == KIND_STREAM) || (stream_default && !(opt && opt->kind >= 0)))
+    if ((opt && opt->kind == KIND_STREAM) || (stream_default && !(opt && opt->kind >= 0))) {
+        if (dtype == F64) pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
         return make_stream_plan(pl, cn, opt, sms, out);
+    }
     const int vmax = (int)(16 / ea);
 
     // vector width: the widest load that keeps every access aligned
@@ -445,9 +447,12 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         if (!vec_ok(V)) return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced vector width violates alignment");
     } else {
         while (V > 1 && !vec_ok(V)) V /= 2;
-        // rows that are not 16-byte aligned and long enough that windows of 32
-        // vectors rarely straddle two rows: realigned 16-byte loads
-        if (V < vmax && realign_ok && !(opt && opt->kind >= 0) && cn.P * ea >= 4096) {
+        // fp32 rows that are not 16-byte aligned and long enough that windows of 32
+        // vectors rarely straddle two rows: realigned 16-byte loads (measured on GB300:
+        // ahead of scalar loads from 4 KB rows on, and from 2 KB rows when the
+        // contraction is short; for fp64 scalar 8-byte loads stay ahead)
+        const bool realign_default = dtype == F32 && (cn.P >= 1024 || (cn.P >= 512 && cn.nq <= 64));
+        if (V < vmax && realign_ok && !(opt && opt->kind >= 0) && realign_default) {
             V = vmax;
             pl.kind = KIND_COL_REALIGN;
         }
@@ -458,12 +463,11 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     const int force_group = opt ? opt->group : 0;
     if (pl.kind == KIND_ROW) {
         // Lanes per row, measured on GB300: fp32 about 16 vector loads per lane (at least
-        // 2 lanes); fp64 up to 64 elements per lane so the shuffle-tree DADDs stay rare,
-        // but two lanes for rows of at most 8 vectors.
+        // 2 lanes); fp64 about 512 bytes of the row per lane.
         const uint64_t nvec = cdiv(cn.nq, V);
         int Gdef;
         if (dtype == F64)
-            Gdef = nvec <= 8 ? 2 : std::min(8, pow2_floor(std::max<uint64_t>(1, nvec / 64)));
+            Gdef = std::max(1, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 64))));
         else
             Gdef = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / 16))));
         int G = force_group > 0 ? force_group : Gdef;
