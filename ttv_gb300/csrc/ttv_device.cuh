@@ -182,7 +182,32 @@ struct AccDF {
     }
     __device__ __forceinline__ void merge(double os, double) { s = s + os; }
     __device__ __forceinline__ double value() const { return s; }
+    // Take over another (unfolded) accumulator of the same output: the
+    // double-floats merge on the FP32 pipe (TwoSum), only the DFMA parts
+    // need one DADD.
+    __device__ __forceinline__ void absorb(const AccDF& o)
+    {
+        const float sum = hi + o.hi;
+        const float v = sum - hi;
+        lo += ((hi - (sum - v)) + (o.hi - v)) + o.lo;
+        hi = sum;
+        d += o.d;
+    }
 };
+
+// Reduce the V accumulators of one lane (parts of the same dot product) into
+// acc[0], folded.
+template <int V, typename T, bool KAHAN> __device__ __forceinline__ void fold_vec(Acc<T, KAHAN> (&acc)[V])
+{
+#pragma unroll
+    for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
+}
+template <int V> __device__ __forceinline__ void fold_vec(AccDF (&acc)[V])
+{
+#pragma unroll
+    for (int v = 1; v < V; ++v) acc[0].absorb(acc[v]);
+    acc[0].fold();
+}
 
 // Accumulator of a kernel instantiation: fp32 plain / Kahan, fp64 native
 // DFMA (KAHAN == false) or double-float emulation (KAHAN == true).

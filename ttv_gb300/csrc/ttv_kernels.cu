@@ -36,12 +36,17 @@ template <typename T> struct Pair {
     T s, c;
 };
 
-// Independent loads each thread keeps in flight: 64 bytes per thread whatever
-// the load width, so narrow (misaligned or odd-extent) layouts still cover the
-// HBM latency-bandwidth product.
+// Independent loads each thread keeps in flight: 4 of 16 bytes, or
+// TLIBG_NARROW_INFLIGHT bytes (at most 16 loads) for narrower loads, so
+// misaligned or odd-extent layouts still cover the HBM latency-bandwidth
+// product.
+#ifndef TLIBG_NARROW_INFLIGHT
+#define TLIBG_NARROW_INFLIGHT 64
+#endif
 template <typename TA, int V> __host__ __device__ constexpr int loads_in_flight()
 {
-    return (int)sizeof(TA) * V >= 16 ? 4 : (64 / ((int)sizeof(TA) * V) > 16 ? 16 : 64 / ((int)sizeof(TA) * V));
+    return (int)sizeof(TA) * V >= 16 ? 4
+           : (TLIBG_NARROW_INFLIGHT / ((int)sizeof(TA) * V) > 16 ? 16 : TLIBG_NARROW_INFLIGHT / ((int)sizeof(TA) * V));
 }
 
 // --------------------------------------------------------------------------
@@ -186,10 +191,7 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
                 acc[0].fma_add(av[0], __ldg(bp + e));
             }
         }
-#pragma unroll
-        for (int v = 0; v < V; ++v) acc[v].fold();
-#pragma unroll
-        for (int v = 1; v < V; ++v) acc[0].merge(acc[v].s, acc[v].c);
+        fold_vec<V>(acc);
         for (uint32_t off = G >> 1; off > 0; off >>= 1) {
             T os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
             T oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
