@@ -455,3 +455,27 @@ def test_realigned_column_kernel(engine, orc, torch_dev, na, pia, q):
                            sync=True)
                 err = orc.rel_error(dc.cpu().numpy(), *truth)
                 assert err <= TOL[dt], (na, pia, q, dt, oa, g, split, acc, err)
+
+
+def test_short_rows(engine, orc, torch_dev):
+    """q-fastest rows of a few vectors: several rows per lane group in flight
+    (one or two vectors per lane), groups wider than the row, row counts that
+    leave the last iteration partial; fp32 compensated and plain, fp64 both modes."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(77)
+    for dt in (np.float32, np.float64):
+        vmax = 16 // np.dtype(dt).itemsize
+        accs = (engine.ACC_COMPENSATED, engine.ACC_PLAIN)
+        for nq in (2, 4, 6, 8, 12, 16, 24, 32, 48, 64):
+            S = 1237 + nq
+            na, pia, q = [nq, S], [1, 2], 1
+            a = rng.uniform(-1, 1, nq * S).astype(dt)
+            b = rng.uniform(-1, 1, nq).astype(dt)
+            truth = orc.truth(S, nq, 1, a, b)
+            for v in (1, 2, 4):
+                if v > vmax or nq % v:
+                    continue
+                for g in (1, 2, 4, 8, 16, 32):
+                    for acc in accs:
+                        check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
+                              kind=engine.KIND_ROW, group=g, vec=v, accumulate=acc)

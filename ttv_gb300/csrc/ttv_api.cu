@@ -463,11 +463,12 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     const int force_group = opt ? opt->group : 0;
     if (pl.kind == KIND_ROW) {
         // Lanes per row, measured on GB300: fp32 about 16 vector loads per lane (at least
-        // 2 lanes); fp64 about 512 bytes of the row per lane.
+        // 2 lanes); fp64 about 64 elements per lane (at least 2 lanes), one lane for rows
+        // of at most 8 vectors.
         const uint64_t nvec = cdiv(cn.nq, V);
         int Gdef;
         if (dtype == F64)
-            Gdef = std::max(1, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 64))));
+            Gdef = nvec <= 8 ? 1 : std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 64))));
         else
             Gdef = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / 16))));
         int G = force_group > 0 ? force_group : Gdef;

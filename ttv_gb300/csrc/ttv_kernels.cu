@@ -41,7 +41,7 @@ template <typename T> struct Pair {
 // misaligned or odd-extent layouts still cover the HBM latency-bandwidth
 // product.
 #ifndef TLIBG_NARROW_INFLIGHT
-#define TLIBG_NARROW_INFLIGHT 64
+#define TLIBG_NARROW_INFLIGHT 128
 #endif
 template <typename TA, int V> __host__ __device__ constexpr int loads_in_flight()
 {
@@ -129,9 +129,102 @@ template <int V, typename AccT> __device__ __forceinline__ void renorm_all(AccT 
     for (int v = 0; v < V; ++v) acc[v].renorm();
 }
 
+// UB rows of the contracted mode for one thread: all loads first, then the
+// products (column form: b[i] shared by the V outputs; u alternates the fp64
+// mix when V == 1).
+template <int UB, int V, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void col_rows(AccT (&acc)[V], const TA* ap, uint64_t P, const T* bs, uint64_t i,
+                                         uint32_t WI)
+{
+    T av[UB][V];
+#pragma unroll
+    for (int u = 0; u < UB; ++u) load_a<TA, T, V>(ap + (i + u * WI) * P, av[u]);
+#pragma unroll
+    for (int u = 0; u < UB; ++u) row_fma<V>(acc, av[u], bs[i + u * WI], u);
+    renorm_all<V>(acc);
+}
+
+// Same for UB vectors of a row (row form: b varies with the element).
+template <int UB, int V, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void row_vecs(AccT (&acc)[V], const TA* ap, const T* bp, uint64_t kv, uint32_t G)
+{
+    T av[UB][V], bv[UB][V];
+#pragma unroll
+    for (int u = 0; u < UB; ++u) {
+        load_a<TA, T, V>(ap + (kv + u * G) * V, av[u]);
+        load_b<T, V>(bp + (kv + u * G) * V, bv[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < UB; ++u) vec_fma<V>(acc, av[u], bv[u], u);
+    renorm_all<V>(acc);
+}
+
 // --------------------------------------------------------------------------
 // row kernel: P == 1
 // --------------------------------------------------------------------------
+
+// Short rows (n_q a multiple of V, at most M vectors per lane of a group, no
+// split): a lane's M vectors of b are the same for every row and loaded once;
+// each iteration loads M vectors of each of R rows before any product, so a
+// row of a few dozen elements still keeps R * M loads per lane in flight.
+// Missing vectors (n_q / V not a multiple of G) are zeros, which add nothing.
+template <int M, int R, typename TA, typename T, int V, bool KAHAN>
+__device__ __forceinline__ void row_short(const KArgs& k, uint32_t G, uint32_t lane, uint64_t warp_id,
+                                          uint64_t nwarps)
+{
+    const uint32_t gl = lane & (G - 1u);
+    const uint32_t gpw = 32u / G;
+    const uint64_t nv = k.nq / V;
+    const TA* __restrict__ A = static_cast<const TA*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    T bv[M][V];
+#pragma unroll
+    for (int t = 0; t < M; ++t) {
+        const uint64_t kv = gl + (uint64_t)t * G;
+        if (kv < nv) {
+            load_b<T, V>(B + kv * V, bv[t]);
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) bv[t][v] = T(0);
+        }
+    }
+    const uint64_t per_iter = (uint64_t)gpw * R;
+    for (uint64_t base = warp_id * per_iter; base < k.items; base += nwarps * per_iter) {
+        T av[R][M][V];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint64_t item = base + (uint64_t)r * gpw + lane / G;
+#pragma unroll
+            for (int t = 0; t < M; ++t) {
+                const uint64_t kv = gl + (uint64_t)t * G;
+                if (item < k.items && kv < nv) {
+                    load_a<TA, T, V>(A + item * k.nq + kv * V, av[r][t]);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) av[r][t][v] = T(0);
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint64_t item = base + (uint64_t)r * gpw + lane / G;
+            typename AccSel<T, KAHAN>::type acc[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].init();
+#pragma unroll
+            for (int t = 0; t < M; ++t) vec_fma<V>(acc, av[r][t], bv[t], t);
+            renorm_all<V>(acc);
+            fold_vec<V>(acc);
+            for (uint32_t off = G >> 1; off > 0; off >>= 1) {
+                T os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
+                T oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
+                acc[0].merge(os, oc);
+            }
+            if (item < k.items && gl == 0) static_cast<T*>(k.out)[item] = acc[0].value();
+        }
+    }
+}
+
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
 {
@@ -144,6 +237,18 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
     constexpr int U = loads_in_flight<TA, V>();
+
+    if (k.nseg == 1 && k.nq % V == 0) {
+        const uint64_t nv = k.nq / V;
+        if (nv <= G) {
+            row_short<1, U, TA, T, V, KAHAN>(k, G, lane, warp_id, nwarps);
+            return;
+        }
+        if (nv <= 2u * G) {
+            row_short<2, (U >= 2 ? U / 2 : 1), TA, T, V, KAHAN>(k, G, lane, warp_id, nwarps);
+            return;
+        }
+    }
 
     for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
         const uint64_t item = wbase + lane / G;
@@ -166,25 +271,22 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
             const uint64_t n = ie - ib;
             const uint64_t nv = n / V;
             uint64_t kv = gl;
-            for (; kv + (U - 1) * G < nv; kv += U * G) {
-                T av[U][V], bv[U][V];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    load_a<TA, T, V>(ap + (kv + u * G) * V, av[u]);
-                    load_b<T, V>(bp + (kv + u * G) * V, bv[u]);
+            // blocks of U vectors, then one of U/2 and one of U/4 at most, then
+            // single vectors: short rows still get their loads in flight together
+            for (; kv + (U - 1) * G < nv; kv += U * G) row_vecs<U, V>(acc, ap, bp, kv, G);
+            if constexpr (U >= 4) {
+                if (kv + (U / 2 - 1) * G < nv) {
+                    row_vecs<U / 2, V>(acc, ap, bp, kv, G);
+                    kv += (U / 2) * G;
                 }
-#pragma unroll
-                for (int u = 0; u < U; ++u) vec_fma<V>(acc, av[u], bv[u], u);
-                renorm_all<V>(acc);
             }
-#pragma unroll 4
-            for (; kv < nv; kv += G) {
-                T av[V], bv[V];
-                load_a<TA, T, V>(ap + kv * V, av);
-                load_b<T, V>(bp + kv * V, bv);
-                vec_fma<V>(acc, av, bv);
-                renorm_all<V>(acc);
+            if constexpr (U >= 8) {
+                if (kv + (U / 4 - 1) * G < nv) {
+                    row_vecs<U / 4, V>(acc, ap, bp, kv, G);
+                    kv += (U / 4) * G;
+                }
             }
+            for (; kv < nv; kv += G) row_vecs<1, V>(acc, ap, bp, kv, G);
             for (uint64_t e = nv * V + gl; e < n; e += G) {
                 T av[1];
                 load_a<TA, T, 1>(ap + e, av);
@@ -269,21 +371,22 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
             const uint64_t j = o0 - s * k.P;
             const TA* ap = A + (s * k.nq) * k.P + j;
             uint64_t i = ib + wi;
-            for (; i + (U - 1) * WI < ie; i += U * WI) {
-                T av[U][V];
-#pragma unroll
-                for (int u = 0; u < U; ++u) load_a<TA, T, V>(ap + (i + u * WI) * k.P, av[u]);
-#pragma unroll
-                for (int u = 0; u < U; ++u) row_fma<V>(acc, av[u], bs[i + u * WI], u);
-                renorm_all<V>(acc);
+            // blocks of U rows, then one of U/2 and one of U/4 at most, then
+            // single rows: short contractions still get their loads in flight together
+            for (; i + (U - 1) * WI < ie; i += U * WI) col_rows<U, V>(acc, ap, k.P, bs, i, WI);
+            if constexpr (U >= 4) {
+                if (i + (U / 2 - 1) * WI < ie) {
+                    col_rows<U / 2, V>(acc, ap, k.P, bs, i, WI);
+                    i += (U / 2) * WI;
+                }
             }
-#pragma unroll 4
-            for (; i < ie; i += WI) {
-                T av[V];
-                load_a<TA, T, V>(ap + i * k.P, av);
-                row_fma<V>(acc, av, bs[i]);
+            if constexpr (U >= 8) {
+                if (i + (U / 4 - 1) * WI < ie) {
+                    col_rows<U / 4, V>(acc, ap, k.P, bs, i, WI);
+                    i += (U / 4) * WI;
+                }
             }
-            renorm_all<V>(acc);
+            for (; i < ie; i += WI) col_rows<1, V>(acc, ap, k.P, bs, i, WI);
         }
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fold();
