@@ -492,6 +492,13 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         pl.split = (int)nseg;
         pl.seg_len = seg_len;
         pl.items = cn.S * nseg;
+        // rows of at most two vectors per lane: the short-row kernel keeps several rows
+        // per lane group in flight (measured on GB300 for fp32 / bf16 storage; fp64 rows
+        // that short are bound by their per-row reductions on the FP64 pipe instead)
+        if (nseg == 1 && cn.nq % V == 0 && dtype != F64) {
+            const uint64_t nv = cn.nq / V;
+            pl.rows_m = nv <= (uint64_t)G ? 1 : (nv <= 2 * (uint64_t)G ? 2 : 0);
+        }
         const uint64_t groups_per_cta = BLOCK / G;
         pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * cps, cdiv(pl.items, groups_per_cta)));
         pl.items_per_cta = 0;
@@ -505,11 +512,13 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         pl.group = WI;
         int cps = std::max(1, plan_ctas_per_sm(pl));
         // Measured on GB300 (tuner sweeps): one warp row per tile and no split are best
-        // whenever the tiles alone cover the grid; otherwise stack warps along q, then
-        // split q until about two items per CTA.
+        // whenever the tiles alone cover the grid; otherwise two warp rows per tile
+        // (more only when q is too short to split), then split q until about two
+        // items per CTA.
         const uint64_t grid_full = (uint64_t)sms * cps;
-        if (force_group <= 0) {
-            while (WI < 8 && tiles_for(WI) < grid_full && cn.nq >= (uint64_t)WI * 2 * 4) WI *= 2;
+        if (force_group <= 0 && tiles_for(1) < grid_full) {
+            WI = 2;
+            while (WI < 8 && cn.nq < 64 && tiles_for(WI) < grid_full && cn.nq >= (uint64_t)WI * 2 * 4) WI *= 2;
             pl.group = WI;
             cps = std::max(1, plan_ctas_per_sm(pl));
         }

@@ -238,18 +238,6 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
     const T* __restrict__ B = static_cast<const T*>(k.b);
     constexpr int U = loads_in_flight<TA, V>();
 
-    if (k.nseg == 1 && k.nq % V == 0) {
-        const uint64_t nv = k.nq / V;
-        if (nv <= G) {
-            row_short<1, U, TA, T, V, KAHAN>(k, G, lane, warp_id, nwarps);
-            return;
-        }
-        if (nv <= 2u * G) {
-            row_short<2, (U >= 2 ? U / 2 : 1), TA, T, V, KAHAN>(k, G, lane, warp_id, nwarps);
-            return;
-        }
-    }
-
     for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
         const uint64_t item = wbase + lane / G;
         const bool valid = item < k.items;
@@ -310,6 +298,18 @@ __global__ void __launch_bounds__(BLOCK) row_kernel(KArgs k)
             }
         }
     }
+}
+
+// Short rows as their own kernel (its registers do not weigh on the general
+// row kernel): M vectors per lane of each row, R = U / M rows in flight.
+template <typename TA, typename T, int V, bool KAHAN, int M>
+__global__ void __launch_bounds__(BLOCK) row_short_kernel(KArgs k)
+{
+    constexpr int U = loads_in_flight<TA, V>();
+    constexpr int R = M == 1 ? U : (U >= 2 ? U / 2 : 1);
+    const uint64_t warp_id = (uint64_t(blockIdx.x) * BLOCK + threadIdx.x) >> 5;
+    const uint64_t nwarps = (uint64_t(gridDim.x) * BLOCK) >> 5;
+    row_short<M, R, TA, T, V, KAHAN>(k, k.group, threadIdx.x & 31u, warp_id, nwarps);
 }
 
 // --------------------------------------------------------------------------
@@ -489,14 +489,29 @@ namespace tlibg {
 // --------------------------------------------------------------------------
 typedef void (*KernelFn)(KArgs);
 
+template <typename TA, typename T, int M, bool KAHAN>
+static KernelFn pick_short(int vec)
+{
+    constexpr int VMAX = 16 / (int)sizeof(TA);
+    switch (vec) {
+    case 1: return row_short_kernel<TA, T, 1, KAHAN, M>;
+    case 2: return row_short_kernel<TA, T, 2, KAHAN, M>;
+    case 4: if constexpr (VMAX >= 4) return row_short_kernel<TA, T, 4, KAHAN, M>; else return nullptr;
+    case 8: if constexpr (VMAX >= 8) return row_short_kernel<TA, T, 8, KAHAN, M>; else return nullptr;
+    }
+    return nullptr;
+}
+
 template <typename TA, typename T, bool KAHAN>
-static KernelFn pick_main(int kind, int vec)
+static KernelFn pick_main(int kind, int vec, int rows_m)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
     if (kind == KIND_COL_REALIGN) {
         if constexpr (std::is_same<TA, T>::value) return col_realign_kernel<T, KAHAN>;
         else return nullptr;
     }
+    if (kind == KIND_ROW && rows_m == 1) return pick_short<TA, T, 1, KAHAN>(vec);
+    if (kind == KIND_ROW && rows_m == 2) return pick_short<TA, T, 2, KAHAN>(vec);
     if (kind == KIND_ROW) {
         switch (vec) {
         case 1: return row_kernel<TA, T, 1, KAHAN>;
@@ -547,14 +562,14 @@ static KernelFn main_kernel(const Plan& p)
     if (p.kind == KIND_STREAM) return reinterpret_cast<KernelFn>(stream_fn(p));
     switch (p.dtype) {
     case F32:
-        return p.kahan ? pick_main<float, float, true>(p.kind, p.vec)
-                       : pick_main<float, float, false>(p.kind, p.vec);
+        return p.kahan ? pick_main<float, float, true>(p.kind, p.vec, p.rows_m)
+                       : pick_main<float, float, false>(p.kind, p.vec, p.rows_m);
     case F64:
-        return p.kahan ? pick_main<double, double, true>(p.kind, p.vec)
-                       : pick_main<double, double, false>(p.kind, p.vec);
+        return p.kahan ? pick_main<double, double, true>(p.kind, p.vec, p.rows_m)
+                       : pick_main<double, double, false>(p.kind, p.vec, p.rows_m);
     case BF16A:
-        return p.kahan ? pick_main<uint16_t, float, true>(p.kind, p.vec)
-                       : pick_main<uint16_t, float, false>(p.kind, p.vec);
+        return p.kahan ? pick_main<uint16_t, float, true>(p.kind, p.vec, p.rows_m)
+                       : pick_main<uint16_t, float, false>(p.kind, p.vec, p.rows_m);
     }
     return nullptr;
 }

@@ -23,6 +23,7 @@ struct Plan {
     int vec = 1;          // elements per vector load (COL_REALIGN: 16 bytes, realigned by shuffles)
     int split = 1;        // segments of the contracted mode
     int kahan = 1;        // compensated fp32 accumulation
+    int rows_m = 0;       // ROW: 1 or 2 = short-row kernel (at most rows_m vectors per lane of a row)
     uint64_t P = 1, nq = 1, S = 1;
     uint64_t seg_len = 1;
     uint64_t items = 0;          // work items (ROW: rows x segments; COL: tiles x segments)
