@@ -52,6 +52,21 @@ __device__ __forceinline__ void load_a(const TA* p, T (&out)[V])
 #pragma unroll
     for (int v = 0; v < V; ++v) out[v] = Cvt<TA, T>::f(e[v]);
 }
+// The same through L1 (read-only path, default caching): for access
+// patterns where one thread reads consecutive vectors of a line that other
+// lanes do not share (one lane per row), so the second half of each 32-byte
+// sector is still in L1 when the thread's next load asks for it.
+template <typename TA, typename T, int V>
+__device__ __forceinline__ void load_a_l1(const TA* p, T (&out)[V])
+{
+    constexpr int B = (int)sizeof(TA) * V;
+    typedef typename RawVec<B>::type R;
+    R r = __ldg(reinterpret_cast<const R*>(p));
+    const TA* e = reinterpret_cast<const TA*>(&r);
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[v] = Cvt<TA, T>::f(e[v]);
+}
+
 template <> __device__ __forceinline__ void load_a<uint16_t, float, 1>(const uint16_t* p, float (&out)[1])
 {
     unsigned short r;

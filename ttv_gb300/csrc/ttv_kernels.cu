@@ -151,7 +151,10 @@ __device__ __forceinline__ void row_vecs(AccT (&acc)[V], const TA* ap, const T* 
     T av[UB][V], bv[UB][V];
 #pragma unroll
     for (int u = 0; u < UB; ++u) {
-        load_a<TA, T, V>(ap + (kv + u * G) * V, av[u]);
+        if (G == 1)   // one lane per row: keep the sector's other half in L1
+            load_a_l1<TA, T, V>(ap + (kv + u) * V, av[u]);
+        else
+            load_a<TA, T, V>(ap + (kv + u * G) * V, av[u]);
         load_b<T, V>(bp + (kv + u * G) * V, bv[u]);
     }
 #pragma unroll
