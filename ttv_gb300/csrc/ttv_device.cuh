@@ -114,12 +114,13 @@ template <typename T, bool KAHAN> struct Acc {
 //
 // GB300 executes about two DFMA per SM per clock (1.25 TFLOP/s), below the
 // one-per-element rate an HBM-bound fp64 TTV needs.  Each double x with
-// exponent in [2^-60, 2^61) is split into x = hi + lo with integer ops only:
-// hi = x cut to its top 24 significand bits (one funnel shift moves the
-// significand into float position, one add rebiases the exponent modulo 256,
-// one bit-select restores the sign); lo = the remaining 29 bits converted to
-// float (rounded to 24 bits, so |x - hi - lo| <= 2^-48 |x|) times
-// +-2^(e-1075), whose bit pattern is hi's sign and exponent minus 52.  The
+// exponent in [2^-60, 2^61) is split into x ~ hi + lo with integer ops and
+// one FP32 add: hi = x cut to its top 24 significand bits (one funnel shift
+// moves the significand into float position, one add rebiases the exponent
+// modulo 256, one bit-select restores the sign); lo = the next 23 bits, built
+// as the float 1.m * 2^(e-1046) minus 2^(e-1046) (exact).  The 6 lowest
+// significand bits are dropped: |x - hi - lo| < 2^-46 |x|.  No int -> float
+// conversion is used: on this part those issue at the FP64 pipe's rate.  The
 // product a*b = hi_a*hi_b + (hi_a*lo_b + lo_a*hi_b) keeps hi_a*hi_b exact
 // through Dekker's TwoProduct (one FMA gives its rounding error); lo_a*lo_b
 // (below 2^-48 of the product) is dropped.  The running sum is a double-float
