@@ -242,7 +242,8 @@ def run_ours(args, rank, world, local_rank):
                 T._p(keep[3]), Cv[dt].data_ptr(), *[T._p(k) for k in keep[4:]], sh)
         pl = T.plan(q, na, pia, dtype=T.F32 if dt == "f32" else T.F64)
         fam = {T.KIND_ROW: "row_kernel", T.KIND_COL: "col_kernel",
-               T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel"}[pl["kind"]]
+               T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel",
+               T.KIND_COL_THIN: "col_thin_kernel"}[pl["kind"]]
         kname = fam + f"<{dt}" + ("" if pl["kind"] == T.KIND_STREAM else f",V{pl['vec']}") + \
             (",kahan" if pl["accumulate"] == T.ACC_COMPENSATED and dt != "f64" else "") + ">"
         prepared.append((fn, argv, keep, case_bytes(c), kname, c))

@@ -58,6 +58,8 @@ extern "C" {
 #define TLIBG_KIND_STREAM 2        /* TMA-streamed rows (whole rows of <= 16 KB), any alignment     */
 #define TLIBG_KIND_COL_REALIGN 3   /* column GEMV with 16-byte loads realigned by warp shuffles,    */
                                    /*   for prefixes whose rows are not 16-byte aligned (fp32/fp64) */
+#define TLIBG_KIND_COL_THIN 4      /* column GEMV for thin prefixes (P / vector width divides 32):  */
+                                   /*   several rows per warp step, for few outputs and long q      */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */

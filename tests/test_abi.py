@@ -145,7 +145,7 @@ def test_planner_kernel_family(engine):
     # fp64 column kernel: the DFMA / double-float mix by default
     assert engine.plan(2, [64, 32, 16], [1, 2, 3], dtype=engine.F64)["accumulate"] == \
         engine.ACC_COMPENSATED
-    assert engine.plan(2, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_COL
+    assert engine.plan(2, [256, 32, 64], [1, 2, 3])["kind"] == engine.KIND_COL
     # its column form on request
     assert engine.plan(2, [645, 645, 645], [1, 2, 3], kind=engine.KIND_STREAM)["kind"] == \
         engine.KIND_STREAM
@@ -165,6 +165,13 @@ def test_planner_kernel_family(engine):
         engine.KIND_COL_REALIGN
     with pytest.raises(engine.TTVError, match="realigning column kernel"):
         engine.plan(1, [25, 25, 25], [1, 2, 3], kind=engine.KIND_COL_REALIGN)
+    # thin prefix, few outputs, long contraction: several rows per warp step
+    assert engine.plan(2, [64, 1 << 22], [1, 2])["kind"] == engine.KIND_COL_THIN
+    assert engine.plan(2, [16, 1 << 20, 16], [1, 2, 3])["kind"] == engine.KIND_COL_THIN
+    assert engine.plan(2, [64, 1 << 22], [1, 2], dtype=engine.F64)["kind"] == engine.KIND_COL_THIN
+    assert engine.plan(2, [16, 16, 1 << 20], [1, 2, 3])["kind"] == engine.KIND_COL   # many outputs
+    with pytest.raises(engine.TTVError, match="thin-prefix column kernel"):
+        engine.plan(2, [24, 1000], [1, 2], kind=engine.KIND_COL_THIN)
     # forced register kernels
     R, Cn = engine.KIND_ROW, engine.KIND_COL
     assert engine.plan(1, [64, 32, 16], [1, 2, 3], kind=R)["kind"] == R
@@ -180,7 +187,7 @@ def test_planner_kernel_family(engine):
         engine.plan(1, [16384, 16384], [1, 2], kind=engine.KIND_STREAM)
     # long contraction with a thin prefix is split, and segments fit the staged b
     pl = engine.plan(2, [64, 1 << 22], [1, 2], kind=Cn)
-    assert pl["split"] >= (1 << 22) // 4096
+    assert pl["kind"] == Cn and pl["split"] >= (1 << 22) // 4096
     assert engine.plan(2, [64, 1 << 22], [1, 2], kind=engine.KIND_STREAM)["split"] > 1
     # forced options are honoured or refused
     assert engine.plan(2, [256, 256, 256], [1, 2, 3], kind=Cn, group=2, split=3)["group"] == 2

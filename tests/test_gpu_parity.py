@@ -479,3 +479,39 @@ def test_short_rows(engine, orc, torch_dev):
                     for acc in accs:
                         check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
                               kind=engine.KIND_ROW, group=g, vec=v, accumulate=acc)
+
+
+THIN_SHAPES = [
+    ([64, 50000], [1, 2], 2),
+    ([16, 30000, 3], [1, 2, 3], 2),
+    ([4, 70000], [1, 2], 2),
+    ([2, 9000, 5], [1, 2, 3], 2),
+    ([128, 5000], [1, 2], 2),
+    ([8, 4, 20000], [1, 2, 3], 3),
+]
+
+
+@pytest.mark.parametrize("na,pia,q", THIN_SHAPES)
+def test_thin_prefix_column_kernel(engine, orc, torch_dev, na, pia, q):
+    """Thin prefixes (P / V divides 32), few outputs, long contraction: several
+    rows per warp step, every vector width and split, fp32 and fp64 both
+    accumulation modes."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(sum(na) + 3 * q)
+    P, nq, S = orc.canonical(na, pia, q)
+    for dt in (np.float32, np.float64):
+        a = rng.uniform(-1, 1, int(np.prod(na))).astype(dt)
+        b = rng.uniform(-1, 1, nq).astype(dt)
+        truth = orc.truth(S, nq, P, a, b)
+        vmax = 16 // np.dtype(dt).itemsize
+        bmax = 16384 // np.dtype(dt).itemsize
+        for v in (1, 2, 4):
+            if v > vmax or P % v or 32 % (P // v):
+                continue
+            for split in (0, 1, 3, 17):
+                if 0 < split < -(-nq // bmax):
+                    continue
+                for acc in (engine.ACC_COMPENSATED, engine.ACC_PLAIN):
+                    check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
+                          kind=engine.KIND_COL_THIN, vec=v, split=split, accumulate=acc)
+        check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth)   # the planner's choice

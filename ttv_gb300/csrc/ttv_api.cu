@@ -409,8 +409,10 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     if (opt && opt->kind == KIND_COL_REALIGN && !realign_ok)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: the realigning column kernel needs prefix P > 1 and "
                                         "fp32 or fp64 A");
+    if (opt && opt->kind == KIND_COL_THIN && cn.P == 1)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the thin-prefix column kernel needs prefix P > 1");
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
-        opt->kind != pl.kind)
+        opt->kind != KIND_COL_THIN && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
     // default for q-fastest rows: the register row kernel when rows allow 16-byte loads;
@@ -505,6 +507,50 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     } else {
         const uint64_t outputs = cn.S * cn.P;
         const uint64_t bmax = BSTAGE_BYTES / et;
+        // thin prefix: P / V lanes cover a row and divide the warp
+        const uint64_t PV = cn.P / V;
+        const bool thin_shape = pl.kind == KIND_COL && cn.P % V == 0 && PV <= 32 && 32 % PV == 0;
+        if (opt && opt->kind == KIND_COL_THIN && !thin_shape)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: the thin-prefix column kernel needs P / vector width "
+                                            "to divide 32");
+        bool thin = opt && opt->kind == KIND_COL_THIN;
+        if (!thin && thin_shape && !(opt && opt->kind >= 0)) {
+            // few outputs: the plain column kernel would leave most lanes idle
+            const uint64_t TO1 = (uint64_t)(BLOCK / 32) * 32 * V;
+            Plan probe = pl;
+            probe.group = 1;
+            thin = cdiv(outputs, TO1) < (uint64_t)sms * std::max(1, plan_ctas_per_sm(probe));
+        }
+        if (thin) {
+            pl.kind = KIND_COL_THIN;
+            pl.group = 1;
+            const int cps = std::max(1, plan_ctas_per_sm(pl));
+            const uint64_t grid_full = (uint64_t)sms * cps;
+            const uint64_t RG = 32 / PV;
+            const uint64_t min_len = (BLOCK / 32) * RG * 4;   // four loads per lane at least
+            uint64_t nseg = cdiv(cn.nq, bmax);
+            if (force_split > 0) {
+                if ((uint64_t)force_split < nseg)
+                    return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced split leaves a segment longer than the staged b buffer");
+                nseg = (uint64_t)force_split;
+            } else if (cn.S * nseg < 2 * grid_full) {
+                nseg = std::max<uint64_t>(nseg, std::min<uint64_t>(cdiv(2 * grid_full, cn.S),
+                                                                   std::max<uint64_t>(1, cn.nq / min_len)));
+            }
+            nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
+            const uint64_t seg_len = cdiv(cn.nq, nseg);
+            nseg = cdiv(cn.nq, seg_len);
+            pl.split = (int)nseg;
+            pl.seg_len = seg_len;
+            pl.items = cn.S * nseg;
+            const uint64_t grid = std::min<uint64_t>(grid_full, pl.items);
+            pl.items_per_cta = cdiv(pl.items, grid);
+            pl.grid = (int)cdiv(pl.items, pl.items_per_cta);
+            pl.f64_combine = (dtype != F64) && pl.split > 1 && cn.nq > (uint64_t(1) << 20);
+            pl.smem = plan_smem_bytes(pl);
+            *out = pl;
+            return TLIBG_OK;
+        }
         int WI = force_group > 0 ? force_group : 1;
         if (WI != 1 && WI != 2 && WI != 4 && WI != 8)
             return fail(TLIBG_ERR_ARGUMENT, "tlibg: warps along the contracted mode must be 1, 2, 4 or 8");

@@ -484,6 +484,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 
 #include "ttv_stream.cuh"
 #include "ttv_realign.cuh"
+#include "ttv_thin.cuh"
 
 namespace tlibg {
 
@@ -512,6 +513,15 @@ static KernelFn pick_main(int kind, int vec, int rows_m)
     if (kind == KIND_COL_REALIGN) {
         if constexpr (std::is_same<TA, T>::value) return col_realign_kernel<T, KAHAN>;
         else return nullptr;
+    }
+    if (kind == KIND_COL_THIN) {
+        switch (vec) {
+        case 1: return col_thin_kernel<TA, T, 1, KAHAN>;
+        case 2: return col_thin_kernel<TA, T, 2, KAHAN>;
+        case 4: if constexpr (VMAX >= 4) return col_thin_kernel<TA, T, 4, KAHAN>; else return nullptr;
+        case 8: if constexpr (VMAX >= 8) return col_thin_kernel<TA, T, 8, KAHAN>; else return nullptr;
+        }
+        return nullptr;
     }
     if (kind == KIND_ROW && rows_m == 1) return pick_short<TA, T, 1, KAHAN>(vec);
     if (kind == KIND_ROW && rows_m == 2) return pick_short<TA, T, 2, KAHAN>(vec);
@@ -590,6 +600,7 @@ size_t plan_smem_bytes(const Plan& p)
     if (p.kind == KIND_ROW) return 0;
     const size_t es = acc_size(p.dtype);
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
+    if (p.kind == KIND_COL_THIN) return 16 + bcap * es + (size_t)(BLOCK / 32) * 32 * 2 * p.vec * es;
     const size_t WO = (BLOCK / 32) / p.group;
     const size_t red = p.group > 1 ? (size_t)(p.group - 1) * WO * 32 * 2 * p.vec * es : 0;
     return 16 + bcap * es + red;
@@ -677,7 +688,9 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     k.items_per_cta = plan.items_per_cta;
     k.nseg = (uint32_t)plan.split;
     k.group = (uint32_t)plan.group;
-    if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {
+    if (plan.kind == KIND_COL_THIN) {
+        k.ntiles = plan.S;
+    } else if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {
         const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec;
         k.ntiles = (plan.S * plan.P + TO - 1) / TO;
     } else {

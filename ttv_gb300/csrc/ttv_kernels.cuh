@@ -7,7 +7,7 @@
 namespace tlibg {
 
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
-enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3 };
+enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
