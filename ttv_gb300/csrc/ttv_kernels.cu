@@ -452,31 +452,53 @@ __global__ void __launch_bounds__(BLOCK) col_kernel(KArgs k)
 // --------------------------------------------------------------------------
 // combine kernel: C[o] = sum over segments of partial[seg][o], fixed order
 // --------------------------------------------------------------------------
+// tpo threads per output (a power of two): thread t sums segments t, t + tpo,
+// ... in order, then the tpo partial sums meet in a fixed shared-memory tree,
+// so the result is the same on every run.  Few outputs with many segments
+// (thin prefixes, long contractions) spread over the whole block.
 template <typename T, bool KAHAN, bool F64>
 __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restrict__ part,
                                                         T* __restrict__ out, uint64_t outputs,
-                                                        uint32_t nseg)
+                                                        uint32_t nseg, uint32_t tpo)
 {
-    for (uint64_t o = uint64_t(blockIdx.x) * BLOCK + threadIdx.x; o < outputs;
-         o += uint64_t(gridDim.x) * BLOCK) {
-        if (F64) {
-            double acc = 0.0;
-            for (uint32_t g = 0; g < nseg; ++g) {
+    __shared__ double red[2 * BLOCK];
+    const uint32_t t = threadIdx.x & (tpo - 1u);
+    const uint32_t ob = threadIdx.x / tpo;
+    const uint32_t opb = BLOCK / tpo;
+    for (uint64_t base = uint64_t(blockIdx.x) * opb; base < outputs; base += uint64_t(gridDim.x) * opb) {
+        const uint64_t o = base + ob;
+        double fs = 0.0;                 // F64: plain double sum
+        Acc<T, KAHAN> acc;               // else: compensated merge of (s, c) pairs
+        acc.init();
+        if (o < outputs) {
+            for (uint32_t g = t; g < nseg; g += tpo) {
                 const Pair<T> p = part[uint64_t(g) * outputs + o];
-                acc += (double)p.s - (double)p.c;
+                if (F64)
+                    fs += (double)p.s - (double)p.c;
+                else
+                    acc.merge(p.s, p.c);
             }
-            out[o] = (T)acc;
-        } else {
-            Acc<T, KAHAN> acc;
-            const Pair<T> p0 = part[o];
-            acc.s = p0.s;
-            acc.c = p0.c;
-            for (uint32_t g = 1; g < nseg; ++g) {
-                const Pair<T> p = part[uint64_t(g) * outputs + o];
-                acc.merge(p.s, p.c);
-            }
-            out[o] = acc.value();
         }
+        if (tpo > 1) {
+            red[2 * threadIdx.x] = F64 ? fs : (double)acc.s;
+            red[2 * threadIdx.x + 1] = F64 ? 0.0 : (double)acc.c;
+            __syncthreads();
+            for (uint32_t h = tpo >> 1; h > 0; h >>= 1) {
+                if (t < h) {
+                    const double os = red[2 * (threadIdx.x + h)], oc = red[2 * (threadIdx.x + h) + 1];
+                    if (F64) {
+                        fs += os;
+                    } else {
+                        acc.merge((T)os, (T)oc);
+                    }
+                    red[2 * threadIdx.x] = F64 ? fs : (double)acc.s;
+                    red[2 * threadIdx.x + 1] = F64 ? 0.0 : (double)acc.c;
+                }
+                __syncthreads();
+            }
+        }
+        if (t == 0 && o < outputs) out[o] = F64 ? (T)fs : acc.value();
+        if (tpo > 1) __syncthreads();
     }
 }
 
@@ -710,8 +732,15 @@ cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_
     cudaError_t err;
     {
         const uint64_t outputs = plan.S * plan.P;
-        int g = (int)((outputs + BLOCK - 1) / BLOCK);
-        if (g > 152 * 16) g = 152 * 16;
+        // threads per output: one when the outputs alone fill the GPU, else enough
+        // to give each thread about eight segments
+        uint32_t tpo = 1;
+        if (outputs < (uint64_t)152 * BLOCK * 4 && plan.split >= 16) {
+            tpo = 1;
+            while (tpo * 2 <= (uint32_t)BLOCK && tpo * 2 * 8 <= (uint32_t)plan.split) tpo *= 2;
+        }
+        const uint64_t opb = BLOCK / tpo;
+        int g = (int)std::min<uint64_t>(152 * 16, (outputs + opb - 1) / opb);
         if (g < 1) g = 1;
         switch (plan.dtype) {
         case F32:
@@ -719,20 +748,20 @@ cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_
             if (plan.f64_combine)
                 combine_kernel<float, true, true><<<g, BLOCK, 0, stream>>>(
                     static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
-                    (uint32_t)plan.split);
+                    (uint32_t)plan.split, tpo);
             else if (plan.kahan)
                 combine_kernel<float, true, false><<<g, BLOCK, 0, stream>>>(
                     static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
-                    (uint32_t)plan.split);
+                    (uint32_t)plan.split, tpo);
             else
                 combine_kernel<float, false, false><<<g, BLOCK, 0, stream>>>(
                     static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
-                    (uint32_t)plan.split);
+                    (uint32_t)plan.split, tpo);
             break;
         case F64:
             combine_kernel<double, false, false><<<g, BLOCK, 0, stream>>>(
                 static_cast<const Pair<double>*>(partial), static_cast<double*>(c), outputs,
-                (uint32_t)plan.split);
+                (uint32_t)plan.split, tpo);
             break;
         }
         err = cudaGetLastError();
