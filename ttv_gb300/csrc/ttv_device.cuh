@@ -152,6 +152,11 @@ __device__ __forceinline__ DSplit split_double(double x)
     return r;
 }
 
+// Out-of-window products: a real call, so the compiler cannot turn the rare
+// branch into a predicated DFMA that would take an FP64 issue slot for every
+// in-window product as well.
+static __device__ __noinline__ double dfma_out_of_window(double a, double b, double d) { return fma(a, b, d); }
+
 struct AccDF {
     double s, c;    // folded value (after fold()); c stays 0
     float hi, lo;   // double-float running sum
@@ -176,7 +181,7 @@ struct AccDF {
             lo += ((hi - (sum - v)) + (p - v)) + t;
             hi = sum;
         } else {
-            d = fma(ad, bd, d);
+            d = dfma_out_of_window(ad, bd, d);
         }
     }
     __device__ __forceinline__ void renorm()
