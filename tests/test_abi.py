@@ -136,11 +136,11 @@ def test_metadata_helpers_match_reference(engine):
 
 
 def test_planner_kernel_family(engine):
-    # q-fastest rows: aligned -> register row kernel; unaligned and within a 16 KB
-    # stage -> the streamed kernel (row form); long unaligned fp64 rows -> row kernel
+    # q-fastest rows: aligned -> register row kernel; unaligned fp32 within a 16 KB
+    # stage -> the streamed kernel (row form); fp64 rows -> row kernel
     assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
     assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_STREAM
-    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_STREAM
+    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
     assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
     # fp64 column kernel: the DFMA / double-float mix by default
     assert engine.plan(2, [64, 32, 16], [1, 2, 3], dtype=engine.F64)["accumulate"] == \
@@ -152,10 +152,11 @@ def test_planner_kernel_family(engine):
     # long rows: the register kernels (q fastest -> row kernel, else column kernel)
     assert engine.plan(1, [16384, 16384], [1, 2])["kind"] == engine.KIND_ROW
     assert engine.plan(2, [16384, 16384], [1, 2])["kind"] == engine.KIND_COL
-    # fp32 rows of the prefix not 16-byte aligned: shuffle-realigned loads from 4 KB rows
-    # (2 KB with a short contraction); fp64 keeps scalar 8-byte loads
+    # fp32 rows of the prefix not 16-byte aligned: shuffle-realigned loads from 4 KB rows;
+    # fp64 keeps scalar 8-byte loads
     assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL_REALIGN
-    assert engine.plan(3, [25, 25, 25, 25], [1, 2, 3, 4])["kind"] == engine.KIND_COL_REALIGN
+    assert engine.plan(3, [25, 25, 25, 25], [1, 2, 3, 4])["kind"] == engine.KIND_COL
+    assert engine.plan(4, [25, 25, 25, 25], [1, 2, 3, 4])["kind"] == engine.KIND_COL_REALIGN
     assert engine.plan(2, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL
     assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_COL
     assert engine.plan(3, [645, 645, 645], [1, 2, 3])["vec"] == 4
