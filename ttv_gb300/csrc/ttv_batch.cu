@@ -238,46 +238,6 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
 // --------------------------------------------------------------------------
 // the persistent executor
 // --------------------------------------------------------------------------
-// Loads kept in flight per thread: 4 of 16 bytes, else 128 bytes (at most 16).
-template <int V> __host__ __device__ constexpr int batch_loads()
-{
-    return 4 * V >= 16 ? 4 : (128 / (4 * V) > 16 ? 16 : 128 / (4 * V));
-}
-
-// UB vectors of a row segment (row form) / UB rows of the contracted mode
-// (column form): every load first, then the products.
-template <int UB, int V, bool KAHAN>
-__device__ __forceinline__ void brow_vecs(Acc<float, KAHAN> (&acc)[V], const float* ap, const float* bp,
-                                          uint64_t kv, uint32_t G)
-{
-    float av[UB][V], bv[UB][V];
-#pragma unroll
-    for (int u = 0; u < UB; ++u) {
-        load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
-#pragma unroll
-        for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
-    }
-#pragma unroll
-    for (int u = 0; u < UB; ++u)
-#pragma unroll
-        for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
-}
-
-template <int UB, int V, bool KAHAN>
-__device__ __forceinline__ void bcol_rows(Acc<float, KAHAN> (&acc)[V], const float* ap, uint64_t P, const float* b,
-                                          uint64_t i, uint32_t WI)
-{
-    float av[UB][V];
-#pragma unroll
-    for (int u = 0; u < UB; ++u) load_a<float, float, V>(ap + (i + u * WI) * P, av[u]);
-#pragma unroll
-    for (int u = 0; u < UB; ++u) {
-        const float bb = __ldg(b + i + u * WI);
-#pragma unroll
-        for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
-    }
-}
-
 template <int V, bool KAHAN>
 __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPair* __restrict__ part)
 {
@@ -285,7 +245,7 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
     const uint64_t gpc = BLOCK / G;
     const uint64_t items = P.S * P.nseg;
     const uint64_t R = rows_per_group(P.seg_len, G);
-    constexpr int U = batch_loads<V>();
+    constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
     for (uint64_t r = 0; r < R; ++r) {
         const uint64_t item = (lu * R + r) * gpc + threadIdx.x / G;
         const bool valid = item < items;
@@ -302,20 +262,26 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
             const float* bp = P.b + ib;
             const uint64_t n = ie - ib, nv = n / V;
             uint64_t kv = gl;
-            for (; kv + (U - 1) * (uint64_t)G < nv; kv += U * (uint64_t)G) brow_vecs<U, V>(acc, ap, bp, kv, G);
-            if constexpr (U >= 4) {
-                if (kv + (U / 2 - 1) * (uint64_t)G < nv) {
-                    brow_vecs<U / 2, V>(acc, ap, bp, kv, G);
-                    kv += (U / 2) * (uint64_t)G;
+            for (; kv + (U - 1) * G < nv; kv += U * G) {
+                float av[U][V], bv[U][V];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
                 }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
             }
-            if constexpr (U >= 8) {
-                if (kv + (U / 4 - 1) * (uint64_t)G < nv) {
-                    brow_vecs<U / 4, V>(acc, ap, bp, kv, G);
-                    kv += (U / 4) * (uint64_t)G;
-                }
+#pragma unroll 4
+            for (; kv < nv; kv += G) {
+                float av[V];
+                load_a<float, float, V>(ap + kv * V, av);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
             }
-            for (; kv < nv; kv += G) brow_vecs<1, V>(acc, ap, bp, kv, G);
             for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
         }
 #pragma unroll
@@ -359,7 +325,7 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
     (void)bar;
     (void)phase;
     (void)abort_flag;
-    constexpr int U = batch_loads<V>();
+    constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
 
     const uint64_t o0 = tile * TO + ((uint64_t)wo * 32u + lane) * V;
     const bool valid = o0 < outputs;
@@ -371,20 +337,25 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
         const uint64_t j = o0 - s * P.P;
         const float* ap = P.a + (s * P.nq) * P.P + j;
         uint64_t i = ib + wi;
-        for (; i + (U - 1) * (uint64_t)WI < ie; i += U * (uint64_t)WI) bcol_rows<U, V>(acc, ap, P.P, bs, i, WI);
-        if constexpr (U >= 4) {
-            if (i + (U / 2 - 1) * (uint64_t)WI < ie) {
-                bcol_rows<U / 2, V>(acc, ap, P.P, bs, i, WI);
-                i += (U / 2) * (uint64_t)WI;
+        for (; i + (U - 1) * WI < ie; i += U * WI) {
+            float av[U][V];
+#pragma unroll
+            for (int u = 0; u < U; ++u) load_a<float, float, V>(ap + (i + u * WI) * P.P, av[u]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float bb = __ldg(bs + i + u * WI);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
             }
         }
-        if constexpr (U >= 8) {
-            if (i + (U / 4 - 1) * (uint64_t)WI < ie) {
-                bcol_rows<U / 4, V>(acc, ap, P.P, bs, i, WI);
-                i += (U / 4) * (uint64_t)WI;
-            }
+#pragma unroll 4
+        for (; i < ie; i += WI) {
+            float av[V];
+            load_a<float, float, V>(ap + i * P.P, av);
+            const float bb = __ldg(bs + i);
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
         }
-        for (; i < ie; i += WI) bcol_rows<1, V>(acc, ap, P.P, bs, i, WI);
     }
     if (WI > 1) {
         const uint32_t slot = wo * 32u + lane;
