@@ -364,7 +364,7 @@ def run_ours(args, rank, world, local_rank):
             Bv.clear()
             Cv.clear()
             torch.cuda.empty_cache()
-            out["batched"] = run_batched(T, torch, dev, args)
+            out["batched"] = run_batched(T, torch, dev, args, n=args.batch_problems)
     return out
 
 
@@ -649,7 +649,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sym")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="sym")
+    ap.add_argument("--batch-problems", type=int, default=4096,
+                    help="problems per launch of the batched configuration")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -678,6 +680,14 @@ def main():
     if args.workload == "precision":
         if rank == 0:
             print(json.dumps(run_precision(args)), flush=True)
+        return
+    if args.workload == "batch":
+        # the batched configuration alone (profiling; --batch-problems sets its size)
+        if rank == 0:
+            import torch
+            import ttv_gb300 as T
+            dev = torch.device("cuda", 0)
+            print(json.dumps(run_batched(T, torch, dev, args, n=args.batch_problems)), flush=True)
         return
     if world > 1:
         import torch
