@@ -14,7 +14,13 @@
  *   execution_policy::gpu_on(s)    enqueue on CUDA stream s, return at once
  *
  * Any slicing_policy / fusion_policy tag is accepted; the engine always fuses
- * every free mode into one grid (the reference's fusion_policy::all).
+ * every free mode into one grid (the reference's fusion_policy::all).  When
+ * a, b and c are all host pointers (for instance the data of the reference's
+ * own tensor<T>, so that its high-level ttv(q, A, b, gpu, ...) works as is),
+ * the call takes the engine's host path and is synchronous.
+ *
+ * tlib/ttv_gpu_tensor.h adds a device-resident tensor with the reference's
+ * tensor / tensor_view / A(q) * b interface.
  *
  * Include this header INSTEAD OF (or before) <tlib/ttv.h>: the reference
  * dispatches through a qualified call, so the overloads must be declared
@@ -103,6 +109,10 @@ template <class size_type> struct Sizes {
     }
 };
 
+// Device pointers run on the device (asynchronously for gpu_on); when a, b
+// and c all live in host memory -- the reference's own tensor<T> keeps its
+// data in a std::vector -- the call goes through the engine's host path
+// (copies in, computes on the GPU, copies C back; synchronous either way).
 template <class value_t, class size_type>
 inline void run(void* stream, bool sync, std::size_t q, std::size_t p, const value_t* a,
                 const size_type* na, const size_type* wa, const size_type* pia, const value_t* b,
@@ -113,6 +123,12 @@ inline void run(void* stream, bool sync, std::size_t q, std::size_t p, const val
     Sizes<size_type> sna(na, p), swa(wa, p), spia(pia, p), snb(nb, 1), snc(nc, pc), swc(wc, pc),
         spic(pic, pc);
     tlibg_options opt{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, sync ? 1 : 0};
+    if (a && b && c && tlibg_pointer_location(a) == 0 && tlibg_pointer_location(b) == 0 &&
+        tlibg_pointer_location(c) == 0) {
+        throw_status(tlibg_ttv_host(dtype_of<value_t>(), q, p, a, sna.ptr, swa.ptr, spia.ptr, b,
+                                    snb.ptr, c, snc.ptr, swc.ptr, spic.ptr, &opt));
+        return;
+    }
     throw_status(tlibg_ttv_ex(dtype_of<value_t>(), q, p, a, sna.ptr, swa.ptr, spia.ptr, b, snb.ptr,
                               c, snc.ptr, swc.ptr, spic.ptr, &opt, stream));
 }

@@ -138,6 +138,12 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
  * use them.  opt == NULL removes the hint; with P = n_q = S = 0, all hints. */
 int tlibg_plan_hint(int dtype, uint64_t P, uint64_t nq, uint64_t S, const tlibg_options* opt);
 
+/* Where a pointer lives: 1 device or managed memory, 0 host memory (pageable
+ * or page-locked; every pointer when no device is present), -1 null or
+ * unknown.  The compute entry points refuse pageable host pointers
+ * (TLIBG_ERR_ARGUMENT) before any launch; host buffers go to tlibg_ttv_host. */
+int tlibg_pointer_location(const void* p);
+
 /* Validation only: the checks of the compute entry points (ttv.h:64-89 and
  * tensor_times_vector.h:147-168, in that order, same messages) on the metadata
  * alone, with no data pointers, no device and no launch.  Lets a host wrapper

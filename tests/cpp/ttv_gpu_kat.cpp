@@ -7,10 +7,15 @@
 //                          exception text equals the reference's
 //   ttv_gpu_kat kat        the KAT grid on the GPU (ranks 2-4, extents
 //                          {2, 4, 8}, every layout and q), float and double
+//   ttv_gpu_kat tensor     the device tensor interface (A(q) * b, ttv(q, A, b))
+//                          on the KAT grid of rank 3, host-pointer calls of the
+//                          gpu policy, and (with the reference headers) the
+//                          reference's own tensor<T> through the gpu policy
 //
 // Built with the reference headers on the include path (the policy hooks into
 // the reference's own dispatch) or without them (standalone mode).
 #include <tlib/ttv_gpu.h>
+#include <tlib/ttv_gpu_tensor.h>
 
 #include <cuda_runtime.h>
 
@@ -77,6 +82,26 @@ static int validate()
     expect_throw("wa", E + "stride vector of A is not valid.", 2, 3, a, na, sizes{1, 8, 2}, pia, b, nb, c, nc, wc, pic);
     expect_throw("pic", "Error in tlib::detail::compute_inverse_pia_m: beginning of layout tuples of both tensors are not correct.",
                  2, 3, a, na, wa, pia, b, nb, c, nc, sizes{4, 1}, sizes{2, 1});
+    // device tensor: the reference's constructor and call-operator checks
+    const std::string T = "Error in tlib::tensor: ";
+    auto expect_tensor_throw = [&](const char* what, const std::string& expected, auto&& make) {
+        try {
+            make();
+            std::printf("FAIL %s: no exception\n", what);
+            ++failures;
+        } catch (std::runtime_error const& e) {
+            if (std::string(e.what()).find(expected) == std::string::npos) {
+                std::printf("FAIL %s: got '%s'\n", what, e.what());
+                ++failures;
+            }
+        }
+    };
+    expect_tensor_throw("tensor lengths", T + "shape vector and layout vector must have the same length.",
+                        [] { tlib::ttv::gpu::tensor<float> x(sizes{2, 3}, sizes{1}); });
+    expect_tensor_throw("tensor shape", T + "shape vector of tensor is not valid.",
+                        [] { tlib::ttv::gpu::tensor<float> x(sizes{2, 0}, sizes{1, 2}); });
+    expect_tensor_throw("tensor layout", T + "layout vector of tensor is not valid.",
+                        [] { tlib::ttv::gpu::tensor<float> x(sizes{2, 3}, sizes{2, 2}); });
     // a valid call reaches the engine (host memory is not device memory: the
     // engine refuses without touching it when no device is present)
     int ndev = 0;
@@ -183,10 +208,86 @@ static int kat_rank(std::size_t rank)
     return bad;
 }
 
+// The device tensor interface on the rank-3 KAT grid, the gpu policy on host
+// pointers, and the reference's own tensor<T> through the gpu policy.
+template <class T>
+static int tensor_api()
+{
+    using gt = tlib::ttv::gpu::tensor<T>;
+    int bad = 0;
+    sizes perm{1, 2, 3};
+    do {
+        for (std::size_t q = 1; q <= 3; ++q) {
+            const sizes na{4, 2, 8};
+            const sizes wa = dense(na, perm);
+            std::vector<T> a(64);
+            init_kat(q, a, na, wa, perm);
+            gt A(na, perm, a);
+            gt b(sizes{na[q - 1]});
+            b = T(1);
+            for (int form = 0; form < 3; ++form) {
+                gt C = form == 0 ? A(q) * b : tlib::ttv::gpu::ttv(q, A, b);
+                std::vector<T> c = C.to_host();
+                if (form == 2) {
+                    // host pointers through the gpu policy: the engine's host path
+                    std::vector<T> bh(na[q - 1], T(1));
+                    const sizes nc = C.shape(), pic = C.layout(), wc = C.strides(), nb{na[q - 1]};
+                    std::fill(c.begin(), c.end(), T(-1));
+                    ttv(execution_policy::gpu, slicing_policy::subtensor, fusion_policy::all, q, std::size_t(3),
+                        a.data(), na.data(), wa.data(), perm.data(), bh.data(), nb.data(), c.data(), nc.data(),
+                        wc.data(), pic.data());
+                }
+                // C's elements in its own layout order are outputs 1, 2, 3, ...
+                const sizes nc = C.shape(), pic = C.layout(), wc = C.strides();
+                const std::size_t nq = na[q - 1];
+                sizes idx(2, 0);
+                for (std::size_t t = 0; t < c.size(); ++t) {
+                    const std::size_t off = idx[0] * wc[0] + idx[1] * wc[1];
+                    const std::size_t i = t + 1;
+                    const T want = T((nq * nq * (2 * i - 1) + nq) / 2);
+                    if (c[off] != want) {
+                        if (bad < 5) std::printf("tensor mismatch form %d q %zu: got %g want %g\n", form, q, double(c[off]), double(want));
+                        ++bad;
+                    }
+                    for (std::size_t d = 0; d < 2; ++d) {
+                        const std::size_t m = pic[d] - 1;
+                        if (++idx[m] < nc[m]) break;
+                        idx[m] = 0;
+                    }
+                }
+            }
+        }
+    } while (std::next_permutation(perm.begin(), perm.end()));
+#if TLIBG_WITH_REFERENCE
+    // the reference's own high-level call with its host tensor<T> and the gpu policy
+    tlib::ttv::tensor<T> Ah({4, 2, 8}, {1, 2, 3}), bh({2});
+    std::iota(Ah.begin(), Ah.end(), T(1));
+    std::fill(bh.begin(), bh.end(), T(1));
+    auto Ch = tlib::ttv::ttv(2, Ah, bh, execution_policy::gpu, slicing_policy::subtensor, fusion_policy::all);
+    auto Cr = tlib::ttv::ttv(2, Ah, bh, execution_policy::seq, slicing_policy::subtensor, fusion_policy::none);
+    if (!std::equal(Ch.begin(), Ch.end(), Cr.begin())) {
+        std::printf("reference tensor<T> through the gpu policy differs from its seq policy\n");
+        ++bad;
+    }
+    gt Ad(Ah);
+    auto Cd = (Ad(2) * gt(bh)).host();
+    if (!std::equal(Cd.begin(), Cd.end(), Cr.begin())) {
+        std::printf("device tensor made from the reference's tensor<T> differs\n");
+        ++bad;
+    }
+#endif
+    return bad;
+}
+
 int main(int argc, char** argv)
 {
     const std::string mode = argc > 1 ? argv[1] : "validate";
     if (mode == "validate") return validate();
+    if (mode == "tensor") {
+        const int bad = tensor_api<float>() + tensor_api<double>();
+        std::printf("%s tensor (%d mismatches)\n", bad ? "FAILED" : "PASSED", bad);
+        return bad ? 1 : 0;
+    }
     int bad = 0;
     for (std::size_t r = 2; r <= 4; ++r) bad += kat_rank<float>(r) + kat_rank<double>(r);
     std::printf("%s kat (%d mismatches)\n", bad ? "FAILED" : "PASSED", bad);

@@ -292,3 +292,19 @@ def test_element_misaligned_pointers_refused(engine):
                             *[engine._p(k) for k in meta[4:]], C.byref(o), None)
         assert st == engine.ERR_UNSUPPORTED, (dt, a, b, c, st)
         assert "aligned to their element sizes" in engine._last_error()
+
+
+def test_pointer_location_without_device(engine):
+    """No device in this process: every pointer is a host pointer; null is unknown."""
+    import ctypes
+    L = engine.library()
+    L.tlibg_pointer_location.argtypes = [ctypes.c_void_p]
+    buf = ctypes.create_string_buffer(64)
+    assert L.tlibg_pointer_location(None) == -1
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if not has_gpu:
+        assert L.tlibg_pointer_location(ctypes.addressof(buf)) == 0

@@ -99,6 +99,17 @@ def test_cpp_kat_through_policy(engine, cuda, tmp_path):
     assert r.returncode == 0 and "PASSED" in r.stdout, r.stdout + r.stderr
 
 
+def test_cpp_device_tensor_interface(engine, cuda, tmp_path):
+    """tlib/ttv_gpu_tensor.h: A(q) * b and ttv(q, A, b) on device tensors, the gpu
+    policy on host pointers (the engine's host path) and, where the reference
+    headers exist, the reference's own tensor<T> through the gpu policy."""
+    from test_abi import _compile_cpp
+    import subprocess
+    exe = _compile_cpp(tmp_path, standalone=True)
+    r = subprocess.run([exe, "tensor"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "PASSED" in r.stdout, r.stdout + r.stderr
+
+
 def test_golden_fixtures(engine, orc, torch_dev):
     """Outputs of the reference itself (fixtures made from it) on random inputs."""
     torch, dev = torch_dev
@@ -515,3 +526,18 @@ def test_thin_prefix_column_kernel(engine, orc, torch_dev, na, pia, q):
                     check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
                           kind=engine.KIND_COL_THIN, vec=v, split=split, accumulate=acc)
         check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth)   # the planner's choice
+
+
+def test_pageable_host_pointers_refused(engine, torch_dev):
+    """Pageable host memory never reaches a kernel: the C ABI refuses it (the
+    host path, tlibg_ttv_host, is the way for host buffers)."""
+    torch, dev = torch_dev
+    na, pia, q = [8, 16, 4], [1, 2, 3], 2
+    wa, nc, wc, pic = meta(engine, na, pia, q)
+    a_h, b_h, c_h = torch.rand(512), torch.rand(16), torch.zeros(32)
+    a_d, b_d, c_d = a_h.to(dev), b_h.to(dev), c_h.to(dev)
+    for a, b, c in ((a_h, b_d, c_d), (a_d, b_h, c_d), (a_d, b_d, c_h)):
+        with pytest.raises(engine.TTVError, match="device-accessible"):
+            engine.ttv(q, 3, a, na, wa, pia, b, [16], c, nc, wc, pic, sync=True)
+    engine.ttv(q, 3, a_d, na, wa, pia, b_d, [16], c_d, nc, wc, pic, sync=True)   # still usable
+    assert engine.device_error() == 0

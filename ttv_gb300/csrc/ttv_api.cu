@@ -635,6 +635,24 @@ int get_scratch(cudaStream_t stream, size_t bytes, void** out)
     return TLIBG_OK;
 }
 
+// Pageable host memory is not addressable by the kernels: refuse it up front
+// (pinned host memory and managed memory are device-accessible and pass).
+int check_device_pointers(const void* a, const void* b, const void* c)
+{
+    for (const void* p : {a, b, c}) {
+        cudaPointerAttributes at{};
+        const cudaError_t e = cudaPointerGetAttributes(&at, p);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cuda_fail(e, "cudaPointerGetAttributes");
+        }
+        if (at.type == cudaMemoryTypeUnregistered)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: a, b and c must be device-accessible pointers "
+                                            "(host buffers: tlibg_ttv_host)");
+    }
+    return TLIBG_OK;
+}
+
 // Every kernel addresses A, b and C per element (and wider): pointers must
 // be aligned to their element types, as a C or C++ caller's own are.
 int check_elem_align(int dtype, const void* a, const void* b, const void* c)
@@ -655,6 +673,8 @@ int run_device(int dtype, size_t q, size_t p, const void* a, const size_t* na, c
     if (st) return st;
     DevInfo d = dev_info();
     if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    st = check_device_pointers(a, b, c);
+    if (st) return st;
     Plan pl;
     st = make_plan(dtype, cn, a, b, opt, d.sms, &pl);
     if (st) return st;
@@ -724,6 +744,23 @@ int tlibg_validate(size_t q, size_t p, const size_t* na, const size_t* wa, const
     Canon cn;
     const int st = analyse(q, p, &stand_in, na, wa, pia, &stand_in, nb, &stand_in, nc, wc, pic, &cn);
     return st ? st : ok();
+}
+
+int tlibg_pointer_location(const void* p)
+{
+    if (!p) return -1;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return 0;   // no device: every pointer is a host pointer
+    }
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return 1;
+    return 0;
 }
 
 int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pia,
@@ -1047,6 +1084,8 @@ extern "C" int tlibg_ttv_f32_noalloc(size_t q, size_t p, const float* a, const s
     if (st) return st;
     DevInfo d = dev_info();
     if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    st = check_device_pointers(a, b, c);
+    if (st) return st;
     Plan pl;
     st = make_plan(F32, cn, a, b, nullptr, d.sms, &pl);
     if (st) return st;
@@ -1109,6 +1148,10 @@ int internal_sms()
 
 int internal_fail(int code, const std::string& msg) { return fail(code, msg); }
 int internal_ok() { return ok(); }
+int internal_check_device_pointers(const void* a, const void* b, const void* c)
+{
+    return check_device_pointers(a, b, c);
+}
 int internal_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
 void internal_count_launches(uint64_t n) { g_launches += n; }
 

@@ -711,6 +711,11 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
     uint64_t total_units = 0, max_part = 0;
     for (size_t i = 0; i < count; ++i) {
         const tlibg_problem& x = probs[i];
+        s = internal_check_device_pointers(x.a, x.b, x.c);
+        if (s) {
+            release(bt);
+            return s;
+        }
         CanonView cn;
         internal_analyse(x.q, x.p, x.a, x.na, x.wa, x.pia, x.b, x.nb, x.c, x.nc, x.wc, x.pic, &cn);
         BProb& b = hp[i];

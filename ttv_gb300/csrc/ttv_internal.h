@@ -26,6 +26,8 @@ int internal_plan(int dtype, const CanonView& cn, const void* a, const void* b,
                   const tlibg_options* opt, int sms, Plan* out);
 // Streaming multiprocessors of the current device (0 without a device).
 int internal_sms();
+// Refuse pageable host pointers among a, b, c (sets the last error).
+int internal_check_device_pointers(const void* a, const void* b, const void* c);
 int internal_fail(int code, const std::string& msg);
 int internal_ok();
 int internal_cuda_fail(cudaError_t e, const char* where);
