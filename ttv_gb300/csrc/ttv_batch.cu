@@ -413,7 +413,14 @@ __device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __r
 }
 
 template <bool KAHAN>
-__global__ void __launch_bounds__(BLOCK) batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map,
+// Resident CTAs per SM the executor is compiled for (registers capped so that
+// this many fit): more warps in flight per SM for the latency-bound units.
+// Measured on GB300 (4096 uneven problems, fixed rule): 1 -> 6.1 ms,
+// 5 -> 3.9 ms, 6 -> 3.7 ms, 7 and 8 -> 3.5 ms per launch, despite spills.
+#ifndef TLIBG_BATCH_MIN_CTAS
+#define TLIBG_BATCH_MIN_CTAS 8
+#endif
+__global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS) batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map,
                                                     BCtl* ctl, BPair* __restrict__ part)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
