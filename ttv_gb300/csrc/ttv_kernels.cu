@@ -40,17 +40,15 @@ template <typename T> struct Pair {
 // TLIBG_NARROW_INFLIGHT bytes (at most 16 loads) for narrower loads, so
 // misaligned or odd-extent layouts still cover the HBM latency-bandwidth
 // product.
-// Resident CTAs per SM each kernel family is compiled for (registers capped
-// accordingly; 1 = no cap).
-#ifndef TLIBG_ROW_MIN_CTAS
-#define TLIBG_ROW_MIN_CTAS 1
-#endif
-#ifndef TLIBG_COL_MIN_CTAS
-#define TLIBG_COL_MIN_CTAS 1
-#endif
-#ifndef TLIBG_REALIGN_MIN_CTAS
-#define TLIBG_REALIGN_MIN_CTAS 1
-#endif
+// Resident CTAs per SM the register kernels are compiled for (the
+// __launch_bounds__ minimum): 4 for 16-byte loads, 1 for narrower ones.
+// Measured on GB300 over the symmetric sweep against other targets (1, 4, 5,
+// 6) and against no minimum: column fp32 V4 5.92 -> 6.57 TB/s, fp64 V2
+// 6.19 -> 6.25, row fp32 V4 6.05 -> 6.46; narrow loads lose with 4.
+template <typename TA, int V> __host__ __device__ constexpr int min_ctas()
+{
+    return (int)sizeof(TA) * V >= 16 ? 4 : 1;
+}
 
 #ifndef TLIBG_NARROW_INFLIGHT
 #define TLIBG_NARROW_INFLIGHT 128
@@ -241,7 +239,7 @@ __device__ __forceinline__ void row_short(const KArgs& k, uint32_t G, uint32_t l
 }
 
 template <typename TA, typename T, int V, bool KAHAN>
-__global__ void __launch_bounds__(BLOCK, TLIBG_ROW_MIN_CTAS) row_kernel(KArgs k)
+__global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k)
 {
     const uint32_t G = k.group;
     const uint32_t lane = threadIdx.x & 31u;
@@ -318,7 +316,7 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_ROW_MIN_CTAS) row_kernel(KArgs k)
 // Short rows as their own kernel (its registers do not weigh on the general
 // row kernel): M vectors per lane of each row, R = U / M rows in flight.
 template <typename TA, typename T, int V, bool KAHAN, int M>
-__global__ void __launch_bounds__(BLOCK, TLIBG_ROW_MIN_CTAS) row_short_kernel(KArgs k)
+__global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_short_kernel(KArgs k)
 {
     constexpr int U = loads_in_flight<TA, V>();
     constexpr int R = M == 1 ? U : (U >= 2 ? U / 2 : 1);
@@ -331,7 +329,7 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_ROW_MIN_CTAS) row_short_kernel(KA
 // column kernel: P > 1
 // --------------------------------------------------------------------------
 template <typename TA, typename T, int V, bool KAHAN>
-__global__ void __launch_bounds__(BLOCK, TLIBG_COL_MIN_CTAS) col_kernel(KArgs k)
+__global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);

@@ -37,7 +37,7 @@ __device__ __forceinline__ void realign_vec(const T (&c)[V], const T (&n)[V], ui
 }
 
 template <typename T, bool KAHAN>
-__global__ void __launch_bounds__(BLOCK, TLIBG_REALIGN_MIN_CTAS) col_realign_kernel(KArgs k)
+__global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
 {
     constexpr int V = 16 / (int)sizeof(T);
     constexpr int U = 4;

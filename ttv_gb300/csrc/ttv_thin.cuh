@@ -14,7 +14,7 @@
 namespace tlibg {
 
 template <typename TA, typename T, int V, bool KAHAN>
-__global__ void __launch_bounds__(BLOCK, TLIBG_COL_MIN_CTAS) col_thin_kernel(KArgs k)
+__global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KArgs k)
 {
     constexpr int NW = BLOCK / 32;
     constexpr int U = loads_in_flight<TA, V>();
