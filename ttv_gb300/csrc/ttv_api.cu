@@ -293,6 +293,10 @@ int pow2_floor(uint64_t x)
 
 // Streamed kernel: A as rows of L contiguous elements, R rows per 16 KB chunk,
 // a static block of units per CTA (row form: rows; column form: (s, segment)).
+#ifndef TLIBG_SCALAR_OUTPUTS
+#define TLIBG_SCALAR_OUTPUTS 2
+#endif
+
 int make_stream_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
 {
     const size_t ea = elem_size_a(pl.dtype);
@@ -553,7 +557,9 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         int WI = force_group > 0 ? force_group : 1;
         if (WI != 1 && WI != 2 && WI != 4 && WI != 8)
             return fail(TLIBG_ERR_ARGUMENT, "tlibg: warps along the contracted mode must be 1, 2, 4 or 8");
-        auto tiles_for = [&](int wi) { return cdiv(outputs, (uint64_t)((BLOCK / 32) / wi) * 32 * V); };
+        // scalar loads: several outputs per thread, 32 apart (more loads in flight per row)
+        if (pl.kind == KIND_COL && V == 1) pl.mo = TLIBG_SCALAR_OUTPUTS;
+        auto tiles_for = [&](int wi) { return cdiv(outputs, (uint64_t)((BLOCK / 32) / wi) * 32 * V * pl.mo); };
         pl.group = WI;
         int cps = std::max(1, plan_ctas_per_sm(pl));
         // Measured on GB300 (tuner sweeps): one warp row per tile and no split are best

@@ -517,6 +517,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 #include "ttv_stream.cuh"
 #include "ttv_realign.cuh"
 #include "ttv_thin.cuh"
+#include "ttv_strided.cuh"
 
 namespace tlibg {
 
@@ -539,9 +540,11 @@ static KernelFn pick_short(int vec)
 }
 
 template <typename TA, typename T, bool KAHAN>
-static KernelFn pick_main(int kind, int vec, int rows_m)
+static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
+    if (kind == KIND_COL && vec == 1 && mo == 2) return col_strided_kernel<TA, T, 2, KAHAN>;
+    if (kind == KIND_COL && vec == 1 && mo == 4) return col_strided_kernel<TA, T, 4, KAHAN>;
     if (kind == KIND_COL_REALIGN) {
         if constexpr (std::is_same<TA, T>::value) return col_realign_kernel<T, KAHAN>;
         else return nullptr;
@@ -607,14 +610,14 @@ static KernelFn main_kernel(const Plan& p)
     if (p.kind == KIND_STREAM) return reinterpret_cast<KernelFn>(stream_fn(p));
     switch (p.dtype) {
     case F32:
-        return p.kahan ? pick_main<float, float, true>(p.kind, p.vec, p.rows_m)
-                       : pick_main<float, float, false>(p.kind, p.vec, p.rows_m);
+        return p.kahan ? pick_main<float, float, true>(p.kind, p.vec, p.rows_m, p.mo)
+                       : pick_main<float, float, false>(p.kind, p.vec, p.rows_m, p.mo);
     case F64:
-        return p.kahan ? pick_main<double, double, true>(p.kind, p.vec, p.rows_m)
-                       : pick_main<double, double, false>(p.kind, p.vec, p.rows_m);
+        return p.kahan ? pick_main<double, double, true>(p.kind, p.vec, p.rows_m, p.mo)
+                       : pick_main<double, double, false>(p.kind, p.vec, p.rows_m, p.mo);
     case BF16A:
-        return p.kahan ? pick_main<uint16_t, float, true>(p.kind, p.vec, p.rows_m)
-                       : pick_main<uint16_t, float, false>(p.kind, p.vec, p.rows_m);
+        return p.kahan ? pick_main<uint16_t, float, true>(p.kind, p.vec, p.rows_m, p.mo)
+                       : pick_main<uint16_t, float, false>(p.kind, p.vec, p.rows_m, p.mo);
     }
     return nullptr;
 }
@@ -634,7 +637,7 @@ size_t plan_smem_bytes(const Plan& p)
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
     if (p.kind == KIND_COL_THIN) return 16 + bcap * es + (size_t)(BLOCK / 32) * 32 * 2 * p.vec * es;
     const size_t WO = (BLOCK / 32) / p.group;
-    const size_t red = p.group > 1 ? (size_t)(p.group - 1) * WO * 32 * 2 * p.vec * es : 0;
+    const size_t red = p.group > 1 ? (size_t)(p.group - 1) * WO * 32 * 2 * p.vec * p.mo * es : 0;
     return 16 + bcap * es + red;
 }
 
@@ -723,7 +726,7 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     if (plan.kind == KIND_COL_THIN) {
         k.ntiles = plan.S;
     } else if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {
-        const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec;
+        const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec * plan.mo;
         k.ntiles = (plan.S * plan.P + TO - 1) / TO;
     } else {
         k.ntiles = 0;

@@ -24,6 +24,7 @@ struct Plan {
     int split = 1;        // segments of the contracted mode
     int kahan = 1;        // compensated fp32 accumulation
     int rows_m = 0;       // ROW: 1 or 2 = short-row kernel (at most rows_m vectors per lane of a row)
+    int mo = 1;           // COL with scalar loads: outputs per thread, 32 apart (strided kernel when > 1)
     uint64_t P = 1, nq = 1, S = 1;
     uint64_t seg_len = 1;
     uint64_t items = 0;          // work items (ROW: rows x segments; COL: tiles x segments)

@@ -1,0 +1,158 @@
+// Column kernel for scalar loads with several outputs per thread (included by
+// ttv_kernels.cu).
+//
+// Prefixes whose rows allow no vector load (P odd, or A at an odd element
+// offset) and are too short for the realigned kernel: each thread owns MO
+// outputs 32 apart (o, o + 32, ...), so every warp load of every output set
+// is still one coalesced run of 32 elements, and each row i puts MO
+// independent loads in flight per thread instead of one.  Short contractions
+// (a few dozen rows) then need half or a quarter of the round trips per
+// output.  Tiles, the b stage, warps stacked along q and the split reduction
+// are those of the column kernel.
+#pragma once
+
+namespace tlibg {
+
+template <int UB, int MO, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* A, const uint64_t (&ofs)[MO],
+                                             const bool (&ok)[MO], uint64_t P, const T* bs, uint64_t i, uint32_t WI)
+{
+    T av[UB][MO];
+#pragma unroll
+    for (int u = 0; u < UB; ++u)
+#pragma unroll
+        for (int m = 0; m < MO; ++m) {
+            if (ok[m]) {
+                T x[1];
+                load_a<TA, T, 1>(A + ofs[m] + (i + u * WI) * P, x);
+                av[u][m] = x[0];
+            } else {
+                av[u][m] = T(0);
+            }
+        }
+#pragma unroll
+    for (int u = 0; u < UB; ++u) row_fma<MO>(acc, av[u], bs[i + u * WI], u);
+    renorm_all<MO>(acc);
+}
+
+template <typename TA, typename T, int MO, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
+    T* sb = reinterpret_cast<T*>(smem_raw + 16);
+    constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));
+
+    const uint32_t WI = k.group;
+    const uint32_t WO = (BLOCK / 32) / WI;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t wi = warp % WI, wo = warp / WI;
+    const uint64_t TO = uint64_t(WO) * 32u * MO;
+    const uint64_t P = k.P;
+    const uint64_t outputs = k.S * P;
+    const TA* __restrict__ A = static_cast<const TA*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    constexpr int U = (loads_in_flight<TA, 1>() / MO) < 1 ? 1 : loads_in_flight<TA, 1>() / MO;
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    uint32_t phase = 0;
+    uint64_t staged_seg = ~uint64_t(0);
+    uint32_t off = 0;
+    const uint64_t first = uint64_t(blockIdx.x) * k.items_per_cta;
+    const uint64_t last = min(k.items, first + k.items_per_cta);
+
+    for (uint64_t item = first; item < last; ++item) {
+        const uint64_t seg = item / k.ntiles;
+        const uint64_t tile = item - seg * k.ntiles;
+        const uint64_t ib = seg * k.seg_len;
+        const uint64_t ie = min(k.nq, ib + k.seg_len);
+        if (seg != staged_seg) {
+            __syncthreads();   // every reader of the previous segment is done
+            if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
+            staged_seg = seg;
+            off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+        }
+        const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+
+        const uint64_t o0 = tile * TO + uint64_t(wo) * 32u * MO + lane;   // outputs o0 + 32 m
+        uint64_t ofs[MO];
+        bool ok[MO];
+        bool any = false;
+#pragma unroll
+        for (int m = 0; m < MO; ++m) {
+            const uint64_t o = o0 + 32u * m;
+            ok[m] = o < outputs;
+            any = any || ok[m];
+            const uint64_t s = ok[m] ? o / P : 0;
+            ofs[m] = s * k.nq * P + (o - s * P);
+        }
+        typename AccSel<T, KAHAN>::type acc[MO];
+#pragma unroll
+        for (int m = 0; m < MO; ++m) acc[m].init();
+        if (any) {
+            uint64_t i = ib + wi;
+            for (; i + (U - 1) * WI < ie; i += U * WI) strided_rows<U, MO>(acc, A, ofs, ok, P, bs, i, WI);
+            if constexpr (U >= 4) {
+                if (i + (U / 2 - 1) * WI < ie) {
+                    strided_rows<U / 2, MO>(acc, A, ofs, ok, P, bs, i, WI);
+                    i += (U / 2) * WI;
+                }
+            }
+            if constexpr (U >= 8) {
+                if (i + (U / 4 - 1) * WI < ie) {
+                    strided_rows<U / 4, MO>(acc, A, ofs, ok, P, bs, i, WI);
+                    i += (U / 4) * WI;
+                }
+            }
+            for (; i < ie; i += WI) strided_rows<1, MO>(acc, A, ofs, ok, P, bs, i, WI);
+        }
+#pragma unroll
+        for (int m = 0; m < MO; ++m) acc[m].fold();
+        if (WI > 1) {
+            // warps stacked along i hand their partials to warp row wi == 0
+            const uint32_t slot = wo * 32u + lane;
+            if (wi > 0) {
+                T* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * MO);
+#pragma unroll
+                for (int m = 0; m < MO; ++m) {
+                    r[2 * m] = acc[m].s;
+                    r[2 * m + 1] = acc[m].c;
+                }
+            }
+            __syncthreads();
+            if (wi == 0) {
+                for (uint32_t w = 1; w < WI; ++w) {
+                    const T* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * MO);
+#pragma unroll
+                    for (int m = 0; m < MO; ++m) acc[m].merge(r[2 * m], r[2 * m + 1]);
+                }
+            }
+            __syncthreads();
+        }
+        if (wi == 0) {
+#pragma unroll
+            for (int m = 0; m < MO; ++m) {
+                if (!ok[m]) continue;
+                const uint64_t o = o0 + 32u * m;
+                if (k.nseg == 1) {
+                    static_cast<T*>(k.out)[o] = acc[m].value();
+                } else {
+                    Pair<T> pr;
+                    pr.s = acc[m].s;
+                    pr.c = KAHAN ? acc[m].c : T(0);
+                    static_cast<Pair<T>*>(k.partial)[seg * outputs + o] = pr;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace tlibg
