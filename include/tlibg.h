@@ -116,12 +116,12 @@ int tlibg_ttv_ex(int dtype, size_t q, size_t p,
                  void* c, const size_t* nc, const size_t* wc, const size_t* pic,
                  const tlibg_options* opt, void* stream);
 
-/* Same call with HOST pointers a, b, c, as the reference takes them.  A is
- * streamed to the device in chunks on copy streams overlapped with the
- * kernels; C is copied back; the call returns when C is complete on the
- * host (the reference's synchronous semantics).  Pinned (page-locked) host
- * buffers give full copy bandwidth; pageable ones work at driver-staged
- * speed. */
+/* Same call with HOST pointers a, b, c, as the reference takes them.  A in
+ * page-locked memory is read in place by the kernels over the host link (one
+ * pass, no staging copy); pageable A is streamed to the device in chunks on a
+ * copy stream overlapped with the kernels.  b and C go through device
+ * buffers; the call returns when C is complete on the host (the reference's
+ * synchronous semantics). */
 int tlibg_ttv_host(int dtype, size_t q, size_t p,
                    const void* a, const size_t* na, const size_t* wa, const size_t* pia,
                    const void* b, const size_t* nb,

@@ -324,8 +324,10 @@ def test_host_buffers(engine, orc, torch_dev):
     """The host-pointer entry point (the reference's own calling convention)."""
     torch, dev = torch_dev
     rng = np.random.default_rng(4)
+    # pinned A is read in place by the kernels (the streamed kernel's shapes, here
+    # rows of 25, take the register row kernel instead); pageable A is staged
     for na, pia, q in (([200, 300, 50], [1, 2, 3], 2), ([128, 64, 300], [3, 1, 2], 3),
-                       ([4096, 4096], [1, 2], 2)):
+                       ([4096, 4096], [1, 2], 2), ([25, 4000], [1, 2], 1), ([7, 999, 5], [1, 2, 3], 2)):
         wa, nc, wc, pic = meta(engine, na, pia, q)
         a = rng.uniform(-1, 1, int(np.prod(na))).astype(np.float32)
         b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)

@@ -888,6 +888,40 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     if ((st = grow(&hc.bbuf, &hc.bbytes, need_b))) return st;
     if ((st = grow(&hc.cbuf, &hc.cbytes, need_c))) return st;
 
+    // Page-locked A: the kernels read it in place over the host link (one pass,
+    // no staging copy; on GB300 a kernel reading page-locked memory moves it as
+    // fast as the copy engines do).  The streamed kernel's bulk copies are kept
+    // to device memory: the register kernels take q-fastest rows instead.
+    cudaPointerAttributes at{};
+    const bool a_pinned = cudaPointerGetAttributes(&at, a) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+                          at.devicePointer != nullptr;
+    cudaGetLastError();
+    if (a_pinned) {
+        if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.comp)) != cudaSuccess)
+            return cuda_fail(e, "copy of b");
+        tlibg_options o2{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, 0};
+        if (opt) o2 = *opt;
+        if (o2.kind == KIND_STREAM) o2.kind = -1;
+        Plan pl;
+        if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &pl))) return st;
+        if (pl.kind == KIND_STREAM) {
+            o2.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
+            if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &pl))) return st;
+        }
+        void* part = nullptr;
+        if ((st = get_scratch(hc.comp, partial_bytes(pl), &part))) return st;
+        uint64_t launches = 0;
+        e = launch_plan(pl, at.devicePointer, hc.bbuf, hc.cbuf, part, hc.comp, &launches);
+        g_launches += launches;
+        if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        if ((e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
+            return cuda_fail(e, "copy of C");
+        if ((e = cudaStreamSynchronize(hc.comp)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
+        if (read_and_clear_device_error())
+            return fail(TLIBG_ERR_TIMEOUT, "tlibg: a bounded device wait expired; results are invalid");
+        return ok();
+    }
+
     if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess)
         return cuda_fail(e, "copy of b");
     Plan pl_full;
