@@ -139,7 +139,8 @@ def test_planner_kernel_family(engine):
     # q-fastest rows: aligned -> register row kernel; unaligned fp32 within a 16 KB
     # stage -> the streamed kernel (row form); fp64 rows -> row kernel
     assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
-    assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_STREAM
+    assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_ROW
+    assert engine.plan(3, [25, 25, 25], [3, 2, 1])["kind"] == engine.KIND_STREAM
     assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
     assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
     # fp64 column kernel: the DFMA / double-float mix by default
@@ -152,14 +153,12 @@ def test_planner_kernel_family(engine):
     # long rows: the register kernels (q fastest -> row kernel, else column kernel)
     assert engine.plan(1, [16384, 16384], [1, 2])["kind"] == engine.KIND_ROW
     assert engine.plan(2, [16384, 16384], [1, 2])["kind"] == engine.KIND_COL
-    # fp32 rows of the prefix not 16-byte aligned: shuffle-realigned loads from 4 KB rows;
-    # fp64 keeps scalar 8-byte loads
-    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL_REALIGN
-    assert engine.plan(3, [25, 25, 25, 25], [1, 2, 3, 4])["kind"] == engine.KIND_COL
-    assert engine.plan(4, [25, 25, 25, 25], [1, 2, 3, 4])["kind"] == engine.KIND_COL_REALIGN
-    assert engine.plan(2, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL
+    # prefix rows not 16-byte aligned: scalar loads (two outputs per thread); the
+    # realigning kernel on request
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["kind"] == engine.KIND_COL
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["vec"] == 1
     assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_COL
-    assert engine.plan(3, [645, 645, 645], [1, 2, 3])["vec"] == 4
+    assert engine.plan(3, [645, 645, 645], [1, 2, 3], kind=engine.KIND_COL_REALIGN)["vec"] == 4
     assert engine.plan(2, [25, 25, 25], [1, 2, 3])["kind"] == engine.KIND_COL
     assert engine.plan(3, [645, 645, 645], [1, 2, 3], dtype=engine.BF16A)["kind"] == engine.KIND_COL
     assert engine.plan(2, [25, 25, 25], [1, 2, 3], kind=engine.KIND_COL_REALIGN)["kind"] == \

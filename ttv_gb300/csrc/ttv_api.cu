@@ -419,16 +419,17 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         opt->kind != KIND_COL_THIN && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
-    // default for q-fastest rows: the register row kernel when rows allow 16-byte loads;
-    // the streamed kernel (alignment-agnostic) for unaligned fp32 / bf16 rows that fit
-    // a stage; fp64 rows always take the register row kernel (measured faster).
+    // default for q-fastest rows: the register row kernel, except unaligned fp32 / bf16
+    // rows shorter than 64 elements, which the streamed kernel (alignment-agnostic)
+    // takes (measured on GB300: rows of 25 floats 4.3 vs 3.8 TB/s; rows of 645 floats
+    // 4.2 vs 5.8 TB/s the other way round).
     // The streamed column form stays available on request.
     bool rows_aligned = false;
     {
         const size_t vb = 16 / ea;
         rows_aligned = cn.nq % vb == 0 && aligned(a, 16) && aligned(b, 16);
     }
-    const bool stream_default = eligible && cn.P == 1 && !rows_aligned && dtype != F64;
+    const bool stream_default = eligible && cn.P == 1 && !rows_aligned && dtype != F64 && cn.nq < 64;
     if ((opt && opt->kind == KIND_STREAM) || (stream_default && !(opt && opt->kind >= 0))) {
         if (dtype == F64) pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
         return make_stream_plan(pl, cn, opt, sms, out);
@@ -453,10 +454,10 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         if (!vec_ok(V)) return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced vector width violates alignment");
     } else {
         while (V > 1 && !vec_ok(V)) V /= 2;
-        // fp32 rows that are not 16-byte aligned and long enough that windows of 32
-        // vectors rarely straddle two rows: realigned 16-byte loads (measured on GB300:
-        // ahead of scalar loads from 4 KB rows on; for fp64 scalar 8-byte loads stay ahead)
-        const bool realign_default = dtype == F32 && cn.P >= 1024;
+        // The realigning kernel (16-byte loads realigned by shuffles) stays available on
+        // request: since scalar loads carry two outputs per thread (the strided kernel)
+        // they measure ahead of it for every unaligned prefix of the sweeps.
+        const bool realign_default = false;
         if (V < vmax && realign_ok && !(opt && opt->kind >= 0) && realign_default) {
             V = vmax;
             pl.kind = KIND_COL_REALIGN;
@@ -467,13 +468,15 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     const int force_split = opt ? opt->split : 0;
     const int force_group = opt ? opt->group : 0;
     if (pl.kind == KIND_ROW) {
-        // Lanes per row, measured on GB300: fp32 about 16 vector loads per lane (at least
-        // 2 lanes); fp64 about 64 elements per lane (at least 2 lanes), one lane for rows
-        // of at most 32 elements.
+        // Lanes per row, measured on GB300: fp32 about 16 vector loads per lane (64
+        // elements with scalar loads; at least 2 lanes); fp64 about 64 elements per lane
+        // (at least 2 lanes), one lane for rows of at most 32 elements.
         const uint64_t nvec = cdiv(cn.nq, V);
         int Gdef;
         if (dtype == F64)
             Gdef = cn.nq <= 32 ? 1 : std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 64))));
+        else if (V == 1)   // scalar loads: about 64 elements per lane
+            Gdef = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 64))));
         else
             Gdef = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, nvec / 16))));
         int G = force_group > 0 ? force_group : Gdef;
