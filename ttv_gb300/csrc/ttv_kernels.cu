@@ -93,6 +93,16 @@ __device__ __forceinline__ void load_b(const T* p, T (&out)[V])
 // DFMA (even outputs, or even unrolled rows when V == 1) and half the FP32 /
 // INT32 emulation, so neither the FP64 pipe nor the issue slots alone bound
 // the kernel; the shared bb is split once.
+// One product in TLIBG_F64_NATIVE_EVERY (counted over the unrolled loads and
+// vector slots) takes the DFMA pipe, the others the double-float emulation.
+#ifndef TLIBG_F64_NATIVE_EVERY
+#define TLIBG_F64_NATIVE_EVERY 2
+#endif
+template <int V> __device__ __forceinline__ constexpr bool f64_native(int u, int v)
+{
+    return ((u * V + v) % TLIBG_F64_NATIVE_EVERY) == 0;
+}
+
 template <int V, typename AccT, typename T>
 __device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, int u = 0)
 {
@@ -100,7 +110,7 @@ __device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, 
         const DSplit bs = split_double(bb);
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-            const bool native = V > 1 ? ((v & 1) == 0) : ((u & 1) == 0);
+            const bool native = f64_native<V>(u, v);
             if (native)
                 acc[v].d = fma(av[v], bb, acc[v].d);
             else
@@ -121,7 +131,7 @@ __device__ __forceinline__ void vec_fma(AccT (&acc)[V], const T (&av)[V], const 
     if constexpr (std::is_same<AccT, AccDF>::value) {
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-            const bool native = V > 1 ? ((v & 1) == 0) : ((u & 1) == 0);
+            const bool native = f64_native<V>(u, v);
             if (native)
                 acc[v].d = fma(av[v], bv[v], acc[v].d);
             else
