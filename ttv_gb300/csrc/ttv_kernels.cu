@@ -93,19 +93,14 @@ __device__ __forceinline__ void load_b(const T* p, T (&out)[V])
 // DFMA (even outputs, or even unrolled rows when V == 1) and half the FP32 /
 // INT32 emulation, so neither the FP64 pipe nor the issue slots alone bound
 // the kernel; the shared bb is split once.
-// Which products (counted over the unrolled loads and vector slots) take the
-// DFMA pipe: one in TLIBG_F64_NATIVE_EVERY, or, when TLIBG_F64_EMULATE_EVERY
-// is set, all but one in that many; the rest take the double-float emulation.
+// One product in TLIBG_F64_NATIVE_EVERY (counted over the unrolled loads and
+// vector slots) takes the DFMA pipe, the others the double-float emulation.
 #ifndef TLIBG_F64_NATIVE_EVERY
 #define TLIBG_F64_NATIVE_EVERY 2
 #endif
-#ifndef TLIBG_F64_EMULATE_EVERY
-#define TLIBG_F64_EMULATE_EVERY 0
-#endif
 template <int V> __device__ __forceinline__ constexpr bool f64_native(int u, int v)
 {
-    return TLIBG_F64_EMULATE_EVERY > 0 ? ((u * V + v) % (TLIBG_F64_EMULATE_EVERY > 0 ? TLIBG_F64_EMULATE_EVERY : 1)) != 0
-                                       : ((u * V + v) % TLIBG_F64_NATIVE_EVERY) == 0;
+    return ((u * V + v) % TLIBG_F64_NATIVE_EVERY) == 0;
 }
 
 template <int V, typename AccT, typename T>
