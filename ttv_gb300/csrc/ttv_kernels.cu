@@ -95,6 +95,8 @@ __device__ __forceinline__ void load_b(const T* p, T (&out)[V])
 // the kernel; the shared bb is split once.
 // One product in TLIBG_F64_NATIVE_EVERY (counted over the unrolled loads and
 // vector slots) takes the DFMA pipe, the others the double-float emulation.
+// Measured on GB300 over the symmetric sweep's fp64 half: one in two is best
+// (one in three or four, or all but one in three or four, lose 3-14 %).
 #ifndef TLIBG_F64_NATIVE_EVERY
 #define TLIBG_F64_NATIVE_EVERY 2
 #endif
