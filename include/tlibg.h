@@ -243,6 +243,10 @@ int tlibg_batch_costs(tlibg_batch* batch, uint64_t* cycles, void* stream);
 /* The variant each problem ran with in the last launch (synchronises). */
 int tlibg_batch_variants(tlibg_batch* batch, int* out, void* stream);
 int tlibg_batch_destroy(tlibg_batch* batch);
+/* fp32 batch in one call with the learned selection (the installed cost
+ * model, else the fixed rule); synchronous.  Same as tlibg_ttv_batch with
+ * TLIBG_F32 and TLIBG_SELECT_LEARNED. */
+int tlibg_ttv_batch_f32(const tlibg_problem* probs, int n, void* stream);
 /* create + launch + destroy (synchronous). */
 int tlibg_ttv_batch(int dtype, const tlibg_problem* probs, size_t count,
                     const tlibg_batch_options* opt, void* stream);

@@ -149,6 +149,9 @@ def test_one_shot_and_errors(engine, orc, cuda):
     B.ttv_batch(probs)
     torch.cuda.synchronize()
     check_all(orc, probs, host)
+    reset(probs)
+    B.ttv_batch_f32(probs)   # learned selection through the short entry point
+    check_all(orc, probs, host)
     bad = B.Problem(2, [4, 5, 6], [1, 2, 3], probs[0].a, probs[0].b, probs[0].c)
     bad._keep[3][0] = 7   # nb != na[q-1]
     with pytest.raises(engine.TTVError, match="contraction dimension of A and B are not equal"):

@@ -59,6 +59,7 @@ def _lib():
         L.tlibg_batch_destroy.argtypes = [_vp]
         L.tlibg_ttv_batch.argtypes = [C.c_int, P, C.c_size_t, C.POINTER(_BatchOptions), _vp]
         L.tlibg_ttv_percall.argtypes = [C.c_int, P, C.c_size_t, _vp]
+        L.tlibg_ttv_batch_f32.argtypes = [P, C.c_int, _vp]
         L.tlibg_batch_features.argtypes = [P, C.c_size_t, C.POINTER(C.c_float),
                                            C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.tlibg_batch_device_error.restype = C.c_uint
@@ -171,6 +172,13 @@ def ttv_batch(problems, select=SELECT_HEURISTIC, variant=0, variants=None, strea
     arr = _array(problems)
     o, keep = _opts(select, variant, 0, True, variants)
     _raise(_lib().tlibg_ttv_batch(0, arr, len(problems), C.byref(o), _stream(stream)))
+
+
+def ttv_batch_f32(problems, stream=None):
+    """tlibg_ttv_batch_f32: one synchronous call, learned selection (fixed rule
+    when no cost model is installed)."""
+    arr = _array(problems)
+    _raise(_lib().tlibg_ttv_batch_f32(arr, len(problems), _stream(stream)))
 
 
 def ttv_percall(problems, stream=None):

@@ -899,6 +899,14 @@ int tlibg_ttv_batch(int dtype, const tlibg_problem* probs, size_t count, const t
     return s;
 }
 
+int tlibg_ttv_batch_f32(const tlibg_problem* probs, int n, void* stream)
+{
+    if (n < 0) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_ttv_batch_f32: negative problem count");
+    tlibg_batch_options o{};
+    o.select = TLIBG_SELECT_LEARNED;   // the installed cost model, else the fixed rule
+    return tlibg_ttv_batch(TLIBG_F32, probs, (size_t)n, &o, stream);
+}
+
 int tlibg_ttv_percall(int dtype, const tlibg_problem* probs, size_t count, void* stream)
 {
     if (!probs && count) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_ttv_percall: null problems");
