@@ -105,11 +105,21 @@ template <int V> __device__ __forceinline__ constexpr bool f64_native(int u, int
     return ((u * V + v) % TLIBG_F64_NATIVE_EVERY) == 0;
 }
 
-template <int V, typename AccT, typename T>
-__device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, int u = 0)
+// bsp (PRE): b's double-float split, computed once per staged segment.
+template <int V, bool PRE = false, typename AccT, typename T>
+__device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, int u = 0,
+                                        const float2* bsp = nullptr)
 {
     if constexpr (std::is_same<AccT, AccDF>::value) {
-        const DSplit bs = split_double(bb);
+        DSplit bs;
+        if constexpr (PRE) {
+            const float2 t = *bsp;
+            bs.hi = t.x;
+            bs.lo = t.y;
+            bs.ok = true;
+        } else {
+            bs = split_double(bb);
+        }
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             const bool native = f64_native<V>(u, v);
@@ -154,16 +164,62 @@ template <int V, typename AccT> __device__ __forceinline__ void renorm_all(AccT 
 // UB rows of the contracted mode for one thread: all loads first, then the
 // products (column form: b[i] shared by the V outputs; u alternates the fp64
 // mix when V == 1).
-template <int UB, int V, typename TA, typename T, typename AccT>
+template <int UB, int V, bool PRE = false, typename TA, typename T, typename AccT>
 __device__ __forceinline__ void col_rows(AccT (&acc)[V], const TA* ap, uint64_t P, const T* bs, uint64_t i,
-                                         uint32_t WI)
+                                         uint32_t WI, const float2* bsp = nullptr)
 {
     T av[UB][V];
 #pragma unroll
     for (int u = 0; u < UB; ++u) load_a<TA, T, V>(ap + (i + u * WI) * P, av[u]);
 #pragma unroll
-    for (int u = 0; u < UB; ++u) row_fma<V>(acc, av[u], bs[i + u * WI], u);
+    for (int u = 0; u < UB; ++u) row_fma<V, PRE>(acc, av[u], bs[i + u * WI], u, PRE ? bsp + i + u * WI : nullptr);
     renorm_all<V>(acc);
+}
+
+// Rows [i0, ie) step WI of one thread: blocks of U rows, then one of U/2 and
+// one of U/4 at most, then single rows, so short contractions still get
+// their loads in flight together.
+template <int U, int V, bool PRE, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void col_loop(AccT (&acc)[V], const TA* ap, uint64_t P, const T* bs, const float2* bsp,
+                                         uint64_t i, uint64_t ie, uint32_t WI)
+{
+    for (; i + (U - 1) * (uint64_t)WI < ie; i += U * (uint64_t)WI) col_rows<U, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+    if constexpr (U >= 4) {
+        if (i + (U / 2 - 1) * (uint64_t)WI < ie) {
+            col_rows<U / 2, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+            i += (U / 2) * (uint64_t)WI;
+        }
+    }
+    if constexpr (U >= 8) {
+        if (i + (U / 4 - 1) * (uint64_t)WI < ie) {
+            col_rows<U / 4, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+            i += (U / 4) * (uint64_t)WI;
+        }
+    }
+    for (; i < ie; i += WI) col_rows<1, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+}
+
+// fp64 with the double-float mix: b's split is computed once per staged
+// segment (shared by every tile of the CTA) instead of once per row and thread.
+template <typename T, bool KAHAN> __host__ __device__ constexpr bool presplit_b()
+{
+    return std::is_same<T, double>::value && KAHAN;
+}
+
+// Split the staged segment b[0..n) into bsp; true (CTA-uniform) when every
+// element is inside the emulation's exponent window.
+template <typename T>
+__device__ __forceinline__ bool stage_b_split(const T* b, uint32_t n, float2* bsp)
+{
+    int ok = 1;
+    if constexpr (std::is_same<T, double>::value) {
+        for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+            const DSplit d = split_double(b[e]);
+            bsp[e] = make_float2(d.hi, d.lo);
+            ok &= d.ok ? 1 : 0;
+        }
+    }
+    return __syncthreads_and(ok) != 0;
 }
 
 // Same for UB vectors of a row (row form: b varies with the element).
@@ -348,7 +404,9 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);
     constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
-    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));
+    constexpr bool PRES = presplit_b<T, KAHAN>();
+    float2* bsplit = reinterpret_cast<float2*>(smem_raw + 16 + BCAP * sizeof(T));
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T) + (PRES ? BCAP * sizeof(float2) : 0));
 
     const uint32_t WI = k.group;
     const uint32_t WO = (BLOCK / 32) / WI;
@@ -359,6 +417,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
     constexpr int U = loads_in_flight<TA, V>();
+    bool b_split_ok = false;
 
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -383,8 +442,10 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
             if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
             staged_seg = seg;
             off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+            if constexpr (PRES) b_split_ok = stage_b_split<T>(sb + off, (uint32_t)(ie - ib), bsplit);
         }
         const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+        const float2* bsp = bsplit - ib;
 
         const uint64_t o0 = tile * TO + (uint64_t(wo) * 32u + lane) * V;
         const bool valid = o0 < outputs;
@@ -395,23 +456,10 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
             const uint64_t s = o0 / k.P;
             const uint64_t j = o0 - s * k.P;
             const TA* ap = A + (s * k.nq) * k.P + j;
-            uint64_t i = ib + wi;
-            // blocks of U rows, then one of U/2 and one of U/4 at most, then
-            // single rows: short contractions still get their loads in flight together
-            for (; i + (U - 1) * WI < ie; i += U * WI) col_rows<U, V>(acc, ap, k.P, bs, i, WI);
-            if constexpr (U >= 4) {
-                if (i + (U / 2 - 1) * WI < ie) {
-                    col_rows<U / 2, V>(acc, ap, k.P, bs, i, WI);
-                    i += (U / 2) * WI;
-                }
-            }
-            if constexpr (U >= 8) {
-                if (i + (U / 4 - 1) * WI < ie) {
-                    col_rows<U / 4, V>(acc, ap, k.P, bs, i, WI);
-                    i += (U / 4) * WI;
-                }
-            }
-            for (; i < ie; i += WI) col_rows<1, V>(acc, ap, k.P, bs, i, WI);
+            if (PRES && b_split_ok)
+                col_loop<U, V, PRES>(acc, ap, k.P, bs, bsp, ib + wi, ie, WI);
+            else
+                col_loop<U, V, false>(acc, ap, k.P, bs, bsp, ib + wi, ie, WI);
         }
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fold();
@@ -647,10 +695,12 @@ size_t plan_smem_bytes(const Plan& p)
     if (p.kind == KIND_ROW) return 0;
     const size_t es = acc_size(p.dtype);
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
-    if (p.kind == KIND_COL_THIN) return 16 + bcap * es + (size_t)(BLOCK / 32) * 32 * 2 * p.vec * es;
+    // fp64 with the double-float mix: b's split beside the staged b (column, strided, thin)
+    const size_t split = (p.dtype == F64 && p.kahan && p.kind != KIND_COL_REALIGN) ? bcap * 8 : 0;
+    if (p.kind == KIND_COL_THIN) return 16 + bcap * es + split + (size_t)(BLOCK / 32) * 32 * 2 * p.vec * es;
     const size_t WO = (BLOCK / 32) / p.group;
     const size_t red = p.group > 1 ? (size_t)(p.group - 1) * WO * 32 * 2 * p.vec * p.mo * es : 0;
-    return 16 + bcap * es + red;
+    return 16 + bcap * es + split + red;
 }
 
 size_t partial_bytes(const Plan& p)

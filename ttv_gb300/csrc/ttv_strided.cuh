@@ -13,9 +13,10 @@
 
 namespace tlibg {
 
-template <int UB, int MO, typename TA, typename T, typename AccT>
+template <int UB, int MO, bool PRE, typename TA, typename T, typename AccT>
 __device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* A, const uint64_t (&ofs)[MO],
-                                             const bool (&ok)[MO], uint64_t P, const T* bs, uint64_t i, uint32_t WI)
+                                             const bool (&ok)[MO], uint64_t P, const T* bs, const float2* bsp,
+                                             uint64_t i, uint32_t WI)
 {
     T av[UB][MO];
 #pragma unroll
@@ -31,8 +32,30 @@ __device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* A, const
             }
         }
 #pragma unroll
-    for (int u = 0; u < UB; ++u) row_fma<MO>(acc, av[u], bs[i + u * WI], u);
+    for (int u = 0; u < UB; ++u) row_fma<MO, PRE>(acc, av[u], bs[i + u * WI], u, PRE ? bsp + i + u * WI : nullptr);
     renorm_all<MO>(acc);
+}
+
+template <int U, int MO, bool PRE, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void strided_loop(AccT (&acc)[MO], const TA* A, const uint64_t (&ofs)[MO],
+                                             const bool (&ok)[MO], uint64_t P, const T* bs, const float2* bsp,
+                                             uint64_t i, uint64_t ie, uint32_t WI)
+{
+    for (; i + (U - 1) * (uint64_t)WI < ie; i += U * (uint64_t)WI)
+        strided_rows<U, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+    if constexpr (U >= 4) {
+        if (i + (U / 2 - 1) * (uint64_t)WI < ie) {
+            strided_rows<U / 2, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+            i += (U / 2) * (uint64_t)WI;
+        }
+    }
+    if constexpr (U >= 8) {
+        if (i + (U / 4 - 1) * (uint64_t)WI < ie) {
+            strided_rows<U / 4, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+            i += (U / 4) * (uint64_t)WI;
+        }
+    }
+    for (; i < ie; i += WI) strided_rows<1, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
 }
 
 template <typename TA, typename T, int MO, bool KAHAN>
@@ -43,7 +66,10 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);
     constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
-    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));
+    constexpr bool PRES = presplit_b<T, KAHAN>();
+    float2* bsplit = reinterpret_cast<float2*>(smem_raw + 16 + BCAP * sizeof(T));
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T) + (PRES ? BCAP * sizeof(float2) : 0));
+    bool b_split_ok = false;
 
     const uint32_t WI = k.group;
     const uint32_t WO = (BLOCK / 32) / WI;
@@ -79,8 +105,10 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
             if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
             staged_seg = seg;
             off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+            if constexpr (PRES) b_split_ok = stage_b_split<T>(sb + off, (uint32_t)(ie - ib), bsplit);
         }
         const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+        const float2* bsp = bsplit - ib;
 
         const uint64_t o0 = tile * TO + uint64_t(wo) * 32u * MO + lane;   // outputs o0 + 32 m
         uint64_t ofs[MO];
@@ -98,21 +126,10 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
 #pragma unroll
         for (int m = 0; m < MO; ++m) acc[m].init();
         if (any) {
-            uint64_t i = ib + wi;
-            for (; i + (U - 1) * WI < ie; i += U * WI) strided_rows<U, MO>(acc, A, ofs, ok, P, bs, i, WI);
-            if constexpr (U >= 4) {
-                if (i + (U / 2 - 1) * WI < ie) {
-                    strided_rows<U / 2, MO>(acc, A, ofs, ok, P, bs, i, WI);
-                    i += (U / 2) * WI;
-                }
-            }
-            if constexpr (U >= 8) {
-                if (i + (U / 4 - 1) * WI < ie) {
-                    strided_rows<U / 4, MO>(acc, A, ofs, ok, P, bs, i, WI);
-                    i += (U / 4) * WI;
-                }
-            }
-            for (; i < ie; i += WI) strided_rows<1, MO>(acc, A, ofs, ok, P, bs, i, WI);
+            if (PRES && b_split_ok)
+                strided_loop<U, MO, PRES>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+            else
+                strided_loop<U, MO, false>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
         }
 #pragma unroll
         for (int m = 0; m < MO; ++m) acc[m].fold();

@@ -23,7 +23,11 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KA
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);
     constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
-    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));   // [NW][32][V][2]
+    constexpr bool PRES = presplit_b<T, KAHAN>();
+    float2* bsplit = reinterpret_cast<float2*>(smem_raw + 16 + BCAP * sizeof(T));
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T) +
+                                  (PRES ? BCAP * sizeof(float2) : 0));   // [NW][32][V][2]
+    bool b_split_ok = false;
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint64_t P = k.P;
@@ -58,28 +62,19 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KA
             if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
             staged_seg = seg;
             off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+            if constexpr (PRES) b_split_ok = stage_b_split<T>(sb + off, (uint32_t)(ie - ib), bsplit);
         }
         const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+        const float2* bsp = bsplit - ib;
 
         typename AccSel<T, KAHAN>::type acc[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].init();
         const TA* ap = A + s * k.nq * P + j0;
-        uint64_t i = ib + warp * RG + g;
-        for (; i + (U - 1) * (uint64_t)step < ie; i += U * (uint64_t)step) col_rows<U, V>(acc, ap, P, bs, i, step);
-        if constexpr (U >= 4) {
-            if (i + (U / 2 - 1) * (uint64_t)step < ie) {
-                col_rows<U / 2, V>(acc, ap, P, bs, i, step);
-                i += (U / 2) * (uint64_t)step;
-            }
-        }
-        if constexpr (U >= 8) {
-            if (i + (U / 4 - 1) * (uint64_t)step < ie) {
-                col_rows<U / 4, V>(acc, ap, P, bs, i, step);
-                i += (U / 4) * (uint64_t)step;
-            }
-        }
-        for (; i < ie; i += step) col_rows<1, V>(acc, ap, P, bs, i, step);
+        if (PRES && b_split_ok)
+            col_loop<U, V, PRES>(acc, ap, P, bs, bsp, ib + warp * RG + g, ie, step);
+        else
+            col_loop<U, V, false>(acc, ap, P, bs, bsp, ib + warp * RG + g, ie, step);
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fold();
         // lanes of the same outputs (row groups g) in the warp, then the warps
