@@ -456,10 +456,14 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
             const uint64_t s = o0 / k.P;
             const uint64_t j = o0 - s * k.P;
             const TA* ap = A + (s * k.nq) * k.P + j;
-            if (PRES && b_split_ok)
-                col_loop<U, V, PRES>(acc, ap, k.P, bs, bsp, ib + wi, ie, WI);
-            else
+            if constexpr (PRES) {
+                if (b_split_ok)
+                    col_loop<U, V, true>(acc, ap, k.P, bs, bsp, ib + wi, ie, WI);
+                else
+                    col_loop<U, V, false>(acc, ap, k.P, bs, bsp, ib + wi, ie, WI);
+            } else {
                 col_loop<U, V, false>(acc, ap, k.P, bs, bsp, ib + wi, ie, WI);
+            }
         }
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fold();

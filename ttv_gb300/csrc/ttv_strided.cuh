@@ -126,10 +126,14 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
 #pragma unroll
         for (int m = 0; m < MO; ++m) acc[m].init();
         if (any) {
-            if (PRES && b_split_ok)
-                strided_loop<U, MO, PRES>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
-            else
+            if constexpr (PRES) {
+                if (b_split_ok)
+                    strided_loop<U, MO, true>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+                else
+                    strided_loop<U, MO, false>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+            } else {
                 strided_loop<U, MO, false>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+            }
         }
 #pragma unroll
         for (int m = 0; m < MO; ++m) acc[m].fold();

@@ -71,10 +71,14 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KA
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].init();
         const TA* ap = A + s * k.nq * P + j0;
-        if (PRES && b_split_ok)
-            col_loop<U, V, PRES>(acc, ap, P, bs, bsp, ib + warp * RG + g, ie, step);
-        else
+        if constexpr (PRES) {
+            if (b_split_ok)
+                col_loop<U, V, true>(acc, ap, P, bs, bsp, ib + warp * RG + g, ie, step);
+            else
+                col_loop<U, V, false>(acc, ap, P, bs, bsp, ib + warp * RG + g, ie, step);
+        } else {
             col_loop<U, V, false>(acc, ap, P, bs, bsp, ib + warp * RG + g, ie, step);
+        }
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].fold();
         // lanes of the same outputs (row groups g) in the warp, then the warps
