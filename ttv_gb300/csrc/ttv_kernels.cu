@@ -137,17 +137,26 @@ __device__ __forceinline__ void row_fma(AccT (&acc)[V], const T (&av)[V], T bb, 
 // acc[v] += av[v] * bv[v] (row form: b varies with the element).  The fp64
 // double-float accumulator mixes the same way: even vector slots (or even
 // unrolled loads when V == 1) on the DFMA pipe, odd ones emulated.
-template <int V, typename AccT, typename T>
-__device__ __forceinline__ void vec_fma(AccT (&acc)[V], const T (&av)[V], const T (&bv)[V], int u = 0)
+template <int V, bool PRE = false, typename AccT, typename T>
+__device__ __forceinline__ void vec_fma(AccT (&acc)[V], const T (&av)[V], const T (&bv)[V], int u = 0,
+                                        const float2* bsp = nullptr)
 {
     if constexpr (std::is_same<AccT, AccDF>::value) {
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             const bool native = f64_native<V>(u, v);
-            if (native)
+            if (native) {
                 acc[v].d = fma(av[v], bv[v], acc[v].d);
-            else
+            } else if constexpr (PRE) {
+                const float2 t = bsp[v];
+                DSplit bs;
+                bs.hi = t.x;
+                bs.lo = t.y;
+                bs.ok = true;
+                acc[v].add_split(split_double(av[v]), bs, av[v], bv[v]);
+            } else {
                 acc[v].add_split(split_double(av[v]), split_double(bv[v]), av[v], bv[v]);
+            }
         }
     } else {
 #pragma unroll
@@ -223,8 +232,9 @@ __device__ __forceinline__ bool stage_b_split(const T* b, uint32_t n, float2* bs
 }
 
 // Same for UB vectors of a row (row form: b varies with the element).
-template <int UB, int V, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void row_vecs(AccT (&acc)[V], const TA* ap, const T* bp, uint64_t kv, uint32_t G)
+template <int UB, int V, bool PRE = false, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void row_vecs(AccT (&acc)[V], const TA* ap, const T* bp, uint64_t kv, uint32_t G,
+                                         const float2* bsp = nullptr)
 {
     T av[UB][V], bv[UB][V];
 #pragma unroll
@@ -236,9 +246,36 @@ __device__ __forceinline__ void row_vecs(AccT (&acc)[V], const TA* ap, const T* 
         load_b<T, V>(bp + (kv + u * G) * V, bv[u]);
     }
 #pragma unroll
-    for (int u = 0; u < UB; ++u) vec_fma<V>(acc, av[u], bv[u], u);
+    for (int u = 0; u < UB; ++u) vec_fma<V, PRE>(acc, av[u], bv[u], u, PRE ? bsp + (kv + u * G) * V : nullptr);
     renorm_all<V>(acc);
 }
+
+// One row segment [0, nv) vectors of a lane (kv = gl, gl + G, ...).
+template <int U, int V, bool PRE, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void row_loop(AccT (&acc)[V], const TA* ap, const T* bp, const float2* bsp, uint64_t kv,
+                                         uint64_t nv, uint32_t G)
+{
+    // blocks of U vectors, then one of U/2 and one of U/4 at most, then
+    // single vectors: short rows still get their loads in flight together
+    for (; kv + (U - 1) * G < nv; kv += U * G) row_vecs<U, V, PRE>(acc, ap, bp, kv, G, bsp);
+    if constexpr (U >= 4) {
+        if (kv + (U / 2 - 1) * G < nv) {
+            row_vecs<U / 2, V, PRE>(acc, ap, bp, kv, G, bsp);
+            kv += (U / 2) * G;
+        }
+    }
+    if constexpr (U >= 8) {
+        if (kv + (U / 4 - 1) * G < nv) {
+            row_vecs<U / 4, V, PRE>(acc, ap, bp, kv, G, bsp);
+            kv += (U / 4) * G;
+        }
+    }
+    for (; kv < nv; kv += G) row_vecs<1, V, PRE>(acc, ap, bp, kv, G, bsp);
+}
+
+// fp64 rows with the double-float mix: b (up to this many elements) is split
+// once per CTA into shared memory.
+constexpr int ROW_SPLIT_MAX = 2048;
 
 // --------------------------------------------------------------------------
 // row kernel: P == 1
@@ -318,6 +355,14 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
     constexpr int U = loads_in_flight<TA, V>();
+    constexpr bool PRES = presplit_b<T, KAHAN>();
+    extern __shared__ __align__(16) unsigned char row_smem[];
+    float2* bsplit = reinterpret_cast<float2*>(row_smem);
+    bool b_split_ok = false;
+    if constexpr (PRES) {
+        // the planner gives this kernel ROW_SPLIT_MAX float2 of shared memory
+        if (k.nq <= (uint64_t)ROW_SPLIT_MAX) b_split_ok = stage_b_split<T>(B, (uint32_t)k.nq, bsplit);
+    }
 
     for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
         const uint64_t item = wbase + lane / G;
@@ -339,23 +384,14 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
             const T* bp = B + ib;
             const uint64_t n = ie - ib;
             const uint64_t nv = n / V;
-            uint64_t kv = gl;
-            // blocks of U vectors, then one of U/2 and one of U/4 at most, then
-            // single vectors: short rows still get their loads in flight together
-            for (; kv + (U - 1) * G < nv; kv += U * G) row_vecs<U, V>(acc, ap, bp, kv, G);
-            if constexpr (U >= 4) {
-                if (kv + (U / 2 - 1) * G < nv) {
-                    row_vecs<U / 2, V>(acc, ap, bp, kv, G);
-                    kv += (U / 2) * G;
-                }
+            if constexpr (PRES) {
+                if (b_split_ok)
+                    row_loop<U, V, true>(acc, ap, bp, bsplit + ib, gl, nv, G);
+                else
+                    row_loop<U, V, false>(acc, ap, bp, bsplit, gl, nv, G);
+            } else {
+                row_loop<U, V, false>(acc, ap, bp, bsplit, gl, nv, G);
             }
-            if constexpr (U >= 8) {
-                if (kv + (U / 4 - 1) * G < nv) {
-                    row_vecs<U / 4, V>(acc, ap, bp, kv, G);
-                    kv += (U / 4) * G;
-                }
-            }
-            for (; kv < nv; kv += G) row_vecs<1, V>(acc, ap, bp, kv, G);
             for (uint64_t e = nv * V + gl; e < n; e += G) {
                 T av[1];
                 load_a<TA, T, 1>(ap + e, av);
@@ -696,7 +732,8 @@ size_t plan_smem_bytes(const Plan& p)
         if (!p.stream_col) extra = std::max(extra, (size_t)p.L * es);
         return 128 + (size_t)STREAM_NS * STREAM_SLOT + extra;
     }
-    if (p.kind == KIND_ROW) return 0;
+    if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements
+        return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.nq <= (uint64_t)ROW_SPLIT_MAX) ? ROW_SPLIT_MAX * 8 : 0;
     const size_t es = acc_size(p.dtype);
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
     // fp64 with the double-float mix: b's split beside the staged b (column, strided, thin)

@@ -41,18 +41,17 @@ __device__ __forceinline__ void strided_loop(AccT (&acc)[MO], const TA* A, const
                                              const bool (&ok)[MO], uint64_t P, const T* bs, const float2* bsp,
                                              uint64_t i, uint64_t ie, uint32_t WI)
 {
-    for (; i + (U - 1) * (uint64_t)WI < ie; i += U * (uint64_t)WI)
-        strided_rows<U, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+    for (; i + (U - 1) * WI < ie; i += U * WI) strided_rows<U, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
     if constexpr (U >= 4) {
-        if (i + (U / 2 - 1) * (uint64_t)WI < ie) {
+        if (i + (U / 2 - 1) * WI < ie) {
             strided_rows<U / 2, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
-            i += (U / 2) * (uint64_t)WI;
+            i += (U / 2) * WI;
         }
     }
     if constexpr (U >= 8) {
-        if (i + (U / 4 - 1) * (uint64_t)WI < ie) {
+        if (i + (U / 4 - 1) * WI < ie) {
             strided_rows<U / 4, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
-            i += (U / 4) * (uint64_t)WI;
+            i += (U / 4) * WI;
         }
     }
     for (; i < ie; i += WI) strided_rows<1, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
