@@ -192,17 +192,17 @@ template <int U, int V, bool PRE, typename TA, typename T, typename AccT>
 __device__ __forceinline__ void col_loop(AccT (&acc)[V], const TA* ap, uint64_t P, const T* bs, const float2* bsp,
                                          uint64_t i, uint64_t ie, uint32_t WI)
 {
-    for (; i + (U - 1) * (uint64_t)WI < ie; i += U * (uint64_t)WI) col_rows<U, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+    for (; i + (U - 1) * WI < ie; i += U * WI) col_rows<U, V, PRE>(acc, ap, P, bs, i, WI, bsp);
     if constexpr (U >= 4) {
-        if (i + (U / 2 - 1) * (uint64_t)WI < ie) {
+        if (i + (U / 2 - 1) * WI < ie) {
             col_rows<U / 2, V, PRE>(acc, ap, P, bs, i, WI, bsp);
-            i += (U / 2) * (uint64_t)WI;
+            i += (U / 2) * WI;
         }
     }
     if constexpr (U >= 8) {
-        if (i + (U / 4 - 1) * (uint64_t)WI < ie) {
+        if (i + (U / 4 - 1) * WI < ie) {
             col_rows<U / 4, V, PRE>(acc, ap, P, bs, i, WI, bsp);
-            i += (U / 4) * (uint64_t)WI;
+            i += (U / 4) * WI;
         }
     }
     for (; i < ie; i += WI) col_rows<1, V, PRE>(acc, ap, P, bs, i, WI, bsp);
@@ -360,8 +360,9 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
     float2* bsplit = reinterpret_cast<float2*>(row_smem);
     bool b_split_ok = false;
     if constexpr (PRES) {
-        // the planner gives this kernel ROW_SPLIT_MAX float2 of shared memory
-        if (k.nq <= (uint64_t)ROW_SPLIT_MAX) b_split_ok = stage_b_split<T>(B, (uint32_t)k.nq, bsplit);
+        // the planner gives this kernel ROW_SPLIT_MAX float2 of shared memory (not
+        // with one lane per row: those rows live off L1, which shared memory shrinks)
+        if (k.nq <= (uint64_t)ROW_SPLIT_MAX && G > 1) b_split_ok = stage_b_split<T>(B, (uint32_t)k.nq, bsplit);
     }
 
     for (uint64_t wbase = warp_id * gpw; wbase < k.items; wbase += nwarps * gpw) {
@@ -733,7 +734,8 @@ size_t plan_smem_bytes(const Plan& p)
         return 128 + (size_t)STREAM_NS * STREAM_SLOT + extra;
     }
     if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements
-        return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.nq <= (uint64_t)ROW_SPLIT_MAX) ? ROW_SPLIT_MAX * 8 : 0;
+        return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.group > 1 && p.nq <= (uint64_t)ROW_SPLIT_MAX)
+                   ? ROW_SPLIT_MAX * 8 : 0;
     const size_t es = acc_size(p.dtype);
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
     // fp64 with the double-float mix: b's split beside the staged b (column, strided, thin)
