@@ -246,6 +246,59 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
     const uint64_t items = P.S * P.nseg;
     const uint64_t R = rows_per_group(P.seg_len, G);
     constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
+    constexpr int M = U / 2;
+    if (P.nseg == 1 && P.nq % V == 0 && P.nq / V <= (uint64_t)G * M) {
+        // short rows (at most U/2 vectors per lane): two rows of the group per
+        // round with all their loads in flight together; b is the same for both
+        const uint64_t nv = P.nq / V;
+        for (uint64_t r = 0; r < R; r += 2) {
+            const uint64_t item0 = (lu * R + r) * gpc + threadIdx.x / G;
+            const uint64_t item1 = (lu * R + r + 1) * gpc + threadIdx.x / G;
+            const bool valid0 = item0 < items;
+            const bool valid1 = r + 1 < R && item1 < items;
+            float a0[M][V], a1[M][V], bv[M][V];
+#pragma unroll
+            for (int t = 0; t < M; ++t) {
+                const uint64_t kv = gl + (uint64_t)t * G;
+                const bool in = kv < nv;
+                if (in && valid0) load_a<float, float, V>(P.a + item0 * P.nq + kv * V, a0[t]);
+                else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) a0[t][v] = 0.f;
+                }
+                if (in && valid1) load_a<float, float, V>(P.a + item1 * P.nq + kv * V, a1[t]);
+                else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) a1[t][v] = 0.f;
+                }
+#pragma unroll
+                for (int v = 0; v < V; ++v) bv[t][v] = in ? __ldg(P.b + kv * V + v) : 0.f;
+            }
+            Acc<float, KAHAN> c0, c1;
+            c0.init();
+            c1.init();
+#pragma unroll
+            for (int t = 0; t < M; ++t)
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    c0.fma_add(a0[t][v], bv[t][v]);
+                    c1.fma_add(a1[t][v], bv[t][v]);
+                }
+            for (int off = G >> 1; off > 0; off >>= 1) {
+                const float s0 = __shfl_xor_sync(0xffffffffu, c0.s, off);
+                const float k0 = __shfl_xor_sync(0xffffffffu, c0.c, off);
+                const float s1 = __shfl_xor_sync(0xffffffffu, c1.s, off);
+                const float k1 = __shfl_xor_sync(0xffffffffu, c1.c, off);
+                c0.merge(s0, k0);
+                c1.merge(s1, k1);
+            }
+            if (gl == 0) {
+                if (valid0) P.c[item0] = c0.value();
+                if (valid1) P.c[item1] = c1.value();
+            }
+        }
+        return;
+    }
     for (uint64_t r = 0; r < R; ++r) {
         const uint64_t item = (lu * R + r) * gpc + threadIdx.x / G;
         const bool valid = item < items;
@@ -416,9 +469,11 @@ template <bool KAHAN>
 // Resident CTAs per SM the executor is compiled for (registers capped so that
 // this many fit): more warps in flight per SM for the latency-bound units.
 // Measured on GB300 (4096 uneven problems, fixed rule): 1 -> 6.1 ms,
-// 5 -> 3.9 ms, 6 -> 3.7 ms, 7 and 8 -> 3.5 ms per launch, despite spills.
+// 5 -> 3.9 ms, 6 -> 3.7 ms, 7 and 8 -> 3.5 ms per launch, despite spills;
+// with two short rows per round in the row units 6, 7 and 8 all give
+// 3.47-3.50 ms, 6 with the fewest spills.
 #ifndef TLIBG_BATCH_MIN_CTAS
-#define TLIBG_BATCH_MIN_CTAS 8
+#define TLIBG_BATCH_MIN_CTAS 6
 #endif
 __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS) batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map,
                                                     BCtl* ctl, BPair* __restrict__ part)
