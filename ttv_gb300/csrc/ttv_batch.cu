@@ -238,6 +238,21 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
 // --------------------------------------------------------------------------
 // the persistent executor
 // --------------------------------------------------------------------------
+// Row units read A through L1 when a lane's loads are narrower than 16 bytes:
+// the lanes of a group then cover a fraction of each 32-byte sector per load and
+// the group's next loads ask for the rest.
+#ifndef TLIBG_BATCH_ROW_L1
+#define TLIBG_BATCH_ROW_L1 1
+#endif
+template <int V>
+__device__ __forceinline__ void row_load(const float* p, float (&out)[V])
+{
+    if constexpr (TLIBG_BATCH_ROW_L1 && V < 4)
+        load_a_l1<float, float, V>(p, out);
+    else
+        load_a<float, float, V>(p, out);
+}
+
 template <int V, bool KAHAN>
 __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPair* __restrict__ part)
 {
@@ -261,12 +276,12 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
             for (int t = 0; t < M; ++t) {
                 const uint64_t kv = gl + (uint64_t)t * G;
                 const bool in = kv < nv;
-                if (in && valid0) load_a<float, float, V>(P.a + item0 * P.nq + kv * V, a0[t]);
+                if (in && valid0) row_load<V>(P.a + item0 * P.nq + kv * V, a0[t]);
                 else {
 #pragma unroll
                     for (int v = 0; v < V; ++v) a0[t][v] = 0.f;
                 }
-                if (in && valid1) load_a<float, float, V>(P.a + item1 * P.nq + kv * V, a1[t]);
+                if (in && valid1) row_load<V>(P.a + item1 * P.nq + kv * V, a1[t]);
                 else {
 #pragma unroll
                     for (int v = 0; v < V; ++v) a1[t][v] = 0.f;
@@ -319,7 +334,7 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
                 float av[U][V], bv[U][V];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    load_a<float, float, V>(ap + (kv + u * G) * V, av[u]);
+                    row_load<V>(ap + (kv + u * G) * V, av[u]);
 #pragma unroll
                     for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
                 }
@@ -331,7 +346,7 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
 #pragma unroll 4
             for (; kv < nv; kv += G) {
                 float av[V];
-                load_a<float, float, V>(ap + kv * V, av);
+                row_load<V>(ap + kv * V, av);
 #pragma unroll
                 for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
             }
