@@ -293,9 +293,6 @@ int pow2_floor(uint64_t x)
 
 // Streamed kernel: A as rows of L contiguous elements, R rows per 16 KB chunk,
 // a static block of units per CTA (row form: rows; column form: (s, segment)).
-#ifndef TLIBG_F64_SHORT_ROWS
-#define TLIBG_F64_SHORT_ROWS 1
-#endif
 #ifndef TLIBG_SCALAR_OUTPUTS
 #define TLIBG_SCALAR_OUTPUTS 2
 #endif
@@ -510,9 +507,6 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
             const uint64_t nv = cn.nq / V;
             pl.rows_m = nv <= (uint64_t)G ? 1 : (nv <= 2 * (uint64_t)G ? 2 : 0);
         }
-        // fp64 rows of one lane and at most 8 vectors: two rows per lane in flight
-        if (nseg == 1 && cn.nq % V == 0 && dtype == F64 && G == 1 && cn.nq / V <= 8 && TLIBG_F64_SHORT_ROWS)
-            pl.rows_m = 8;
         const uint64_t groups_per_cta = BLOCK / G;
         pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * cps, cdiv(pl.items, groups_per_cta)));
         pl.items_per_cta = 0;

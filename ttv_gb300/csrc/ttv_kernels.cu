@@ -316,10 +316,7 @@ __device__ __forceinline__ void row_short(const KArgs& k, uint32_t G, uint32_t l
             for (int t = 0; t < M; ++t) {
                 const uint64_t kv = gl + (uint64_t)t * G;
                 if (item < k.items && kv < nv) {
-                    if (G == 1)   // one lane per row: keep the sector's other half in L1
-                        load_a_l1<TA, T, V>(A + item * k.nq + kv * V, av[r][t]);
-                    else
-                        load_a<TA, T, V>(A + item * k.nq + kv * V, av[r][t]);
+                    load_a<TA, T, V>(A + item * k.nq + kv * V, av[r][t]);
                 } else {
 #pragma unroll
                     for (int v = 0; v < V; ++v) av[r][t][v] = T(0);
@@ -422,13 +419,12 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
 }
 
 // Short rows as their own kernel (its registers do not weigh on the general
-// row kernel): M vectors per lane of each row, R = U / M rows in flight (two
-// rows of up to eight vectors for fp64 rows owned by one lane).
+// row kernel): M vectors per lane of each row, R = U / M rows in flight.
 template <typename TA, typename T, int V, bool KAHAN, int M>
-__global__ void __launch_bounds__(BLOCK, (M >= 8 ? 2 : min_ctas<TA, V>())) row_short_kernel(KArgs k)
+__global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_short_kernel(KArgs k)
 {
     constexpr int U = loads_in_flight<TA, V>();
-    constexpr int R = M == 1 ? U : (M == 2 ? (U >= 2 ? U / 2 : 1) : 2);
+    constexpr int R = M == 1 ? U : (U >= 2 ? U / 2 : 1);
     const uint64_t warp_id = (uint64_t(blockIdx.x) * BLOCK + threadIdx.x) >> 5;
     const uint64_t nwarps = (uint64_t(gridDim.x) * BLOCK) >> 5;
     row_short<M, R, TA, T, V, KAHAN>(k, k.group, threadIdx.x & 31u, warp_id, nwarps);
@@ -665,9 +661,6 @@ static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
     }
     if (kind == KIND_ROW && rows_m == 1) return pick_short<TA, T, 1, KAHAN>(vec);
     if (kind == KIND_ROW && rows_m == 2) return pick_short<TA, T, 2, KAHAN>(vec);
-    if constexpr (std::is_same<TA, double>::value) {
-        if (kind == KIND_ROW && rows_m == 8) return pick_short<TA, T, 8, KAHAN>(vec);
-    }
     if (kind == KIND_ROW) {
         switch (vec) {
         case 1: return row_kernel<TA, T, 1, KAHAN>;
