@@ -13,6 +13,11 @@
 
 namespace tlibg {
 
+// Scalar loads each thread keeps in flight (over its MO outputs).
+#ifndef TLIBG_STRIDED_LOADS
+#define TLIBG_STRIDED_LOADS 16
+#endif
+
 template <int UB, int MO, bool PRE, typename TA, typename T, typename AccT>
 __device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* A, const uint64_t (&ofs)[MO],
                                              const bool (&ok)[MO], uint64_t P, const T* bs, const float2* bsp,
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
     const uint64_t outputs = k.S * P;
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
-    constexpr int U = (loads_in_flight<TA, 1>() / MO) < 1 ? 1 : loads_in_flight<TA, 1>() / MO;
+    constexpr int U = (TLIBG_STRIDED_LOADS / MO) < 1 ? 1 : TLIBG_STRIDED_LOADS / MO;
 
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
