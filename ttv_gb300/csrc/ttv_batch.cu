@@ -68,10 +68,15 @@ struct BCtl {
 constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
 constexpr int BCAP_F32 = BMAX_F32 + 4;
 
+// Lanes per row of row-form variant g = 0: G = TLIBG_BATCH_ROW_G0 << g.
+#ifndef TLIBG_BATCH_ROW_G0
+#define TLIBG_BATCH_ROW_G0 4
+#endif
+
 __host__ __device__ inline void decode_variant(int kind, int v, uint64_t nq, int* group, uint32_t* nseg)
 {
     const int gi = (v >> 1) & 3, si = v & 1;
-    *group = kind == KIND_ROW ? (4 << gi) : (1 << gi);
+    *group = kind == KIND_ROW ? (TLIBG_BATCH_ROW_G0 << gi) : (1 << gi);
     uint64_t ns = 1;
     if (si) ns = nq >= 64 ? 4 : (nq >= 16 ? 2 : 1);
     const uint64_t min_seg = kind == KIND_COL ? (nq + BMAX_F32 - 1) / BMAX_F32 : 1;
@@ -613,6 +618,9 @@ int heuristic_variant(int kind, uint64_t P, uint64_t nq, uint64_t S, int vec)
     // problem has few outputs and a long contraction; never split.
     (void)vec;
     int g = 0;
+    if (kind == KIND_ROW) {
+        while ((TLIBG_BATCH_ROW_G0 << g) < 4 && g < 3) ++g;
+    }
     if (kind == KIND_COL) {
         const uint64_t outputs = S * P;
         if (outputs < 512 && nq >= 128) g = 2;
