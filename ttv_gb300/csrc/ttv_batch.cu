@@ -16,7 +16,7 @@
 //                 staged by TMA); the CTA that completes a split problem's
 //                 last unit combines its partials in fixed segment order
 //
-// Variants (8): index v = 2*g + s.  Row form: lanes per row G = 4 << g;
+// Variants (8): index v = 2*g + s.  Row form: lanes per row G = 1 << g;
 // column form: warps along q WI = 1 << g.  s = 1 splits q into up to 4
 // segments (two-phase, deterministic).
 #include "ttv_device.cuh"
@@ -68,9 +68,13 @@ struct BCtl {
 constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
 constexpr int BCAP_F32 = BMAX_F32 + 4;
 
-// Lanes per row of row-form variant g = 0: G = TLIBG_BATCH_ROW_G0 << g.
+// Lanes per row of the row-form variants: G = TLIBG_BATCH_ROW_G0 << g, g = 0..3.
+// Measured on GB300 (22,000 tuned shapes in mixed batches): one lane per row is
+// the best single variant for the batch's rows of 8-512 elements (regret 4.5 %
+// against 13.5 % for four lanes), and with G in {1, 2, 4, 8} the learned
+// selection gains 8 % over a fixed four lanes in the 4096-problem launch.
 #ifndef TLIBG_BATCH_ROW_G0
-#define TLIBG_BATCH_ROW_G0 4
+#define TLIBG_BATCH_ROW_G0 1
 #endif
 
 __host__ __device__ inline void decode_variant(int kind, int v, uint64_t nq, int* group, uint32_t* nseg)
@@ -614,13 +618,10 @@ int batch_vec(int kind, const CanonView& cn, const void* a, const void* b)
 // The fixed rule the engine uses without the cost model.
 int heuristic_variant(int kind, uint64_t P, uint64_t nq, uint64_t S, int vec)
 {
-    // Row form: four lanes per row; column form: one warp row per tile unless the
-    // problem has few outputs and a long contraction; never split.
+    // Row form: the first lane count (one lane per row); column form: one warp row
+    // per tile unless the problem has few outputs and a long contraction; never split.
     (void)vec;
     int g = 0;
-    if (kind == KIND_ROW) {
-        while ((TLIBG_BATCH_ROW_G0 << g) < 4 && g < 3) ++g;
-    }
     if (kind == KIND_COL) {
         const uint64_t outputs = S * P;
         if (outputs < 512 && nq >= 128) g = 2;
