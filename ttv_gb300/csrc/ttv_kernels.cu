@@ -738,8 +738,8 @@ size_t plan_smem_bytes(const Plan& p)
                    ? ROW_SPLIT_MAX * 8 : 0;
     const size_t es = acc_size(p.dtype);
     const size_t bcap = BSTAGE_BYTES / es + 16 / es;
-    // fp64 with the double-float mix: b's split beside the staged b (column, strided, thin)
-    const size_t split = (p.dtype == F64 && p.kahan && p.kind != KIND_COL_REALIGN) ? bcap * 8 : 0;
+    // fp64 with the double-float mix: b's split beside the staged b (every column form)
+    const size_t split = (p.dtype == F64 && p.kahan) ? bcap * 8 : 0;
     if (p.kind == KIND_COL_THIN) return 16 + bcap * es + split + (size_t)(BLOCK / 32) * 32 * 2 * p.vec * es;
     const size_t WO = (BLOCK / 32) / p.group;
     const size_t red = p.group > 1 ? (size_t)(p.group - 1) * WO * 32 * 2 * p.vec * p.mo * es : 0;

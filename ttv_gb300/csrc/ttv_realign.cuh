@@ -46,7 +46,10 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);
     constexpr int BCAP = BSTAGE_BYTES / (int)sizeof(T) + 16 / (int)sizeof(T);
-    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T));
+    constexpr bool PRES = presplit_b<T, KAHAN>();
+    float2* bsplit = reinterpret_cast<float2*>(smem_raw + 16 + BCAP * sizeof(T));
+    T* red = reinterpret_cast<T*>(smem_raw + 16 + BCAP * sizeof(T) + (PRES ? BCAP * sizeof(float2) : 0));
+    bool b_split_ok = false;
 
     const uint32_t WI = k.group;
     const uint32_t WO = (BLOCK / 32) / WI;
@@ -83,8 +86,10 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
             if (!stage_b<T>(sb, B, ib, ie, bar, phase, abort_flag, &g_device_error)) return;
             staged_seg = seg;
             off = (uint32_t)((reinterpret_cast<uintptr_t>(B + ib) & 15u) / sizeof(T));
+            if constexpr (PRES) b_split_ok = stage_b_split<T>(sb + off, (uint32_t)(ie - ib), bsplit);
         }
         const T* bs = sb + off - ib;   // bs[i] = b[i] for i in [ib, ie)
+        const float2* bsp = bsplit - ib;
 
         const uint64_t ow = tile * TO + uint64_t(wo) * 32u * V;   // the warp's window
         const uint64_t o0 = ow + uint64_t(lane) * V;
@@ -118,7 +123,10 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
                             nxt[v] = lane == 31u ? ext[u][v] : t;
                         }
                         realign_vec<T, V>(cur[u], nxt, r[u], av);
-                        row_fma<V>(acc, av, bs[i + u * WI], u);
+                        if (PRES && b_split_ok)
+                            row_fma<V, PRES>(acc, av, bs[i + u * WI], u, bsp + i + u * WI);
+                        else
+                            row_fma<V>(acc, av, bs[i + u * WI], u);
                     }
                     renorm_all<V>(acc);
                 }
@@ -135,7 +143,10 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
                         nxt[v] = lane == 31u ? ext[v] : t;
                     }
                     realign_vec<T, V>(cur, nxt, rr, av);
-                    row_fma<V>(acc, av, bs[i]);
+                    if (PRES && b_split_ok)
+                        row_fma<V, PRES>(acc, av, bs[i], 0, bsp + i);
+                    else
+                        row_fma<V>(acc, av, bs[i]);
                 }
                 renorm_all<V>(acc);
             } else {
