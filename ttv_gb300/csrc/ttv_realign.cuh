@@ -14,7 +14,9 @@
 // element of the window, so no access leaves A's allocation.  Windows that
 // straddle two slabs or end past a row (the last window of each row) take
 // scalar loads.  Work items, the b stage, the warps stacked along q and the
-// split reduction are those of the column kernel.
+// split reduction are those of the column kernel.  Chosen only on request
+// (TLIBG_KIND_COL_REALIGN): the strided kernel's scalar loads with two
+// outputs per thread measured faster on every unaligned prefix of the sweeps.
 #pragma once
 
 namespace tlibg {

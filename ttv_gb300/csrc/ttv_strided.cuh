@@ -2,13 +2,14 @@
 // ttv_kernels.cu).
 //
 // Prefixes whose rows allow no vector load (P odd, or A at an odd element
-// offset) and are too short for the realigned kernel: each thread owns MO
-// outputs 32 apart (o, o + 32, ...), so every warp load of every output set
-// is still one coalesced run of 32 elements, and each row i puts MO
-// independent loads in flight per thread instead of one.  Short contractions
-// (a few dozen rows) then need half or a quarter of the round trips per
-// output.  Tiles, the b stage, warps stacked along q and the split reduction
-// are those of the column kernel.
+// offset): each thread owns MO outputs 32 apart (o, o + 32, ...), so every
+// warp load of every output set is still one coalesced run of 32 elements,
+// and each row i puts MO independent loads in flight per thread instead of
+// one.  Short contractions (a few dozen rows) then need half the round trips
+// per output.  Tiles, the b stage (and its double-float split for fp64),
+// warps stacked along q and the split reduction are those of the column
+// kernel.  Measured on GB300 ahead of the realigning kernel for every
+// unaligned prefix of the sweeps, which is why that one is only on request.
 #pragma once
 
 namespace tlibg {
