@@ -138,6 +138,14 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
  * use them.  opt == NULL removes the hint; with P = n_q = S = 0, all hints. */
 int tlibg_plan_hint(int dtype, uint64_t P, uint64_t nq, uint64_t S, const tlibg_options* opt);
 
+/* Self-test of the failure path: launches one kernel whose mbarrier wait
+ * nothing completes, with a short poll limit (a few milliseconds).  The wait
+ * gives up, records it in the device error word and the kernel returns; the
+ * call then reports exactly what an expired wait inside a TTV reports:
+ * TLIBG_ERR_TIMEOUT with its message.  No trap, no fault: the context stays
+ * usable.  Synchronises `stream`. */
+int tlibg_selftest_bounded_wait(void* stream);
+
 /* Where a pointer lives: 1 device or managed memory, 0 host memory (pageable
  * or page-locked; every pointer when no device is present), -1 null or
  * unknown.  The compute entry points refuse pageable host pointers

@@ -543,3 +543,22 @@ def test_pageable_host_pointers_refused(engine, torch_dev):
             engine.ttv(q, 3, a, na, wa, pia, b, [16], c, nc, wc, pic, sync=True)
     engine.ttv(q, 3, a_d, na, wa, pia, b_d, [16], c_d, nc, wc, pic, sync=True)   # still usable
     assert engine.device_error() == 0
+
+
+def test_bounded_wait_expiry_reports_timeout(engine, orc, torch_dev):
+    """An mbarrier wait that nothing completes gives up after its poll limit:
+    the call returns TLIBG_ERR_TIMEOUT with the engine's message, nothing
+    traps or hangs, and the next TTV on the same context is correct."""
+    import ctypes
+    torch, dev = torch_dev
+    L = engine.library()
+    L.tlibg_selftest_bounded_wait.argtypes = [ctypes.c_void_p]
+    st = L.tlibg_selftest_bounded_wait(torch.cuda.current_stream().cuda_stream)
+    assert st == engine.ERR_TIMEOUT, st
+    assert "bounded device wait expired" in engine._last_error()
+    assert engine.device_error() == 0   # read and cleared by the call
+    na, pia, q = [64, 48, 32], [1, 2, 3], 2
+    rng = np.random.default_rng(1)
+    a = rng.uniform(-1, 1, int(np.prod(na))).astype(np.float32)
+    b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)
+    check(orc, engine, torch, dev, q, na, pia, a, b)

@@ -755,6 +755,20 @@ int tlibg_validate(size_t q, size_t p, const size_t* na, const size_t* wa, const
     return st ? st : ok();
 }
 
+int tlibg_selftest_bounded_wait(void* stream)
+{
+    DevInfo d = dev_info();
+    if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_wait_probe(st, 1u << 14);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    g_launches += 1;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
+    if (read_and_clear_device_error())
+        return fail(TLIBG_ERR_TIMEOUT, "tlibg: a bounded device wait expired; results are invalid");
+    return ok();
+}
+
 int tlibg_pointer_location(const void* p)
 {
     if (!p) return -1;

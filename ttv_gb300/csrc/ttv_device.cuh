@@ -298,10 +298,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 }
 
 // Bounded wait; false (and the device error word set) if the phase never
-// completed within WAIT_POLL_LIMIT polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned int* err)
+// completed within `limit` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned int* err,
+                                                  uint32_t limit = WAIT_POLL_LIMIT)
 {
-    for (uint32_t it = 0; it < WAIT_POLL_LIMIT; ++it)
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     atomicOr(err, ERR_WAIT_TIMEOUT);
     return false;

@@ -889,6 +889,26 @@ cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_
     return cudaSuccess;
 }
 
+// Self-test of the expiry path: an mbarrier nothing arrives at, waited on
+// with a short poll limit; the wait gives up, sets the device error word and
+// the kernel returns (no trap, no fault, the context stays usable).
+__global__ void wait_expiry_probe(uint32_t limit)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait_bounded(&bar, 0u, &g_device_error, limit);
+}
+
+cudaError_t launch_wait_probe(cudaStream_t stream, uint32_t limit)
+{
+    wait_expiry_probe<<<1, 32, 0, stream>>>(limit);
+    return cudaGetLastError();
+}
+
 unsigned int read_and_clear_device_error()
 {
     unsigned int v = 0, zero = 0;

@@ -72,4 +72,7 @@ int plan_ctas_per_sm(const Plan& p);
 
 unsigned int read_and_clear_device_error();
 
+// Self-test kernel: one bounded mbarrier wait that nothing completes.
+cudaError_t launch_wait_probe(cudaStream_t stream, uint32_t limit);
+
 }  // namespace tlibg
