@@ -675,6 +675,7 @@ int run_device(int dtype, size_t q, size_t p, const void* a, const size_t* na, c
                const size_t* pia, const void* b, const size_t* nb, void* c, const size_t* nc,
                const size_t* wc, const size_t* pic, const tlibg_options* opt, cudaStream_t stream)
 {
+    NvtxRange nvtx("tlibg_ttv");
     Canon cn;
     int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
     if (st) return st;
@@ -832,6 +833,7 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
 {
     if (dtype != F32 && dtype != F64 && dtype != BF16A)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: unknown element type");
+    NvtxRange nvtx("tlibg_ttv_host");
     Canon cn;
     int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
     if (st) return st;

@@ -906,6 +906,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
 
 int tlibg_batch_launch(tlibg_batch* bt, void* stream)
 {
+    NvtxRange nvtx("tlibg_batch_launch");
     if (!bt) return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_launch: null batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (bt->exec) {

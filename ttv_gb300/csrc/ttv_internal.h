@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -10,6 +11,15 @@
 #include "ttv_kernels.cuh"
 
 namespace tlibg {
+
+// NVTX range over one C-ABI call (header-only NVTX: a no-op unless a
+// profiler such as Nsight Systems attaches).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct CanonView {
     uint64_t P = 1, nq = 1, S = 1;
