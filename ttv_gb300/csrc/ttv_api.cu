@@ -293,9 +293,6 @@ int pow2_floor(uint64_t x)
 
 // Streamed kernel: A as rows of L contiguous elements, R rows per 16 KB chunk,
 // a static block of units per CTA (row form: rows; column form: (s, segment)).
-#ifndef TLIBG_F64_STREAM_ROWS
-#define TLIBG_F64_STREAM_ROWS 1
-#endif
 #ifndef TLIBG_SCALAR_OUTPUTS
 #define TLIBG_SCALAR_OUTPUTS 2
 #endif
@@ -432,10 +429,9 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         const size_t vb = 16 / ea;
         rows_aligned = cn.nq % vb == 0 && aligned(a, 16) && aligned(b, 16);
     }
-    const bool stream_default = eligible && cn.P == 1 && cn.nq < 64 &&
-                                (dtype == F64 ? TLIBG_F64_STREAM_ROWS != 0 : !rows_aligned);
+    const bool stream_default = eligible && cn.P == 1 && !rows_aligned && dtype != F64 && cn.nq < 64;
     if ((opt && opt->kind == KIND_STREAM) || (stream_default && !(opt && opt->kind >= 0))) {
-        if (dtype == F64) pl.kahan = (opt && opt->accumulate == TLIBG_ACC_PLAIN) ? 0 : 1;
+        if (dtype == F64) pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
         return make_stream_plan(pl, cn, opt, sms, out);
     }
     const int vmax = (int)(16 / ea);

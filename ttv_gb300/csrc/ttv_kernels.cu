@@ -731,8 +731,6 @@ size_t plan_smem_bytes(const Plan& p)
         const size_t es = acc_size(p.dtype);
         size_t extra = 2 * (size_t)STREAM_NT * es;
         if (!p.stream_col) extra = std::max(extra, (size_t)p.L * es);
-        // fp64 rows with the mix: b's split (float2 per element) after b (rounded to an even count)
-        if (!p.stream_col && p.dtype == F64 && p.kahan) extra = (p.L + 1) / 2 * 2 * es + (size_t)p.L * 8;
         return 128 + (size_t)STREAM_NS * STREAM_SLOT + extra;
     }
     if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements

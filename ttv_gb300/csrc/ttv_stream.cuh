@@ -147,22 +147,11 @@ __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
         *abort_flag = 0;
         fence_mbar_init();
     }
-    // fp64 rows with the DFMA / double-float mix: b's split beside b
-    constexpr bool MIX = !COL && std::is_same<typename AccSel<T, KAHAN>::type, AccDF>::value;
-    float2* sbs = reinterpret_cast<float2*>(sbuf + (k.L + 1) / 2 * 2);
-    int b_ok = 1;
     if (!COL && warp > 0) {
         // row form: the whole b in shared memory (L elements)
-        for (uint64_t e = threadIdx.x - 32; e < k.L; e += STREAM_NT) {
-            sbuf[e] = Bv[e];
-            if constexpr (MIX) {
-                const DSplit d = split_double(Bv[e]);
-                sbs[e] = make_float2(d.hi, d.lo);
-                b_ok &= d.ok ? 1 : 0;
-            }
-        }
+        for (uint64_t e = threadIdx.x - 32; e < k.L; e += STREAM_NT) sbuf[e] = Bv[e];
     }
-    const bool b_split_ok = __syncthreads_and(b_ok) != 0;
+    __syncthreads();
 
     if (warp == 0) {
         // ---------------- producer ----------------
@@ -218,35 +207,8 @@ __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
                     const TA* rp = rows + rr * k.L;
                     const uint32_t Lr = (uint32_t)k.L;
                     const uint32_t rot = (Lr & (Lr - 1)) == 0 ? (uint32_t)((rr * G) & (Lr - 1)) : 0u;
-                    if constexpr (MIX) {
-                        if (b_split_ok) {
-                            // every other element of the lane on the DFMA pipe, the rest emulated
-                            // with b's pre-split halves; renormalised every eight elements
-                            uint32_t n = 0;
-                            auto step = [&](uint32_t e) {
-                                const T a = Cvt<TA, T>::f(rp[e]);
-                                if (n & 1u) {
-                                    const float2 t = sbs[e];
-                                    DSplit bs;
-                                    bs.hi = t.x;
-                                    bs.lo = t.y;
-                                    bs.ok = true;
-                                    acc.add_split(split_double(a), bs, a, sbuf[e]);
-                                } else {
-                                    acc.d = fma(a, sbuf[e], acc.d);
-                                }
-                                if ((++n & 7u) == 0u) acc.renorm();
-                            };
-                            for (uint32_t e = rot + gl; e < Lr; e += G) step(e);
-                            for (uint32_t e = gl; e < rot; e += G) step(e);
-                        } else {
-                            for (uint32_t e = rot + gl; e < Lr; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
-                            for (uint32_t e = gl; e < rot; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
-                        }
-                    } else {
-                        for (uint32_t e = rot + gl; e < Lr; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
-                        for (uint32_t e = gl; e < rot; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
-                    }
+                    for (uint32_t e = rot + gl; e < Lr; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
+                    for (uint32_t e = gl; e < rot; e += G) acc.fma_add(Cvt<TA, T>::f(rp[e]), sbuf[e]);
                 }
                 acc.fold();
                 for (uint32_t off = G >> 1; off > 0; off >>= 1) {
