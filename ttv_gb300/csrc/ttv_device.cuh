@@ -147,8 +147,12 @@ __device__ __forceinline__ DSplit split_double(double x)
     const uint32_t top = __funnelshift_l(lo32, hi32, 3) + (128u << 23);
     const uint32_t hb = (top & 0x7fffffffu) | (hi32 & 0x80000000u);
     r.hi = __uint_as_float(hb);
-    const float scale = __uint_as_float((hb & 0xff800000u) - (52u << 23));   // +-2^(e-1075)
-    r.lo = (float)(lo32 & 0x1fffffffu) * scale;
+    // +-2^(e-1046) (hi's sign and exponent field minus 23; the field is at
+    // least 67, so nothing borrows from the sign); the same with significand
+    // bits 28..6 of x is +-(1 + f/2^23) 2^(e-1046), and the difference of the
+    // two is exact (Sterbenz): +-f 2^(e-1069), the next 23 bits of x
+    const uint32_t sgnexp = (hb & 0xff800000u) - (23u << 23);
+    r.lo = __uint_as_float(sgnexp | ((lo32 >> 6) & 0x7fffffu)) - __uint_as_float(sgnexp);
     return r;
 }
 

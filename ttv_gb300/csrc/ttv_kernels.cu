@@ -173,13 +173,18 @@ template <int V, typename AccT> __device__ __forceinline__ void renorm_all(AccT 
 // UB rows of the contracted mode for one thread: all loads first, then the
 // products (column form: b[i] shared by the V outputs; u alternates the fp64
 // mix when V == 1).
+// rp points at the thread's vector in row i and moves on by `step` elements
+// (WI rows) per row: one pointer add per load.
 template <int UB, int V, bool PRE = false, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void col_rows(AccT (&acc)[V], const TA* ap, uint64_t P, const T* bs, uint64_t i,
+__device__ __forceinline__ void col_rows(AccT (&acc)[V], const TA*& rp, uint64_t step, const T* bs, uint64_t i,
                                          uint32_t WI, const float2* bsp = nullptr)
 {
     T av[UB][V];
 #pragma unroll
-    for (int u = 0; u < UB; ++u) load_a<TA, T, V>(ap + (i + u * WI) * P, av[u]);
+    for (int u = 0; u < UB; ++u) {
+        load_a<TA, T, V>(rp, av[u]);
+        rp += step;
+    }
 #pragma unroll
     for (int u = 0; u < UB; ++u) row_fma<V, PRE>(acc, av[u], bs[i + u * WI], u, PRE ? bsp + i + u * WI : nullptr);
     renorm_all<V>(acc);
@@ -192,20 +197,22 @@ template <int U, int V, bool PRE, typename TA, typename T, typename AccT>
 __device__ __forceinline__ void col_loop(AccT (&acc)[V], const TA* ap, uint64_t P, const T* bs, const float2* bsp,
                                          uint64_t i, uint64_t ie, uint32_t WI)
 {
-    for (; i + (U - 1) * WI < ie; i += U * WI) col_rows<U, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+    const TA* rp = ap + i * P;
+    const uint64_t step = uint64_t(WI) * P;
+    for (; i + (U - 1) * WI < ie; i += U * WI) col_rows<U, V, PRE>(acc, rp, step, bs, i, WI, bsp);
     if constexpr (U >= 4) {
         if (i + (U / 2 - 1) * WI < ie) {
-            col_rows<U / 2, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+            col_rows<U / 2, V, PRE>(acc, rp, step, bs, i, WI, bsp);
             i += (U / 2) * WI;
         }
     }
     if constexpr (U >= 8) {
         if (i + (U / 4 - 1) * WI < ie) {
-            col_rows<U / 4, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+            col_rows<U / 4, V, PRE>(acc, rp, step, bs, i, WI, bsp);
             i += (U / 4) * WI;
         }
     }
-    for (; i < ie; i += WI) col_rows<1, V, PRE>(acc, ap, P, bs, i, WI, bsp);
+    for (; i < ie; i += WI) col_rows<1, V, PRE>(acc, rp, step, bs, i, WI, bsp);
 }
 
 // fp64 with the double-float mix: b's split is computed once per staged
@@ -470,7 +477,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
     const uint64_t last = min(k.items, first + k.items_per_cta);
 
     for (uint64_t item = first; item < last; ++item) {
-        const uint64_t seg = item / k.ntiles;
+        const uint64_t seg = idx_div(item, k.tdiv);
         const uint64_t tile = item - seg * k.ntiles;
         const uint64_t ib = seg * k.seg_len;
         const uint64_t ie = min(k.nq, ib + k.seg_len);
@@ -490,7 +497,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].init();
         if (valid) {
-            const uint64_t s = o0 / k.P;
+            const uint64_t s = idx_div(o0, k.pdiv);
             const uint64_t j = o0 - s * k.P;
             const TA* ap = A + (s * k.nq) * k.P + j;
             if constexpr (PRES) {
@@ -836,6 +843,8 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     } else {
         k.ntiles = 0;
     }
+    k.pdiv = make_idx_div(plan.P, plan.S * plan.P);
+    k.tdiv = make_idx_div(k.ntiles, plan.items);
     const size_t smem = plan_smem_bytes(plan);
     fn<<<plan.grid, BLOCK, smem, stream>>>(k);
     cudaError_t err = cudaGetLastError();

@@ -41,6 +41,45 @@ struct Plan {
 // Whether the streamed kernel can take a problem (whole rows fit a stage).
 bool stream_eligible(int dtype, uint64_t P, uint64_t nq);
 
+// --------------------------------------------------------------------------
+// division by a divisor fixed for a launch (output -> slice, item -> segment)
+// --------------------------------------------------------------------------
+// When every dividend and the divisor fit 32 bits, n / d is one multiply-high,
+// a subtract, an add and two shifts: the round-up method of Granlund and
+// Montgomery ("Division by invariant integers using multiplication", PLDI
+// 1994, section 4) with l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// t = hi32(m n), n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0).
+// Otherwise the plain 64-bit division.  Built on the host per launch.
+struct IdxDiv {
+    uint64_t d;
+    uint32_t m;
+    uint8_t s1, s2, fast;
+};
+
+inline IdxDiv make_idx_div(uint64_t d, uint64_t max_dividend)
+{
+    IdxDiv v{d == 0 ? 1 : d, 0, 0, 0, 0};
+    if (v.d < (uint64_t(1) << 32) && max_dividend < (uint64_t(1) << 32)) {
+        uint32_t l = 0;
+        while ((uint64_t(1) << l) < v.d) ++l;
+        v.m = (uint32_t)(((uint64_t(1) << 32) * ((uint64_t(1) << l) - v.d)) / v.d + 1);
+        v.s1 = (uint8_t)(l < 1 ? l : 1);
+        v.s2 = (uint8_t)(l > 0 ? l - 1 : 0);
+        v.fast = 1;
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint64_t idx_div(uint64_t n, const IdxDiv& v)
+{
+    if (v.fast) {
+        const uint32_t x = (uint32_t)n;
+        const uint32_t t = __umulhi(v.m, x);
+        return (t + ((x - t) >> v.s1)) >> v.s2;
+    }
+    return n / v.d;
+}
+
 struct KArgs {
     const void* a;
     const void* b;
@@ -51,6 +90,8 @@ struct KArgs {
     uint64_t items, items_per_cta, ntiles;
     uint32_t nseg;
     uint32_t group;
+    IdxDiv pdiv;      // outputs -> slice (division by P)
+    IdxDiv tdiv;      // items -> segment (division by ntiles)
 };
 
 // Bytes of partial storage a plan needs (0 when split == 1).

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
     const uint64_t last = min(k.items, first + k.items_per_cta);
 
     for (uint64_t item = first; item < last; ++item) {
-        const uint64_t seg = item / k.ntiles;
+        const uint64_t seg = idx_div(item, k.tdiv);
         const uint64_t tile = item - seg * k.ntiles;
         const uint64_t ib = seg * k.seg_len;
         const uint64_t ie = min(k.nq, ib + k.seg_len);
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[v].init();
         if (ow < outputs) {
-            const uint64_t sw = ow / P;
+            const uint64_t sw = idx_div(ow, k.pdiv);
             const uint64_t jw = ow - sw * P;
             if (jw + 32u * V <= P) {
                 // whole window inside row (sw, i, .): realigned vector loads
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
                 for (int v = 0; v < V; ++v) {
                     const uint64_t o = o0 + v;
                     ok[v] = o < outputs;
-                    const uint64_t s = ok[v] ? o / P : 0;
+                    const uint64_t s = ok[v] ? idx_div(o, k.pdiv) : 0;
                     ofs[v] = s * k.nq * P + (o - s * P);
                 }
                 for (uint64_t i = ib + wi; i < ie; i += WI) {

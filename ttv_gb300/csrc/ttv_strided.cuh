@@ -14,28 +14,46 @@
 
 namespace tlibg {
 
-// Scalar loads each thread keeps in flight (over its MO outputs).
-#ifndef TLIBG_STRIDED_LOADS
-#define TLIBG_STRIDED_LOADS 16
+// Scalar loads each thread keeps in flight (over its MO outputs): 16 for
+// 8-byte elements, 24 for narrower ones.  Measured on GB300 over the
+// symmetric sweep's unaligned prefixes: fp32 5.37 / 5.71 / 5.69 TB/s with
+// 16 / 24 / 32 loads, fp64 6.07 / 5.38 / 5.58 TB/s (fp64 carries the
+// double-float state per output, so more loads cost it occupancy).
+#ifndef TLIBG_STRIDED_LOADS_WIDE
+#define TLIBG_STRIDED_LOADS_WIDE 16
 #endif
+#ifndef TLIBG_STRIDED_LOADS_NARROW
+#define TLIBG_STRIDED_LOADS_NARROW 24
+#endif
+template <typename TA> __device__ __forceinline__ constexpr int strided_loads()
+{
+    return sizeof(TA) >= 8 ? TLIBG_STRIDED_LOADS_WIDE : TLIBG_STRIDED_LOADS_NARROW;
+}
 
+// 8-byte elements load through L1 with default caching: the sector a warp's
+// unaligned run shares with the next run is then an L1 hit (fp64 +4 % over
+// streaming loads on the symmetric sweep; fp32 unchanged, so it streams).
+template <typename TA> __device__ __forceinline__ constexpr bool strided_l1() { return sizeof(TA) == 8; }
+
+// UB rows of the contracted mode: MO loads per row, all loads first.  rp[m]
+// points at the thread's element of output m in the current row and moves
+// on by `step` elements (WI rows) per row: one pointer add per load.
 template <int UB, int MO, bool PRE, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* A, const uint64_t (&ofs)[MO],
-                                             const bool (&ok)[MO], uint64_t P, const T* bs, const float2* bsp,
-                                             uint64_t i, uint32_t WI)
+__device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* (&rp)[MO], uint64_t step, const T* bs,
+                                             const float2* bsp, uint64_t i, uint32_t WI)
 {
     T av[UB][MO];
 #pragma unroll
     for (int u = 0; u < UB; ++u)
 #pragma unroll
         for (int m = 0; m < MO; ++m) {
-            if (ok[m]) {
-                T x[1];
-                load_a<TA, T, 1>(A + ofs[m] + (i + u * WI) * P, x);
-                av[u][m] = x[0];
-            } else {
-                av[u][m] = T(0);
-            }
+            T x[1];
+            if constexpr (strided_l1<TA>())
+                load_a_l1<TA, T, 1>(rp[m], x);
+            else
+                load_a<TA, T, 1>(rp[m], x);
+            av[u][m] = x[0];
+            rp[m] += step;
         }
 #pragma unroll
     for (int u = 0; u < UB; ++u) row_fma<MO, PRE>(acc, av[u], bs[i + u * WI], u, PRE ? bsp + i + u * WI : nullptr);
@@ -43,24 +61,23 @@ __device__ __forceinline__ void strided_rows(AccT (&acc)[MO], const TA* A, const
 }
 
 template <int U, int MO, bool PRE, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void strided_loop(AccT (&acc)[MO], const TA* A, const uint64_t (&ofs)[MO],
-                                             const bool (&ok)[MO], uint64_t P, const T* bs, const float2* bsp,
-                                             uint64_t i, uint64_t ie, uint32_t WI)
+__device__ __forceinline__ void strided_loop(AccT (&acc)[MO], const TA* (&rp)[MO], uint64_t step, const T* bs,
+                                             const float2* bsp, uint64_t i, uint64_t ie, uint32_t WI)
 {
-    for (; i + (U - 1) * WI < ie; i += U * WI) strided_rows<U, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+    for (; i + (U - 1) * WI < ie; i += U * WI) strided_rows<U, MO, PRE>(acc, rp, step, bs, bsp, i, WI);
     if constexpr (U >= 4) {
         if (i + (U / 2 - 1) * WI < ie) {
-            strided_rows<U / 2, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+            strided_rows<U / 2, MO, PRE>(acc, rp, step, bs, bsp, i, WI);
             i += (U / 2) * WI;
         }
     }
     if constexpr (U >= 8) {
         if (i + (U / 4 - 1) * WI < ie) {
-            strided_rows<U / 4, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+            strided_rows<U / 4, MO, PRE>(acc, rp, step, bs, bsp, i, WI);
             i += (U / 4) * WI;
         }
     }
-    for (; i < ie; i += WI) strided_rows<1, MO, PRE>(acc, A, ofs, ok, P, bs, bsp, i, WI);
+    for (; i < ie; i += WI) strided_rows<1, MO, PRE>(acc, rp, step, bs, bsp, i, WI);
 }
 
 template <typename TA, typename T, int MO, bool KAHAN>
@@ -85,7 +102,7 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
     const uint64_t outputs = k.S * P;
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
-    constexpr int U = (TLIBG_STRIDED_LOADS / MO) < 1 ? 1 : TLIBG_STRIDED_LOADS / MO;
+    constexpr int U = (strided_loads<TA>() / MO) < 1 ? 1 : strided_loads<TA>() / MO;
 
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -101,7 +118,7 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
     const uint64_t last = min(k.items, first + k.items_per_cta);
 
     for (uint64_t item = first; item < last; ++item) {
-        const uint64_t seg = item / k.ntiles;
+        const uint64_t seg = idx_div(item, k.tdiv);
         const uint64_t tile = item - seg * k.ntiles;
         const uint64_t ib = seg * k.seg_len;
         const uint64_t ie = min(k.nq, ib + k.seg_len);
@@ -116,28 +133,31 @@ __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
         const float2* bsp = bsplit - ib;
 
         const uint64_t o0 = tile * TO + uint64_t(wo) * 32u * MO + lane;   // outputs o0 + 32 m
-        uint64_t ofs[MO];
         bool ok[MO];
-        bool any = false;
 #pragma unroll
-        for (int m = 0; m < MO; ++m) {
-            const uint64_t o = o0 + 32u * m;
-            ok[m] = o < outputs;
-            any = any || ok[m];
-            const uint64_t s = ok[m] ? o / P : 0;
-            ofs[m] = s * k.nq * P + (o - s * P);
-        }
+        for (int m = 0; m < MO; ++m) ok[m] = o0 + 32u * m < outputs;
         typename AccSel<T, KAHAN>::type acc[MO];
 #pragma unroll
         for (int m = 0; m < MO; ++m) acc[m].init();
-        if (any) {
+        if (ok[0]) {
+            // an output past the end re-reads output o0's elements (no load
+            // predicates; its sum is never stored)
+            const TA* rp[MO];
+            const uint64_t row0 = (ib + wi) * P;
+#pragma unroll
+            for (int m = 0; m < MO; ++m) {
+                const uint64_t o = ok[m] ? o0 + 32u * m : o0;
+                const uint64_t s = idx_div(o, k.pdiv);
+                rp[m] = A + s * k.nq * P + (o - s * P) + row0;
+            }
+            const uint64_t step = uint64_t(WI) * P;
             if constexpr (PRES) {
                 if (b_split_ok)
-                    strided_loop<U, MO, true>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+                    strided_loop<U, MO, true>(acc, rp, step, bs, bsp, ib + wi, ie, WI);
                 else
-                    strided_loop<U, MO, false>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+                    strided_loop<U, MO, false>(acc, rp, step, bs, bsp, ib + wi, ie, WI);
             } else {
-                strided_loop<U, MO, false>(acc, A, ofs, ok, P, bs, bsp, ib + wi, ie, WI);
+                strided_loop<U, MO, false>(acc, rp, step, bs, bsp, ib + wi, ie, WI);
             }
         }
 #pragma unroll

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KA
     const uint64_t last = min(k.items, first + k.items_per_cta);
 
     for (uint64_t item = first; item < last; ++item) {
-        const uint64_t seg = item / k.S;
+        const uint64_t seg = idx_div(item, k.tdiv);
         const uint64_t s = item - seg * k.S;
         const uint64_t ib = seg * k.seg_len;
         const uint64_t ie = min(k.nq, ib + k.seg_len);
