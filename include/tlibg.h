@@ -60,6 +60,9 @@ extern "C" {
                                    /*   for prefixes whose rows are not 16-byte aligned (fp32/fp64) */
 #define TLIBG_KIND_COL_THIN 4      /* column GEMV for thin prefixes (P / vector width divides 32):  */
                                    /*   several rows per warp step, for few outputs and long q      */
+#define TLIBG_KIND_ROW_TILE 5      /* short rows (P == 1, n_q <= 64, no split): tiles of 32 rows    */
+                                   /*   moved to shared memory by TMA, one lane per row, any        */
+                                   /*   alignment                                                   */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */

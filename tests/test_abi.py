@@ -140,8 +140,29 @@ def test_planner_kernel_family(engine):
     # stage -> the streamed kernel (row form); fp64 rows -> row kernel
     assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
     assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_ROW
-    assert engine.plan(3, [25, 25, 25], [3, 2, 1])["kind"] == engine.KIND_STREAM
-    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
+    # unaligned fp32 rows under 64 elements: the row-tile kernel; aligned ones the row kernel
+    assert engine.plan(3, [25, 25, 25], [3, 2, 1])["kind"] == engine.KIND_ROW_TILE
+    assert engine.plan(1, [63, 99], [1, 2])["kind"] == engine.KIND_ROW_TILE
+    assert engine.plan(1, [16, 99], [1, 2])["kind"] == engine.KIND_ROW
+    assert engine.plan(1, [65, 99], [1, 2])["kind"] == engine.KIND_ROW
+    assert engine.plan(3, [25, 25, 25], [3, 2, 1], kind=engine.KIND_STREAM)["kind"] == engine.KIND_STREAM
+    # fp64 rows of at most 64 elements: the row-tile kernel (native-DFMA mode keeps the row kernel)
+    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW_TILE
+    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64)["block"] == 128
+    assert engine.plan(1, [32, 9], [1, 2], dtype=engine.F64)["kind"] == engine.KIND_ROW_TILE
+    assert engine.plan(1, [33, 9], [1, 2], dtype=engine.F64)["kind"] == engine.KIND_ROW
+    # fp64 rows under 8 elements: native DFMA in the row-tile kernel unless the mix is asked for
+    pl = engine.plan(1, [5, 999], [1, 2], dtype=engine.F64)
+    assert pl["kind"] == engine.KIND_ROW_TILE and pl["accumulate"] == engine.ACC_PLAIN
+    assert engine.plan(1, [5, 999], [1, 2], dtype=engine.F64,
+                       accumulate=engine.ACC_DOUBLE_FLOAT)["accumulate"] == engine.ACC_COMPENSATED
+    assert engine.plan(1, [25, 25, 25], [1, 2, 3], dtype=engine.F64,
+                       accumulate=engine.ACC_PLAIN)["kind"] == engine.KIND_ROW
+    assert engine.plan(1, [16, 4096], [1, 2], kind=engine.KIND_ROW_TILE)["kind"] == engine.KIND_ROW_TILE
+    with pytest.raises(engine.TTVError):
+        engine.plan(1, [65, 9], [1, 2], kind=engine.KIND_ROW_TILE)
+    with pytest.raises(engine.TTVError):
+        engine.plan(2, [16, 9], [1, 2], kind=engine.KIND_ROW_TILE)
     assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
     # fp64 column kernel: the DFMA / double-float mix by default
     assert engine.plan(2, [64, 32, 16], [1, 2, 3], dtype=engine.F64)["accumulate"] == \

@@ -189,6 +189,13 @@ def test_variant_sweep(engine, orc, torch_dev, na, pia, q):
                         continue
                     check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
                           group=g, vec=v, split=split)
+        # the row-tile kernel, for short q-fastest rows
+        if P == 1 and nq <= 64:
+            accs = (engine.ACC_COMPENSATED, engine.ACC_PLAIN) if dt == np.float32 else \
+                (engine.ACC_COMPENSATED, engine.ACC_PLAIN, engine.ACC_DOUBLE_FLOAT)
+            for acc in accs:
+                check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
+                      kind=engine.KIND_ROW_TILE, accumulate=acc)
         # the TMA-streamed kernel, where whole rows fit a stage
         L = nq if P == 1 else P
         if L * np.dtype(dt).itemsize <= 16384 and (P == 1 or -(-P // 256) <= 8):
@@ -414,6 +421,8 @@ def test_fp64_emulation_window_and_fallback(engine, orc, torch_dev):
         P, nq, S = orc.canonical(na, pia, q)
         truth = orc.truth(S, nq, P, a, b)
         kinds = (-1, engine.KIND_ROW) if P == 1 else (-1, engine.KIND_COL, engine.KIND_COL_REALIGN)
+        if P == 1 and nq <= 64:
+            kinds += (engine.KIND_ROW_TILE,)
         for kind in kinds:
             check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, kind=kind,
                   accumulate=engine.ACC_DOUBLE_FLOAT)
@@ -492,6 +501,55 @@ def test_short_rows(engine, orc, torch_dev):
                     for acc in accs:
                         check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth,
                               kind=engine.KIND_ROW, group=g, vec=v, accumulate=acc)
+
+
+def test_row_tile_kernel(engine, orc, torch_dev):
+    """Short q-fastest rows through the row-tile kernel: every n_q up to 64 (odd
+    and even, so both column walks), row counts below, at and around one
+    32-row tile and across many tiles, A at element offsets 0-3 (ragged bulk
+    copies), fp32 (compensated and plain), fp64 (mix, native, double-float)
+    and bf16-stored A; fp64 rows of at most 32 elements take it by default."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(55)
+    for nq in (1, 2, 3, 5, 8, 15, 16, 17, 24, 25, 31, 32, 33, 48, 63, 64):
+        for S in (1, 31, 32, 33, 1000 + nq, 4099):
+            na, pia, q = [nq, S], [1, 2], 1
+            N = nq * S
+            for dt in (np.float32, np.float64):
+                tdt = torch.float32 if dt == np.float32 else torch.float64
+                a = rng.uniform(-1, 1, N + 3).astype(dt)
+                b = rng.uniform(-1, 1, nq).astype(dt)
+                da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+                dc = torch.empty(S, dtype=tdt, device=dev)
+                accs = (engine.ACC_COMPENSATED, engine.ACC_PLAIN) if dt == np.float32 else \
+                    (engine.ACC_COMPENSATED, engine.ACC_PLAIN, engine.ACC_DOUBLE_FLOAT)
+                for oa in ((0, 1, 2, 3) if S >= 1000 else (0, 3)):
+                    truth = orc.truth(S, nq, 1, a[oa:oa + N], b)
+                    for acc in accs:
+                        dc.fill_(float("nan"))
+                        engine.ttv(q, 2, da[oa:oa + N], na, [1, nq], pia, db, [nq], dc, [S], [1], [1],
+                                   kind=engine.KIND_ROW_TILE, accumulate=acc, sync=True)
+                        err = orc.rel_error(dc.cpu().numpy(), *truth)
+                        assert err <= TOL[dt], (nq, S, dt, oa, acc, err)
+        pl = engine.plan(1, [nq, 4099], [1, 2], dtype=engine.F64)
+        assert pl["kind"] == (engine.KIND_ROW_TILE if nq <= 32 else engine.KIND_ROW), pl
+    # bf16-stored A
+    for nq, S in ((25, 3001), (16, 64), (64, 33)):
+        a32 = rng.uniform(-1, 1, nq * S).astype(np.float32)
+        b = rng.uniform(-1, 1, nq).astype(np.float32)
+        abf = torch.from_numpy(a32).to(torch.bfloat16)
+        bits = abf.view(torch.int16).numpy().view(np.uint16).copy()
+        dc = torch.empty(S, dtype=torch.float32, device=dev)
+        engine.ttv(1, 2, abf.to(dev).view(torch.int16), [nq, S], [1, nq], [1, 2],
+                   torch.from_numpy(b).to(dev), [nq], dc, [S], [1], [1],
+                   dtype=engine.BF16A, kind=engine.KIND_ROW_TILE, sync=True)
+        refb, absnb = orc.truth(S, nq, 1, bits, b, kind="bf16a")
+        assert orc.rel_error(dc.cpu().numpy(), refb, absnb) <= 1e-5
+    # refused where it does not apply
+    with pytest.raises(engine.TTVError):
+        engine.ttv(1, 2, torch.zeros(65 * 4, device=dev), [65, 4], [1, 65], [1, 2],
+                   torch.zeros(65, device=dev), [65], torch.zeros(4, device=dev), [4], [1], [1],
+                   kind=engine.KIND_ROW_TILE)
 
 
 THIN_SHAPES = [

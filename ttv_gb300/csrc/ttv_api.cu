@@ -387,6 +387,27 @@ int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tl
     return make_plan_inner(dtype, cn, a, b, opt, sms, out);
 }
 
+// Row-tile kernel: tiles of 32 R rows (R rows per lane), a static round robin
+// of tiles over the warps of a grid of resident CTAs.
+int make_row_tile_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
+{
+    if (opt && opt->split > 1)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-tile kernel does not split the contracted mode");
+    pl.kind = KIND_ROW_TILE;
+    pl.group = 1;
+    pl.vec = 1;
+    pl.split = 1;
+    pl.seg_len = cn.nq;
+    pl.items = cn.S;
+    pl.rows_m = rowt_rows_per_lane(cn.nq, elem_size_a(pl.dtype));
+    const int cps = std::max(1, plan_ctas_per_sm(pl));
+    const uint64_t tiles = cdiv(cn.S, 32 * (uint64_t)pl.rows_m);
+    pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * cps, cdiv(tiles, ROWT_WARPS)));
+    pl.smem = plan_smem_bytes(pl);
+    *out = pl;
+    return TLIBG_OK;
+}
+
 int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
                     int sms, Plan* out)
 {
@@ -415,22 +436,36 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
                                         "fp32 or fp64 A");
     if (opt && opt->kind == KIND_COL_THIN && cn.P == 1)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: the thin-prefix column kernel needs prefix P > 1");
+    const bool row_tile_ok = cn.P == 1 && cn.nq <= (uint64_t)ROWT_MAX_NQ;
+    if (opt && opt->kind == KIND_ROW_TILE && !row_tile_ok)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-tile kernel needs prefix P == 1 and n_q <= 64");
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
-        opt->kind != KIND_COL_THIN && opt->kind != pl.kind)
+        opt->kind != KIND_COL_THIN && opt->kind != KIND_ROW_TILE && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
                                         "(row kernel needs prefix P == 1, column kernel P > 1)");
-    // default for q-fastest rows: the register row kernel, except unaligned fp32 / bf16
-    // rows shorter than 64 elements, which the streamed kernel (alignment-agnostic)
-    // takes (measured on GB300: rows of 25 floats 4.3 vs 3.8 TB/s; rows of 645 floats
-    // 4.2 vs 5.8 TB/s the other way round).
-    // The streamed column form stays available on request.
+    // Default for q-fastest rows: the register row kernel, except the short rows below.
+    // The streamed kernel (row and column forms) stays available on request.
     bool rows_aligned = false;
     {
         const size_t vb = 16 / ea;
         rows_aligned = cn.nq % vb == 0 && aligned(a, 16) && aligned(b, 16);
     }
-    const bool stream_default = eligible && cn.P == 1 && !rows_aligned && dtype != F64 && cn.nq < 64;
-    if ((opt && opt->kind == KIND_STREAM) || (stream_default && !(opt && opt->kind >= 0))) {
+    // Short q-fastest rows take the row-tile kernel (measured on GB300 against the
+    // register row kernel and the streamed kernel): fp64 rows of at most 32 elements
+    // with the double-float mix (rows of 16 / 25: 5.2-5.4 vs 4.0-4.1 TB/s; from 40
+    // elements on the row kernel's lane pairs win), and fp32 / bf16 rows under 64
+    // elements that are not 16-byte aligned (rows of 25: 5.5 vs 4.2 TB/s streamed).
+    // fp64 rows under 8 elements accumulate with native DFMA only there: the mix's
+    // per-row fold costs more than it saves (rows of 3: 4.6 vs 3.2 TB/s).
+    const bool no_split = !(opt && opt->split > 1);
+    const bool row_tile_default =
+        row_tile_ok && no_split &&
+        ((dtype == F64 && pl.kahan && cn.nq <= 32) || (dtype != F64 && !rows_aligned && cn.nq < 64));
+    if ((opt && opt->kind == KIND_ROW_TILE) || (row_tile_default && !(opt && opt->kind >= 0))) {
+        if (dtype == F64 && cn.nq < 8 && !(opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT)) pl.kahan = 0;
+        return make_row_tile_plan(pl, cn, opt, sms, out);
+    }
+    if (opt && opt->kind == KIND_STREAM) {
         if (dtype == F64) pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
         return make_stream_plan(pl, cn, opt, sms, out);
     }
@@ -820,7 +855,7 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
     out->split = pl.split;
     out->accumulate = pl.kahan ? TLIBG_ACC_COMPENSATED : TLIBG_ACC_PLAIN;
     out->grid = pl.grid;
-    out->block = BLOCK;
+    out->block = pl.kind == KIND_STREAM ? STREAM_CONSUMERS + 32 : (pl.kind == KIND_ROW_TILE ? ROWT_THREADS : BLOCK);
     return ok();
 }
 
@@ -909,8 +944,8 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
 
     // Page-locked A: the kernels read it in place over the host link (one pass,
     // no staging copy; on GB300 a kernel reading page-locked memory moves it as
-    // fast as the copy engines do).  The streamed kernel's bulk copies are kept
-    // to device memory: the register kernels take q-fastest rows instead.
+    // fast as the copy engines do).  The bulk copies of the streamed and row-tile
+    // kernels are kept to device memory: the register kernels take those rows.
     cudaPointerAttributes at{};
     const bool a_pinned = cudaPointerGetAttributes(&at, a) == cudaSuccess && at.type == cudaMemoryTypeHost &&
                           at.devicePointer != nullptr;
@@ -920,10 +955,10 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
             return cuda_fail(e, "copy of b");
         tlibg_options o2{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, 0};
         if (opt) o2 = *opt;
-        if (o2.kind == KIND_STREAM) o2.kind = -1;
+        if (o2.kind == KIND_STREAM || o2.kind == KIND_ROW_TILE) o2.kind = -1;
         Plan pl;
         if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &pl))) return st;
-        if (pl.kind == KIND_STREAM) {
+        if (pl.kind == KIND_STREAM || pl.kind == KIND_ROW_TILE) {
             o2.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
             if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &pl))) return st;
         }

@@ -160,6 +160,23 @@ __device__ __forceinline__ DSplit split_double(double x)
 // branch into a predicated DFMA that would take an FP64 issue slot for every
 // in-window product as well.
 static __device__ __noinline__ double dfma_out_of_window(double a, double b, double d) { return fma(a, b, d); }
+static __device__ __noinline__ double f2d_convert(float x) { return (double)x; }
+
+// float -> double without the conversion instruction (it issues at the FP64
+// pipe's rate here): for a normal float the double's high word is the
+// float's magnitude bits shifted right by 3 plus the exponent rebias
+// (1023 - 127) << 20, with the sign kept; the low word holds the last 3
+// significand bits.  Zeros are built directly; subnormal and non-finite
+// floats take the conversion through a real call (never predicated in).
+__device__ __forceinline__ double f2d(float x)
+{
+    const uint32_t u = __float_as_uint(x);
+    const uint32_t m = u & 0x7fffffffu;
+    if (m - 0x00800000u < 0x7f000000u)
+        return __hiloint2double((int)(((m >> 3) + (896u << 20)) | (u & 0x80000000u)), (int)(u << 29));
+    if (m == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return f2d_convert(x);
+}
 
 struct AccDF {
     double s, c;    // folded value (after fold()); c stays 0
@@ -202,7 +219,7 @@ struct AccDF {
     __device__ __forceinline__ void fold()
     {
         renorm();
-        s = ((double)hi + (double)lo) + d;
+        s = (f2d(hi) + f2d(lo)) + d;
         c = 0.0;
     }
     __device__ __forceinline__ void merge(double os, double) { s = s + os; }

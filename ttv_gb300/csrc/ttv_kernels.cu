@@ -626,6 +626,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 #include "ttv_realign.cuh"
 #include "ttv_thin.cuh"
 #include "ttv_strided.cuh"
+#include "ttv_rowtile.cuh"
 
 namespace tlibg {
 
@@ -651,6 +652,14 @@ template <typename TA, typename T, bool KAHAN>
 static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
+    if (kind == KIND_ROW_TILE) {
+        switch (rows_m) {
+        case 1: return row_tile_kernel<TA, T, KAHAN, 1>;
+        case 2: return row_tile_kernel<TA, T, KAHAN, 2>;
+        case 4: return row_tile_kernel<TA, T, KAHAN, 4>;
+        }
+        return nullptr;
+    }
     if (kind == KIND_COL && vec == 1 && mo == 2) return col_strided_kernel<TA, T, 2, KAHAN>;
     if (kind == KIND_COL && vec == 1 && mo == 4) return col_strided_kernel<TA, T, 4, KAHAN>;
     if (kind == KIND_COL_REALIGN) {
@@ -740,6 +749,11 @@ size_t plan_smem_bytes(const Plan& p)
         if (!p.stream_col) extra = std::max(extra, (size_t)p.L * es);
         return 128 + (size_t)STREAM_NS * STREAM_SLOT + extra;
     }
+    if (p.kind == KIND_ROW_TILE) {
+        const size_t ea = p.dtype == F64 ? 8 : (p.dtype == BF16A ? 2 : 4);
+        return 128 + rowt_b_bytes(p.nq, acc_size(p.dtype)) + rowt_split_bytes(p.nq, p.dtype == F64 && p.kahan) +
+               (size_t)ROWT_WARPS * ROWT_NS * rowt_slot_bytes(p.nq, ea, p.rows_m);
+    }
     if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements
         return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.group > 1 && p.nq <= (uint64_t)ROW_SPLIT_MAX)
                    ? ROW_SPLIT_MAX * 8 : 0;
@@ -776,7 +790,7 @@ int plan_ctas_per_sm(const Plan& p)
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-    const int threads = p.kind == KIND_STREAM ? STREAM_THREADS : BLOCK;
+    const int threads = p.kind == KIND_STREAM ? STREAM_THREADS : (p.kind == KIND_ROW_TILE ? ROWT_THREADS : BLOCK);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(fn), threads, smem) !=
         cudaSuccess) {
         cudaGetLastError();
@@ -846,7 +860,9 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     k.pdiv = make_idx_div(plan.P, plan.S * plan.P);
     k.tdiv = make_idx_div(k.ntiles, plan.items);
     const size_t smem = plan_smem_bytes(plan);
-    fn<<<plan.grid, BLOCK, smem, stream>>>(k);
+    if (plan.kind == KIND_ROW_TILE && smem > 48 * 1024)
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fn<<<plan.grid, plan.kind == KIND_ROW_TILE ? ROWT_THREADS : BLOCK, smem, stream>>>(k);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (launches) ++*launches;

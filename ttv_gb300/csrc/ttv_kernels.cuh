@@ -7,12 +7,29 @@
 namespace tlibg {
 
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
-enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4 };
+enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4, KIND_ROW_TILE = 5 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
 constexpr int STREAM_STAGE_BYTES = 16384;   // streamed kernel: bytes of A per shared-memory stage
 constexpr int STREAM_CONSUMERS = 256;       // streamed kernel: consumer threads per CTA
+// row-tile kernel: warps per CTA, shared-memory stages per warp, longest row
+constexpr int ROWT_WARPS = 4;
+constexpr int ROWT_THREADS = ROWT_WARPS * 32;
+constexpr int ROWT_NS = 2;
+constexpr int ROWT_MAX_NQ = 64;
+// Bytes of one row-tile stage: 32 R rows of n_q elements of A plus up to 15
+// bytes of misalignment, rounded to 16.
+__host__ __device__ inline size_t rowt_slot_bytes(uint64_t nq, size_t ea, int R)
+{
+    return (size_t)((32 * (uint64_t)R * nq * ea + 16 + 15) & ~uint64_t(15));
+}
+// Rows per lane of a row tile: enough that a tile holds about 4 KB of A.
+inline int rowt_rows_per_lane(uint64_t nq, size_t ea)
+{
+    const uint64_t b = 32 * nq * ea;
+    return b >= 4096 ? 1 : (2 * b >= 4096 ? 2 : 4);
+}
 
 // One planned launch of a canonical problem C[s, j] = sum_i A[s, i, j] b[i],
 // A dense (S, nq, P) row-major, C dense (S, P).
@@ -23,7 +40,8 @@ struct Plan {
     int vec = 1;          // elements per vector load (COL_REALIGN: 16 bytes, realigned by shuffles)
     int split = 1;        // segments of the contracted mode
     int kahan = 1;        // compensated fp32 accumulation
-    int rows_m = 0;       // ROW: 1 or 2 = short-row kernel (at most rows_m vectors per lane of a row)
+    int rows_m = 0;       // ROW: 1 or 2 = short-row kernel (at most rows_m vectors per lane of a row);
+                          // ROW_TILE: rows per lane (1, 2 or 4)
     int mo = 1;           // COL with scalar loads: outputs per thread, 32 apart (strided kernel when > 1)
     uint64_t P = 1, nq = 1, S = 1;
     uint64_t seg_len = 1;

@@ -21,7 +21,7 @@ import sys
 
 import numpy as np
 
-from . import F32, F64, KIND_COL, KIND_COL_REALIGN, KIND_ROW, KIND_STREAM, ACC_DOUBLE_FLOAT, \
+from . import F32, F64, KIND_COL, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_TILE, KIND_STREAM, ACC_DOUBLE_FLOAT, \
     _options, library, output_layout, output_shape, plan, strides, ttv
 
 L2_FLUSH_BYTES = 256 << 20
@@ -39,6 +39,9 @@ def candidates(dtype, P, nq, S):
         if nq * es <= 16384:
             for g in (0, 2, 4, 8, 16, 32):
                 out.append({"kind": KIND_STREAM, "group": g})
+        if nq <= 64:
+            for acc in accs:
+                out.append({"kind": KIND_ROW_TILE, "accumulate": acc})
     else:
         min_split = -(-nq // (16384 // es))
         kinds = (KIND_COL, KIND_COL_REALIGN) if P % (16 // es) else (KIND_COL,)
