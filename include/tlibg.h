@@ -45,12 +45,13 @@ extern "C" {
 
 /* ---- accumulation ---- */
 #define TLIBG_ACC_COMPENSATED  0  /* default.  fp32: per-thread Kahan partials.  fp64: register   */
-                                  /*   kernels mix native DFMA (half the products) with double-  */
-                                  /*   float accumulation on the FP32/INT32 pipes; the streamed   */
-                                  /*   kernel uses DFMA                                            */
+                                  /*   and row-tile kernels mix native DFMA (half the products)  */
+                                  /*   with double-float accumulation on the FP32/INT32 pipes;    */
+                                  /*   the streamed kernel, and the row-tile kernel on rows under */
+                                  /*   8 elements, use DFMA                                        */
 #define TLIBG_ACC_PLAIN        1  /* fp32: plain FMA accumulation; fp64: native DFMA only          */
-#define TLIBG_ACC_DOUBLE_FLOAT 2  /* fp64: the mix in the register kernels, double-float for every */
-                                  /*   in-window product in the streamed kernel                    */
+#define TLIBG_ACC_DOUBLE_FLOAT 2  /* fp64: the mix everywhere (double-float for every in-window   */
+                                  /*   product in the streamed kernel)                             */
 
 /* ---- kernel families chosen by the planner ---- */
 #define TLIBG_KIND_ROW 0   /* q is the fastest layout mode (prefix P == 1): lane-group dot products */
@@ -60,8 +61,8 @@ extern "C" {
                                    /*   for prefixes whose rows are not 16-byte aligned (fp32/fp64) */
 #define TLIBG_KIND_COL_THIN 4      /* column GEMV for thin prefixes (P / vector width divides 32):  */
                                    /*   several rows per warp step, for few outputs and long q      */
-#define TLIBG_KIND_ROW_TILE 5      /* short rows (P == 1, n_q <= 64, no split): tiles of 32 rows    */
-                                   /*   moved to shared memory by TMA, one lane per row, any        */
+#define TLIBG_KIND_ROW_TILE 5      /* short rows (P == 1, n_q <= 64, no split): tiles of 32-128     */
+                                   /*   rows moved to shared memory by TMA, 1-4 rows per lane, any  */
                                    /*   alignment                                                   */
 
 typedef struct tlibg_options {
