@@ -383,8 +383,10 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
             if (k.nseg == 1) {
                 row = item;
             } else {
-                row = item / k.nseg;
-                seg = item - row * k.nseg;
+                // segment-major: the rows' pieces of one b segment are taken up
+                // together, so b (as long as a row) is read from HBM about once
+                seg = item / k.S;
+                row = item - seg * k.S;
             }
             const uint64_t ib = seg * k.seg_len;
             const uint64_t ie = min(k.nq, ib + k.seg_len);
