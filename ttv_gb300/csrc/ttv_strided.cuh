@@ -32,7 +32,8 @@ template <typename TA> __device__ __forceinline__ constexpr int strided_loads()
 
 // 8-byte elements load through L1 with default caching: the sector a warp's
 // unaligned run shares with the next run is then an L1 hit (fp64 +4 % over
-// streaming loads on the symmetric sweep; fp32 unchanged, so it streams).
+// streaming loads on the symmetric sweep; fp32 the same with streaming, L1 or
+// L2-only loads, so it streams).
 template <typename TA> __device__ __forceinline__ constexpr bool strided_l1() { return sizeof(TA) == 8; }
 
 // UB rows of the contracted mode: MO loads per row, all loads first.  rp[m]
