@@ -605,11 +605,16 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         // (more only when q is too short to split), then split q until about two
         // items per CTA.
         const uint64_t grid_full = (uint64_t)sms * cps;
-        if (force_group <= 0 && tiles_for(1) < grid_full) {
+        // tiles that keep the HBM system busy: a full grid, or 4 CTAs per SM for the
+        // narrow-load kernels that fit more (fp32 strided: 6 per SM; rows of 645 with
+        // 813 tiles, one warp row and no split: 168-180 us against 191-205 us)
+        uint64_t fill = std::min<uint64_t>(grid_full, (uint64_t)sms * 4);
+        if (force_group <= 0 && tiles_for(1) < fill) {
             WI = 2;
             while (WI < 8 && cn.nq < 64 && tiles_for(WI) < grid_full && cn.nq >= (uint64_t)WI * 2 * 4) WI *= 2;
             pl.group = WI;
             cps = std::max(1, plan_ctas_per_sm(pl));
+            fill = std::min<uint64_t>((uint64_t)sms * cps, (uint64_t)sms * 4);
         }
         const uint64_t want = 2 * (uint64_t)sms * cps;
         const uint64_t tiles = tiles_for(WI);
@@ -618,7 +623,7 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
             nseg = std::max<uint64_t>(nseg, (uint64_t)force_split);
             if ((uint64_t)force_split < cdiv(cn.nq, bmax))
                 return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced split leaves a segment longer than the staged b buffer");
-        } else if (tiles < (uint64_t)sms * cps && tiles * nseg < want) {
+        } else if (tiles < fill && tiles * nseg < want) {
             const uint64_t min_len = (uint64_t)WI * 4 * 4;
             nseg = std::max<uint64_t>(nseg, std::min<uint64_t>(cdiv(want, tiles), std::max<uint64_t>(1, cn.nq / min_len)));
         }
