@@ -50,8 +50,12 @@ template <typename TA, int V> __host__ __device__ constexpr int min_ctas()
     return (int)sizeof(TA) * V >= 16 ? 4 : 1;
 }
 
+// Narrow loads: 64 bytes in flight (at most 16 loads).  Measured on GB300 over
+// the symmetric sweep: rows of 645 doubles (fp64 scalar loads, 8 in flight)
+// 5.70 TB/s against 5.31 with 128 bytes (16 loads: 111 registers, 2 CTAs per
+// SM) and 4.73 with 96; fp32 scalar loads keep 16 either way.
 #ifndef TLIBG_NARROW_INFLIGHT
-#define TLIBG_NARROW_INFLIGHT 128
+#define TLIBG_NARROW_INFLIGHT 64
 #endif
 template <typename TA, int V> __host__ __device__ constexpr int loads_in_flight()
 {
