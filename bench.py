@@ -243,10 +243,11 @@ def run_ours(args, rank, world, local_rank):
         pl = T.plan(q, na, pia, dtype=T.F32 if dt == "f32" else T.F64)
         fam = {T.KIND_ROW: "row_kernel", T.KIND_COL: "col_kernel",
                T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel",
-               T.KIND_COL_THIN: "col_thin_kernel", T.KIND_ROW_TILE: "row_tile_kernel"}[pl["kind"]]
+               T.KIND_COL_THIN: "col_thin_kernel", T.KIND_ROW_TILE: "row_tile_kernel",
+               T.KIND_COL_BULK: "col_bulk_kernel"}[pl["kind"]]
         if pl["kind"] == T.KIND_COL and pl["vec"] == 1:
             fam = "col_strided_kernel"   # scalar loads, two outputs per thread
-        kname = fam + f"<{dt}" + ("" if pl["kind"] in (T.KIND_STREAM, T.KIND_ROW_TILE) else f",V{pl['vec']}") + \
+        kname = fam + f"<{dt}" + ("" if pl["kind"] in (T.KIND_STREAM, T.KIND_ROW_TILE, T.KIND_COL_BULK) else f",V{pl['vec']}") + \
             (",kahan" if pl["accumulate"] == T.ACC_COMPENSATED and dt != "f64" else "") + ">"
         prepared.append((fn, argv, keep, case_bytes(c), kname, c))
 

@@ -64,6 +64,8 @@ extern "C" {
 #define TLIBG_KIND_ROW_TILE 5      /* short rows (P == 1, n_q <= 64, no split): tiles of 32-128     */
                                    /*   rows moved to shared memory by TMA, 1-4 rows per lane, any  */
                                    /*   alignment                                                   */
+#define TLIBG_KIND_COL_BULK 6      /* column GEMV (P > 1) fed by a TMA producer warp: 4 KB runs of  */
+                                   /*   each row in a 3-stage shared-memory ring, any alignment     */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */

@@ -163,6 +163,13 @@ def test_planner_kernel_family(engine):
         engine.plan(1, [65, 9], [1, 2], kind=engine.KIND_ROW_TILE)
     with pytest.raises(engine.TTVError):
         engine.plan(2, [16, 9], [1, 2], kind=engine.KIND_ROW_TILE)
+    # the TMA-staged column kernel: on request for any prefix P > 1, 288 threads
+    pl = engine.plan(2, [645, 33, 7], [1, 2, 3], kind=engine.KIND_COL_BULK)
+    assert pl["kind"] == engine.KIND_COL_BULK and pl["block"] == 288 and pl["vec"] == 4
+    assert engine.plan(2, [645, 33, 7], [1, 2, 3], dtype=engine.F64, kind=engine.KIND_COL_BULK)["vec"] == 2
+    assert engine.plan(2, [645, 33, 7], [1, 2, 3])["kind"] == engine.KIND_COL
+    with pytest.raises(engine.TTVError):
+        engine.plan(1, [16, 9], [1, 2], kind=engine.KIND_COL_BULK)
     assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
     # fp64 column kernel: the DFMA / double-float mix by default
     assert engine.plan(2, [64, 32, 16], [1, 2, 3], dtype=engine.F64)["accumulate"] == \

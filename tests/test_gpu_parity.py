@@ -552,6 +552,56 @@ def test_row_tile_kernel(engine, orc, torch_dev):
                    kind=engine.KIND_ROW_TILE)
 
 
+BULK_SHAPES = [
+    ([1024, 33, 7], [1, 2, 3], 2),       # P = 1024: one full tile per slice (fp32)
+    ([1001, 9, 5], [1, 2, 3], 2),        # odd P, partial tile, short contraction
+    ([2, 3, 1023, 5], [1, 2, 3, 4], 4),  # P = 6138 = 2 (mod 4): partial last tile
+    ([645, 33, 7], [1, 2, 3], 2),        # P = 645: one partial tile per slice
+    ([129, 5000, 2], [1, 2, 3], 2),      # long contraction: several b segments
+    ([5, 3, 700], [3, 1, 2], 2),         # layout permuted: P = 3500, n_q = 3
+    ([4097, 6], [1, 2], 2),              # S = 1, P one past a multiple of the tile
+]
+
+
+@pytest.mark.parametrize("na,pia,q", BULK_SHAPES)
+def test_bulk_column_kernel(engine, orc, torch_dev, na, pia, q):
+    """The TMA-staged column kernel: rows of the prefix at every misalignment
+    (A at element offsets 0-3), full and partial tiles, splits of q, fp32
+    (compensated and plain), fp64 (mix and native) and bf16-stored A."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(sum(na) * 11 + q)
+    P, nq, S = orc.canonical(na, pia, q)
+    wa, nc, wc, pic = meta(engine, na, pia, q)
+    N, M = int(np.prod(na)), int(np.prod(nc))
+    for dt in (np.float32, np.float64):
+        tdt = torch.float32 if dt == np.float32 else torch.float64
+        a = rng.uniform(-1, 1, N + 3).astype(dt)
+        b = rng.uniform(-1, 1, nq).astype(dt)
+        da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+        dc = torch.empty(M, dtype=tdt, device=dev)
+        bmax = 16384 // np.dtype(dt).itemsize
+        accs = (engine.ACC_COMPENSATED, engine.ACC_PLAIN)
+        for oa in (0, 1, 2, 3):
+            truth = orc.truth(S, nq, P, a[oa:oa + N], b)
+            for split, acc in itertools.product((0, 1, 3, 17), accs):
+                if (0 < split < -(-nq // bmax)) or split > nq:
+                    continue
+                dc.fill_(float("nan"))
+                engine.ttv(q, len(na), da[oa:oa + N], na, wa, pia, db, [nq], dc, nc, wc, pic,
+                           kind=engine.KIND_COL_BULK, split=split, accumulate=acc, sync=True)
+                err = orc.rel_error(dc.cpu().numpy(), *truth)
+                assert err <= TOL[dt], (na, pia, q, dt, oa, split, acc, err)
+    a32 = rng.uniform(-1, 1, N).astype(np.float32)
+    b = rng.uniform(-1, 1, nq).astype(np.float32)
+    abf = torch.from_numpy(a32).to(torch.bfloat16)
+    bits = abf.view(torch.int16).numpy().view(np.uint16).copy()
+    dc = torch.empty(M, dtype=torch.float32, device=dev)
+    engine.ttv(q, len(na), abf.to(dev).view(torch.int16), na, wa, pia, torch.from_numpy(b).to(dev), [nq],
+               dc, nc, wc, pic, dtype=engine.BF16A, kind=engine.KIND_COL_BULK, sync=True)
+    refb, absnb = orc.truth(S, nq, P, bits, b, kind="bf16a")
+    assert orc.rel_error(dc.cpu().numpy(), refb, absnb) <= 1e-5
+
+
 THIN_SHAPES = [
     ([64, 50000], [1, 2], 2),
     ([16, 30000, 3], [1, 2, 3], 2),

@@ -29,7 +29,7 @@ __all__ = [
     "output_shape", "output_layout", "strides", "k_order_layout", "inverse_mode",
     "library", "library_path", "launch_count", "device_error", "F32", "F64", "BF16A",
     "ACC_COMPENSATED", "ACC_PLAIN", "ACC_DOUBLE_FLOAT", "KIND_ROW", "KIND_COL", "KIND_STREAM",
-    "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE",
+    "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE", "KIND_COL_BULK",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -37,7 +37,8 @@ LIB_PATH = os.path.join(HERE, "libttvgpu.so")
 
 F32, F64, BF16A = 0, 1, 2
 ACC_COMPENSATED, ACC_PLAIN, ACC_DOUBLE_FLOAT = 0, 1, 2
-KIND_ROW, KIND_COL, KIND_STREAM, KIND_COL_REALIGN, KIND_COL_THIN, KIND_ROW_TILE = 0, 1, 2, 3, 4, 5
+KIND_ROW, KIND_COL, KIND_STREAM, KIND_COL_REALIGN, KIND_COL_THIN, KIND_ROW_TILE, KIND_COL_BULK = \
+    0, 1, 2, 3, 4, 5, 6
 OK, ERR_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = range(6)
 
 

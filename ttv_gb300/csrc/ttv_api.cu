@@ -387,6 +387,43 @@ int make_plan(int dtype, const Canon& cn, const void* a, const void* b, const tl
     return make_plan_inner(dtype, cn, a, b, opt, sms, out);
 }
 
+// TMA-staged column kernel: items (segment, slice, tile of 4 KB of a row), a
+// contiguous block of items per CTA; q is split only to fill the grid.
+int make_col_bulk_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
+{
+    pl.kind = KIND_COL_BULK;
+    pl.group = 1;
+    pl.vec = (int)(col_bulk_tile(pl.dtype) / BLOCK);
+    const uint64_t ntiles = cdiv(cn.P, col_bulk_tile(pl.dtype));
+    const uint64_t tiles = cn.S * ntiles;
+    const uint64_t bmax = BSTAGE_BYTES / elem_size_t(pl.dtype);
+    const int cps = std::max(1, plan_ctas_per_sm(pl));
+    const uint64_t grid_full = (uint64_t)sms * cps;
+    const int force_split = opt ? opt->split : 0;
+    uint64_t nseg = cdiv(cn.nq, bmax);
+    if (force_split > 0) {
+        if ((uint64_t)force_split < nseg)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced split leaves a segment longer than the staged b buffer");
+        nseg = (uint64_t)force_split;
+    } else if (tiles < 2 * grid_full) {
+        nseg = std::max<uint64_t>(nseg, std::min<uint64_t>(cdiv(2 * grid_full, tiles),
+                                                           std::max<uint64_t>(1, cn.nq / (4 * CB_RB))));
+    }
+    nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
+    const uint64_t seg_len = cdiv(cn.nq, nseg);
+    nseg = cdiv(cn.nq, seg_len);
+    pl.split = (int)nseg;
+    pl.seg_len = seg_len;
+    pl.items = tiles * nseg;
+    const uint64_t grid = std::min<uint64_t>(grid_full, pl.items);
+    pl.items_per_cta = cdiv(pl.items, grid);
+    pl.grid = (int)cdiv(pl.items, pl.items_per_cta);
+    pl.f64_combine = (pl.dtype != F64) && pl.split > 1 && cn.nq > (uint64_t(1) << 20);
+    pl.smem = plan_smem_bytes(pl);
+    *out = pl;
+    return TLIBG_OK;
+}
+
 // Row-tile kernel: tiles of 32 R rows (R rows per lane), a static round robin
 // of tiles over the warps of a grid of resident CTAs.
 int make_row_tile_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
@@ -439,6 +476,9 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     const bool row_tile_ok = cn.P == 1 && cn.nq <= (uint64_t)ROWT_MAX_NQ;
     if (opt && opt->kind == KIND_ROW_TILE && !row_tile_ok)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-tile kernel needs prefix P == 1 and n_q <= 64");
+    if (opt && opt->kind == KIND_COL_BULK && cn.P == 1)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the TMA-staged column kernel needs prefix P > 1");
+    if (opt && opt->kind == KIND_COL_BULK) return make_col_bulk_plan(pl, cn, opt, sms, out);
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
         opt->kind != KIND_COL_THIN && opt->kind != KIND_ROW_TILE && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
@@ -860,7 +900,8 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
     out->split = pl.split;
     out->accumulate = pl.kahan ? TLIBG_ACC_COMPENSATED : TLIBG_ACC_PLAIN;
     out->grid = pl.grid;
-    out->block = pl.kind == KIND_STREAM ? STREAM_CONSUMERS + 32 : (pl.kind == KIND_ROW_TILE ? ROWT_THREADS : BLOCK);
+    out->block = pl.kind == KIND_STREAM ? STREAM_CONSUMERS + 32
+                 : (pl.kind == KIND_ROW_TILE ? ROWT_THREADS : (pl.kind == KIND_COL_BULK ? CB_THREADS : BLOCK));
     return ok();
 }
 
@@ -949,8 +990,9 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
 
     // Page-locked A: the kernels read it in place over the host link (one pass,
     // no staging copy; on GB300 a kernel reading page-locked memory moves it as
-    // fast as the copy engines do).  The bulk copies of the streamed and row-tile
-    // kernels are kept to device memory: the register kernels take those rows.
+    // fast as the copy engines do).  The bulk copies of the streamed, row-tile and
+    // TMA-staged column kernels are kept to device memory: the register kernels
+    // take those problems.
     cudaPointerAttributes at{};
     const bool a_pinned = cudaPointerGetAttributes(&at, a) == cudaSuccess && at.type == cudaMemoryTypeHost &&
                           at.devicePointer != nullptr;
@@ -960,10 +1002,10 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
             return cuda_fail(e, "copy of b");
         tlibg_options o2{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, 0};
         if (opt) o2 = *opt;
-        if (o2.kind == KIND_STREAM || o2.kind == KIND_ROW_TILE) o2.kind = -1;
+        if (o2.kind == KIND_STREAM || o2.kind == KIND_ROW_TILE || o2.kind == KIND_COL_BULK) o2.kind = -1;
         Plan pl;
         if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &pl))) return st;
-        if (pl.kind == KIND_STREAM || pl.kind == KIND_ROW_TILE) {
+        if (pl.kind == KIND_STREAM || pl.kind == KIND_ROW_TILE || pl.kind == KIND_COL_BULK) {
             o2.kind = cn.P == 1 ? KIND_ROW : KIND_COL;
             if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &pl))) return st;
         }

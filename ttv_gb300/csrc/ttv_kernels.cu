@@ -633,6 +633,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 #include "ttv_thin.cuh"
 #include "ttv_strided.cuh"
 #include "ttv_rowtile.cuh"
+#include "ttv_colbulk.cuh"
 
 namespace tlibg {
 
@@ -658,6 +659,7 @@ template <typename TA, typename T, bool KAHAN>
 static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
+    if (kind == KIND_COL_BULK) return col_bulk_kernel<TA, T, KAHAN>;
     if (kind == KIND_ROW_TILE) {
         switch (rows_m) {
         case 1: return row_tile_kernel<TA, T, KAHAN, 1>;
@@ -755,6 +757,7 @@ size_t plan_smem_bytes(const Plan& p)
         if (!p.stream_col) extra = std::max(extra, (size_t)p.L * es);
         return 128 + (size_t)STREAM_NS * STREAM_SLOT + extra;
     }
+    if (p.kind == KIND_COL_BULK) return 128 + (size_t)CB_NS * CB_STAGE_AL;
     if (p.kind == KIND_ROW_TILE) {
         const size_t ea = p.dtype == F64 ? 8 : (p.dtype == BF16A ? 2 : 4);
         return 128 + rowt_b_bytes(p.nq, acc_size(p.dtype)) + rowt_split_bytes(p.nq, p.dtype == F64 && p.kahan) +
@@ -796,7 +799,8 @@ int plan_ctas_per_sm(const Plan& p)
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-    const int threads = p.kind == KIND_STREAM ? STREAM_THREADS : (p.kind == KIND_ROW_TILE ? ROWT_THREADS : BLOCK);
+    const int threads = p.kind == KIND_STREAM ? STREAM_THREADS
+                        : (p.kind == KIND_ROW_TILE ? ROWT_THREADS : (p.kind == KIND_COL_BULK ? CB_THREADS : BLOCK));
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(fn), threads, smem) !=
         cudaSuccess) {
         cudaGetLastError();
@@ -857,18 +861,27 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     k.group = (uint32_t)plan.group;
     if (plan.kind == KIND_COL_THIN) {
         k.ntiles = plan.S;
+    } else if (plan.kind == KIND_COL_BULK) {
+        k.ntiles = (plan.P + col_bulk_tile(plan.dtype) - 1) / col_bulk_tile(plan.dtype);   // tiles per slice
     } else if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {
         const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec * plan.mo;
         k.ntiles = (plan.S * plan.P + TO - 1) / TO;
     } else {
         k.ntiles = 0;
     }
-    k.pdiv = make_idx_div(plan.P, plan.S * plan.P);
-    k.tdiv = make_idx_div(k.ntiles, plan.items);
+    if (plan.kind == KIND_COL_BULK) {
+        // item -> segment (S * ntiles items each), then -> slice (ntiles each)
+        k.tdiv = make_idx_div(plan.S * k.ntiles, plan.items);
+        k.pdiv = make_idx_div(k.ntiles, plan.S * k.ntiles);
+    } else {
+        k.pdiv = make_idx_div(plan.P, plan.S * plan.P);
+        k.tdiv = make_idx_div(k.ntiles, plan.items);
+    }
     const size_t smem = plan_smem_bytes(plan);
-    if (plan.kind == KIND_ROW_TILE && smem > 48 * 1024)
+    if ((plan.kind == KIND_ROW_TILE || plan.kind == KIND_COL_BULK) && smem > 48 * 1024)
         cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    fn<<<plan.grid, plan.kind == KIND_ROW_TILE ? ROWT_THREADS : BLOCK, smem, stream>>>(k);
+    const int threads = plan.kind == KIND_ROW_TILE ? ROWT_THREADS : (plan.kind == KIND_COL_BULK ? CB_THREADS : BLOCK);
+    fn<<<plan.grid, threads, smem, stream>>>(k);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     if (launches) ++*launches;

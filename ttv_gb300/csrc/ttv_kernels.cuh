@@ -7,12 +7,22 @@
 namespace tlibg {
 
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
-enum Kind { KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4, KIND_ROW_TILE = 5 };
+enum Kind {
+    KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4, KIND_ROW_TILE = 5,
+    KIND_COL_BULK = 6
+};
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
 constexpr int STREAM_STAGE_BYTES = 16384;   // streamed kernel: bytes of A per shared-memory stage
 constexpr int STREAM_CONSUMERS = 256;       // streamed kernel: consumer threads per CTA
+// TMA-staged column kernel: bytes of A per row of a tile (4 KB), a stage's row
+// slot (plus the cover's misalignment), rows per stage, stages, threads
+constexpr int CB_ROW_BYTES = 4096;
+constexpr int CB_ROWB = CB_ROW_BYTES + 16;
+constexpr int CB_RB = 8;
+constexpr int CB_NS = 3;
+constexpr int CB_THREADS = BLOCK + 32;   // 8 consumer warps and a producer warp
 // row-tile kernel: warps per CTA, shared-memory stages per warp, longest row
 constexpr int ROWT_WARPS = 4;
 constexpr int ROWT_THREADS = ROWT_WARPS * 32;
@@ -24,6 +34,8 @@ __host__ __device__ inline size_t rowt_slot_bytes(uint64_t nq, size_t ea, int R)
 {
     return (size_t)((32 * (uint64_t)R * nq * ea + 16 + 15) & ~uint64_t(15));
 }
+// Outputs per tile of the TMA-staged column kernel (4 KB of A per row).
+inline uint64_t col_bulk_tile(int dtype) { return (uint64_t)CB_ROW_BYTES / (dtype == F64 ? 8 : (dtype == BF16A ? 2 : 4)); }
 // Rows per lane of a row tile: enough that a tile holds about 4 KB of A.
 inline int rowt_rows_per_lane(uint64_t nq, size_t ea)
 {

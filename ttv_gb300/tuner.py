@@ -21,7 +21,8 @@ import sys
 
 import numpy as np
 
-from . import F32, F64, KIND_COL, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_TILE, KIND_STREAM, ACC_DOUBLE_FLOAT, \
+from . import F32, F64, KIND_COL, KIND_COL_BULK, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_TILE, KIND_STREAM, \
+    ACC_DOUBLE_FLOAT, \
     _options, library, output_layout, output_shape, plan, strides, ttv
 
 L2_FLUSH_BYTES = 256 << 20
@@ -54,6 +55,12 @@ def candidates(dtype, P, nq, S):
                         out.append({"kind": kind, "group": wi, "split": split, "accumulate": acc})
         if P * es <= 16384 and -(-P // 256) <= 8:
             out.append({"kind": KIND_STREAM})
+        if P * es >= 2048:
+            for split in (0, 1):
+                if split and split < min_split:
+                    continue
+                for acc in accs:
+                    out.append({"kind": KIND_COL_BULK, "split": split, "accumulate": acc})
     return out
 
 
