@@ -393,7 +393,7 @@ int make_col_bulk_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int s
 {
     pl.kind = KIND_COL_BULK;
     pl.group = 1;
-    pl.vec = (int)(col_bulk_tile(pl.dtype) / BLOCK);
+    pl.vec = (int)(col_bulk_tile(pl.dtype) / CB_CONSUMERS);
     const uint64_t ntiles = cdiv(cn.P, col_bulk_tile(pl.dtype));
     const uint64_t tiles = cn.S * ntiles;
     const uint64_t bmax = BSTAGE_BYTES / elem_size_t(pl.dtype);

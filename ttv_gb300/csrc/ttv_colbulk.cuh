@@ -3,18 +3,19 @@
 //
 // A work item is (segment of q, slice s, tile of CB_TJ = 4 KB of consecutive
 // outputs of the prefix); its rows i are the runs A[s, i, j0 .. j0 + TJ).
-// Warp 8 is the producer: for each block of CB_RB rows of the CTA's walk it
-// waits until the consumers have released the stage (empty mbarrier), writes
-// b[i] of the block's rows (and, for fp64, their double-float split) into the
-// stage, and issues one 1-D bulk copy (cp.async.bulk) per row of the 16-byte-
-// aligned cover of the row's run (at most 15 bytes on either side, inside the
-// same 16-byte chunks as the run's first and last element, so inside the
-// allocation) against the stage's full mbarrier.  Warps 0-7 consume: they
-// wait on the full barrier, read their elements of each row from shared
-// memory at the row's own misalignment, accumulate, and release the stage.
-// The ring of CB_NS stages, not registers, holds the bytes in flight.  Thread
-// t owns the outputs j0 + t + 256 v (v < V): each shared-memory read of a warp
-// is 32 consecutive elements and each store of C is coalesced.  Every wait is
+// The last warp is the producer: for each block of CB_RB rows of the CTA's
+// walk it waits until the consumers have released the stage (empty mbarrier),
+// writes b[i] of the block's rows (and, for fp64, their double-float split)
+// into the stage, and issues one 1-D bulk copy (cp.async.bulk) per row of the
+// 16-byte-aligned cover of the row's run (at most 15 bytes on either side,
+// inside the same 16-byte chunks as the run's first and last element, so
+// inside the allocation) against the stage's full mbarrier.  The CB_CONSUMERS
+// threads before it wait on the full barrier, read their elements of each row
+// from shared memory at the row's own misalignment, accumulate, and release
+// the stage.  The ring of CB_NS stages, not registers, holds the bytes in
+// flight.  Thread t owns the outputs j0 + t + CB_CONSUMERS v (v < V): each
+// shared-memory read of a warp is 32 consecutive elements and each store of C
+// is coalesced.  Every wait is
 // bounded; on expiry the CTA records the device error, waits (bounded) for its
 // own copies in flight and leaves.
 #pragma once
@@ -22,7 +23,6 @@
 namespace tlibg {
 
 template <typename TA> __host__ __device__ constexpr int cb_tj() { return CB_ROW_BYTES / (int)sizeof(TA); }
-constexpr int CB_CONSUMERS = BLOCK;                 // 8 consumer warps (+ the producer: CB_THREADS)
 // stage layout: CB_RB row slots, then b of those rows (8 bytes each), their
 // split (float2) and their in-window flags
 constexpr int CB_STAGE = CB_RB * CB_ROWB + CB_RB * 8 + CB_RB * 8 + CB_RB * 4;

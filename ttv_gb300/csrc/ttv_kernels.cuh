@@ -22,7 +22,8 @@ constexpr int CB_ROW_BYTES = 4096;
 constexpr int CB_ROWB = CB_ROW_BYTES + 16;
 constexpr int CB_RB = 8;
 constexpr int CB_NS = 3;
-constexpr int CB_THREADS = BLOCK + 32;   // 8 consumer warps and a producer warp
+constexpr int CB_CONSUMERS = BLOCK;                // consumer threads (512 measured slower)
+constexpr int CB_THREADS = CB_CONSUMERS + 32;      // and a producer warp
 // row-tile kernel: warps per CTA, shared-memory stages per warp, longest row
 constexpr int ROWT_WARPS = 4;
 constexpr int ROWT_THREADS = ROWT_WARPS * 32;
