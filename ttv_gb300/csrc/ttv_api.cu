@@ -1025,7 +1025,6 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
 
     if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess)
         return cuda_fail(e, "copy of b");
-    Plan pl_full;
     uint64_t launches = 0;
     for (uint64_t k = 0; k < nchunks; ++k) {
         const int slot = (int)(k & 1);
@@ -1048,7 +1047,6 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         e = launch_plan(pl, hc.abuf[slot], hc.bbuf, cdst, part, hc.comp, &launches);
         if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
         cudaEventRecord(hc.done[slot], hc.comp);
-        pl_full = pl;
     }
     g_launches += launches;
     if ((e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
@@ -1056,7 +1054,6 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     if ((e = cudaStreamSynchronize(hc.comp)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
     unsigned int derr = read_and_clear_device_error();
     if (derr) return fail(TLIBG_ERR_TIMEOUT, "tlibg: a bounded device wait expired; results are invalid");
-    (void)pl_full;
     return ok();
 }
 

@@ -66,7 +66,6 @@ struct BCtl {
 };
 
 constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
-constexpr int BCAP_F32 = BMAX_F32 + 4;
 
 // Lanes per row of the row-form variants: G = TLIBG_BATCH_ROW_G0 << g, g = 0..3.
 // Measured on GB300 (22,000 tuned shapes in mixed batches): one lane per row is

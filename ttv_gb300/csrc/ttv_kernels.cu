@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_short_kernel(K
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);
@@ -730,9 +730,10 @@ bool stream_eligible(int dtype, uint64_t P, uint64_t nq)
     return P * ea <= (uint64_t)STREAM_STAGE && (P + STREAM_NT - 1) / STREAM_NT <= (uint64_t)STREAM_MAXJ;
 }
 
+// The kernel of a plan that takes KArgs (every kind but the streamed one).
 static KernelFn main_kernel(const Plan& p)
 {
-    if (p.kind == KIND_STREAM) return reinterpret_cast<KernelFn>(stream_fn(p));
+    if (p.kind == KIND_STREAM) return nullptr;
     switch (p.dtype) {
     case F32:
         return p.kahan ? pick_main<float, float, true>(p.kind, p.vec, p.rows_m, p.mo)
@@ -782,11 +783,18 @@ size_t partial_bytes(const Plan& p)
     return (size_t)p.split * p.S * p.P * 2 * acc_size(p.dtype);
 }
 
+// Entry address of a plan's main kernel, for occupancy queries and attributes.
+static const void* kernel_entry(const Plan& p)
+{
+    if (p.kind == KIND_STREAM) return reinterpret_cast<const void*>(stream_fn(p));
+    return reinterpret_cast<const void*>(main_kernel(p));
+}
+
 int plan_ctas_per_sm(const Plan& p)
 {
     static std::mutex mu;
     static std::unordered_map<uint64_t, int> cache;
-    KernelFn fn = main_kernel(p);
+    const void* fn = kernel_entry(p);
     if (!fn) return 0;
     const size_t smem = plan_smem_bytes(p);
     const uint64_t key = (reinterpret_cast<uintptr_t>(fn) << 20) ^ smem;
@@ -797,11 +805,10 @@ int plan_ctas_per_sm(const Plan& p)
     }
     int n = 0;
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int threads = p.kind == KIND_STREAM ? STREAM_THREADS
                         : (p.kind == KIND_ROW_TILE ? ROWT_THREADS : (p.kind == KIND_COL_BULK ? CB_THREADS : BLOCK));
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, reinterpret_cast<const void*>(fn), threads, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) !=
         cudaSuccess) {
         cudaGetLastError();
         n = 0;
@@ -814,8 +821,6 @@ int plan_ctas_per_sm(const Plan& p)
 cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c, void* partial,
                         cudaStream_t stream, uint64_t* launches)
 {
-    KernelFn fn = main_kernel(plan);
-    if (!fn) return cudaErrorInvalidConfiguration;
     if (plan.kind == KIND_STREAM) {
         SArgs sa;
         sa.a = a;
@@ -846,6 +851,8 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
         if (plan.split > 1) return launch_combine(plan, partial, c, stream, launches);
         return cudaSuccess;
     }
+    KernelFn fn = main_kernel(plan);
+    if (!fn) return cudaErrorInvalidConfiguration;
     KArgs k;
     k.a = a;
     k.b = b;

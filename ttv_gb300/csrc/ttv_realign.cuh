@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
 {
     constexpr int V = 16 / (int)sizeof(T);
     constexpr int U = 4;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);

@@ -18,7 +18,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KA
 {
     constexpr int NW = BLOCK / 32;
     constexpr int U = loads_in_flight<TA, V>();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
     T* sb = reinterpret_cast<T*>(smem_raw + 16);
