@@ -71,42 +71,80 @@ __device__ __forceinline__ void rowt_step(AccT (&acc)[R], const TA* (&rp)[R], co
     }
 }
 
-// The lane's R rows (rp[r]) over all n_q columns, walking from column c and
-// wrapping.  fp64 with the double-float mix: the first step of every
-// TLIBG_ROWT_NATIVE_EVERY on the DFMA pipe, the rest emulated, renormalised
-// at least every 8 emulated products; the last n_q mod E steps native.
-template <int R, bool PRE, typename TA, typename T, typename AccT>
+// Next column of the walk: wrapping at n_q (rotated walks of even n_q), or
+// straight (odd n_q, which starts at column 0).
+template <bool WRAP> __device__ __forceinline__ uint32_t rowt_next(uint32_t c, uint32_t nq)
+{
+    if constexpr (WRAP) return (c + 1 == nq) ? 0u : c + 1;
+    return c + 1;
+}
+
+// The lane's R rows (rp[r]) over all n_q columns, walking from column c.
+// fp64 with the double-float mix: the first step of every
+// TLIBG_ROWT_NATIVE_EVERY on the DFMA pipe, the rest emulated, in blocks of
+// RT_G such groups with one renormalisation each (at most 8 emulated
+// products between two); the last n_q mod E steps native.
+constexpr int RT_G = 4;
+template <int R, bool PRE, bool WRAP, typename TA, typename T, typename AccT>
 __device__ __forceinline__ void rowt_dot(AccT (&acc)[R], const TA* (&rp)[R], const T* sb, const float2* bsp,
                                          uint32_t nq, uint32_t c)
 {
     if constexpr (std::is_same<AccT, AccDF>::value) {
         constexpr int E = TLIBG_ROWT_NATIVE_EVERY;
-        uint32_t j = 0, ne = 0;
-        for (; j + E <= nq; j += E) {
+        static_assert(RT_G * (E - 1) <= 8, "renormalise at least every 8 emulated products");
+        uint32_t j = 0;
+        for (; j + RT_G * E <= nq; j += RT_G * E) {
+#pragma unroll
+            for (int gq = 0; gq < RT_G; ++gq) {
+                rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
+                c = rowt_next<WRAP>(c, nq);
+#pragma unroll
+                for (int u = 1; u < E; ++u) {
+                    rowt_step<R, false, PRE>(acc, rp, sb, bsp, c);
+                    c = rowt_next<WRAP>(c, nq);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r].renorm();
+        }
+        for (; j + E <= nq; j += E) {   // fewer than RT_G groups left: fold() renormalises
             rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-            c = (c + 1 == nq) ? 0u : c + 1;
+            c = rowt_next<WRAP>(c, nq);
 #pragma unroll
             for (int u = 1; u < E; ++u) {
                 rowt_step<R, false, PRE>(acc, rp, sb, bsp, c);
-                c = (c + 1 == nq) ? 0u : c + 1;
-            }
-            ne += E - 1;
-            if (ne > (uint32_t)(8 - (E - 1))) {
-#pragma unroll
-                for (int r = 0; r < R; ++r) acc[r].renorm();
-                ne = 0;
+                c = rowt_next<WRAP>(c, nq);
             }
         }
         for (; j < nq; ++j) {
             rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-            c = (c + 1 == nq) ? 0u : c + 1;
+            c = rowt_next<WRAP>(c, nq);
         }
     } else {
-        for (uint32_t j = 0; j < nq; ++j) {
+        uint32_t j = 0;
+        for (; j + 8 <= nq; j += 8) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
+                c = rowt_next<WRAP>(c, nq);
+            }
+        }
+        for (; j < nq; ++j) {
             rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-            c = (c + 1 == nq) ? 0u : c + 1;
+            c = rowt_next<WRAP>(c, nq);
         }
     }
+}
+
+// Even n_q walks rotated (wrapping), odd n_q straight.
+template <int R, bool PRE, typename TA, typename T, typename AccT>
+__device__ __forceinline__ void rowt_dot_any(AccT (&acc)[R], const TA* (&rp)[R], const T* sb, const float2* bsp,
+                                             uint32_t nq, uint32_t c)
+{
+    if (nq & 1u)
+        rowt_dot<R, PRE, false>(acc, rp, sb, bsp, nq, 0u);
+    else
+        rowt_dot<R, PRE, true>(acc, rp, sb, bsp, nq, c);
 }
 
 template <typename TA, typename T, bool KAHAN, int R>
@@ -170,11 +208,11 @@ __global__ void __launch_bounds__(ROWT_THREADS) row_tile_kernel(KArgs k)
                 rp[r] = rows + (size_t)((r0 + lane + 32u * r < k.S) ? lane + 32u * r : lane) * nq;
             if constexpr (PRES) {
                 if (split_ok)
-                    rowt_dot<R, true>(acc, rp, sb, bsp, nq, rot);
+                    rowt_dot_any<R, true>(acc, rp, sb, bsp, nq, rot);
                 else
-                    rowt_dot<R, false>(acc, rp, sb, bsp, nq, rot);
+                    rowt_dot_any<R, false>(acc, rp, sb, bsp, nq, rot);
             } else {
-                rowt_dot<R, false>(acc, rp, sb, bsp, nq, rot);
+                rowt_dot_any<R, false>(acc, rp, sb, bsp, nq, rot);
             }
         }
 #pragma unroll
