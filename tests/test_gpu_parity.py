@@ -552,6 +552,27 @@ def test_row_tile_kernel(engine, orc, torch_dev):
                    kind=engine.KIND_ROW_TILE)
 
 
+def test_short_contraction_column_kernel(engine, orc, torch_dev):
+    """Column form with n_q <= 4 and vector loads: two tiles per thread, every row
+    loaded before any product; odd and even tile counts, one slice and many,
+    fp32 (compensated and plain) and fp64 (mix and native)."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(404)
+    for na, pia, q in (([64, 3, 1000], [1, 2, 3], 2), ([4096, 4], [1, 2], 2), ([8, 2, 33], [1, 2, 3], 2),
+                       ([1024, 4, 4, 4], [1, 2, 3, 4], 3), ([16, 1, 4100], [1, 2, 3], 2),
+                       ([2, 4, 4, 3, 5], [1, 2, 3, 4, 5], 4), ([100, 4, 7], [3, 2, 1], 1)):
+        P, nq, S = orc.canonical(na, pia, q)
+        for dt in (np.float32, np.float64):
+            a = rng.uniform(-1, 1, int(np.prod(na))).astype(dt)
+            b = rng.uniform(-1, 1, nq).astype(dt)
+            truth = orc.truth(S, nq, P, a, b)
+            accs = (engine.ACC_COMPENSATED, engine.ACC_PLAIN)
+            for acc in accs:
+                check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, accumulate=acc)
+                check(orc, engine, torch, dev, q, na, pia, a, b, truth=truth, accumulate=acc,
+                      kind=engine.KIND_COL, group=1, split=1)
+
+
 BULK_SHAPES = [
     ([1024, 33, 7], [1, 2, 3], 2),       # P = 1024: one full tile per slice (fp32)
     ([1001, 9, 5], [1, 2, 3], 2),        # odd P, partial tile, short contraction

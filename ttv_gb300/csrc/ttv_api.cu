@@ -632,6 +632,24 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
             *out = pl;
             return TLIBG_OK;
         }
+        // contractions of at most CS_MAXQ rows with vector loads: the short-contraction
+        // kernel (two tiles per thread, every row of both loaded before any product)
+        if (pl.kind == KIND_COL && V > 1 && dtype != BF16A && cn.nq <= (uint64_t)CS_MAXQ && force_group <= 1 &&
+            force_split <= 1) {
+            pl.rows_m = 1;
+            pl.group = 1;
+            pl.split = 1;
+            pl.seg_len = cn.nq;
+            const int cps = std::max(1, plan_ctas_per_sm(pl));
+            const uint64_t tiles = cdiv(cn.S * cn.P, (uint64_t)BLOCK * V);
+            pl.items = cdiv(tiles, 2);
+            const uint64_t grid = std::min<uint64_t>((uint64_t)sms * cps, pl.items);
+            pl.items_per_cta = cdiv(pl.items, grid);
+            pl.grid = (int)cdiv(pl.items, pl.items_per_cta);
+            pl.smem = plan_smem_bytes(pl);
+            *out = pl;
+            return TLIBG_OK;
+        }
         int WI = force_group > 0 ? force_group : 1;
         if (WI != 1 && WI != 2 && WI != 4 && WI != 8)
             return fail(TLIBG_ERR_ARGUMENT, "tlibg: warps along the contracted mode must be 1, 2, 4 or 8");

@@ -431,6 +431,86 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
     }
 }
 
+// Column form with a contraction of at most CS_MAXQ rows (no split, vector
+// loads): one round of the column kernel's tile loop would keep only n_q
+// loads in flight per thread, one HBM round trip per tile.  Here each thread
+// owns V consecutive outputs in each of two tiles TO apart and loads every row
+// of both before any product: 2 n_q vector loads in flight per thread.  b's
+// n_q values (and for fp64 their split) live in registers.
+template <typename TA, typename T, int V, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_short_kernel(KArgs k)
+{
+    constexpr bool PRES = presplit_b<T, KAHAN>();
+    const TA* __restrict__ A = static_cast<const TA*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    const uint32_t nq = (uint32_t)k.nq;
+    const uint64_t P = k.P;
+    const uint64_t outputs = k.S * P;
+    constexpr uint64_t TO = (uint64_t)BLOCK * V;
+    T bq[CS_MAXQ];
+    float2 bsp[CS_MAXQ];
+    bool split_ok = true;
+#pragma unroll
+    for (int i = 0; i < CS_MAXQ; ++i) {
+        bq[i] = (uint32_t)i < nq ? __ldg(B + i) : T(0);
+        if constexpr (PRES) {
+            const DSplit d = split_double((double)bq[i]);
+            bsp[i] = make_float2(d.hi, d.lo);
+            split_ok = split_ok && (d.ok || (uint32_t)i >= nq);
+        }
+    }
+    const uint64_t first = uint64_t(blockIdx.x) * k.items_per_cta;
+    const uint64_t last = min(k.items, first + k.items_per_cta);
+    for (uint64_t pair = first; pair < last; ++pair) {
+        T av[2][CS_MAXQ][V];
+        bool valid[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint64_t o = (2 * pair + h) * TO + (uint64_t)threadIdx.x * V;
+            valid[h] = o < outputs;
+            const uint64_t s = valid[h] ? idx_div(o, k.pdiv) : 0;
+            const TA* ap = A + (s * k.nq) * P + (o - s * P);
+#pragma unroll
+            for (int i = 0; i < CS_MAXQ; ++i) {
+                if (valid[h] && (uint32_t)i < nq) {
+                    load_a<TA, T, V>(ap + (uint64_t)i * P, av[h][i]);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v) av[h][i][v] = T(0);
+                }
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            typename AccSel<T, KAHAN>::type acc[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].init();
+#pragma unroll
+            for (int i = 0; i < CS_MAXQ; ++i) {
+                if ((uint32_t)i < nq) {
+                    if constexpr (PRES) {
+                        if (split_ok)
+                            row_fma<V, true>(acc, av[h][i], bq[i], i, &bsp[i]);
+                        else
+                            row_fma<V, false>(acc, av[h][i], bq[i], i, nullptr);
+                    } else {
+                        row_fma<V, false>(acc, av[h][i], bq[i], i, nullptr);
+                    }
+                }
+            }
+            renorm_all<V>(acc);
+            if (valid[h]) {
+                const uint64_t o = (2 * pair + h) * TO + (uint64_t)threadIdx.x * V;
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    acc[v].fold();
+                    static_cast<T*>(k.out)[o + v] = acc[v].value();
+                }
+            }
+        }
+    }
+}
+
 // Short rows as their own kernel (its registers do not weigh on the general
 // row kernel): M vectors per lane of each row, R = U / M rows in flight.
 template <typename TA, typename T, int V, bool KAHAN, int M>
@@ -668,6 +748,14 @@ static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
         }
         return nullptr;
     }
+    if (kind == KIND_COL && rows_m == 1 && vec > 1) {
+        switch (vec) {
+        case 2: return col_short_kernel<TA, T, 2, KAHAN>;
+        case 4: if constexpr (VMAX >= 4) return col_short_kernel<TA, T, 4, KAHAN>; else return nullptr;
+        case 8: if constexpr (VMAX >= 8) return col_short_kernel<TA, T, 8, KAHAN>; else return nullptr;
+        }
+        return nullptr;
+    }
     if (kind == KIND_COL && vec == 1 && mo == 2) return col_strided_kernel<TA, T, 2, KAHAN>;
     if (kind == KIND_COL && vec == 1 && mo == 4) return col_strided_kernel<TA, T, 4, KAHAN>;
     if (kind == KIND_COL_REALIGN) {
@@ -764,6 +852,7 @@ size_t plan_smem_bytes(const Plan& p)
         return 128 + rowt_b_bytes(p.nq, acc_size(p.dtype)) + rowt_split_bytes(p.nq, p.dtype == F64 && p.kahan) +
                (size_t)ROWT_WARPS * ROWT_NS * rowt_slot_bytes(p.nq, ea, p.rows_m);
     }
+    if (p.kind == KIND_COL && p.rows_m == 1) return 0;   // short contraction: b in registers
     if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements
         return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.group > 1 && p.nq <= (uint64_t)ROW_SPLIT_MAX)
                    ? ROW_SPLIT_MAX * 8 : 0;
@@ -870,6 +959,8 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
         k.ntiles = plan.S;
     } else if (plan.kind == KIND_COL_BULK) {
         k.ntiles = (plan.P + col_bulk_tile(plan.dtype) - 1) / col_bulk_tile(plan.dtype);   // tiles per slice
+    } else if (plan.kind == KIND_COL && plan.rows_m == 1) {
+        k.ntiles = 0;   // pairs of tiles of BLOCK * V outputs are the items
     } else if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {
         const uint64_t TO = uint64_t((BLOCK / 32) / plan.group) * 32u * plan.vec * plan.mo;
         k.ntiles = (plan.S * plan.P + TO - 1) / TO;

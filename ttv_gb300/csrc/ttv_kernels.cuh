@@ -16,6 +16,8 @@ constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
 constexpr int STREAM_STAGE_BYTES = 16384;   // streamed kernel: bytes of A per shared-memory stage
 constexpr int STREAM_CONSUMERS = 256;       // streamed kernel: consumer threads per CTA
+// Longest contraction of the short-contraction column kernel.
+constexpr int CS_MAXQ = 4;
 // TMA-staged column kernel: bytes of A per row of a tile (4 KB), a stage's row
 // slot (plus the cover's misalignment), rows per stage, stages, threads
 constexpr int CB_ROW_BYTES = 4096;
@@ -54,6 +56,7 @@ struct Plan {
     int split = 1;        // segments of the contracted mode
     int kahan = 1;        // compensated fp32 accumulation
     int rows_m = 0;       // ROW: 1 or 2 = short-row kernel (at most rows_m vectors per lane of a row);
+                          // COL: 1 = short-contraction kernel (n_q <= CS_MAXQ, two tiles per thread);
                           // ROW_TILE: rows per lane (1, 2 or 4)
     int mo = 1;           // COL with scalar loads: outputs per thread, 32 apart (strided kernel when > 1)
     uint64_t P = 1, nq = 1, S = 1;
