@@ -328,7 +328,8 @@ def test_full_size_properties(engine, torch_dev):
 
 
 def test_host_buffers(engine, orc, torch_dev):
-    """The host-pointer entry point (the reference's own calling convention)."""
+    """The host-pointer entry point (the reference's own calling convention): pinned A
+    is read in place, pinned C written in place, pageable buffers staged."""
     torch, dev = torch_dev
     rng = np.random.default_rng(4)
     # pinned A is read in place by the kernels (the streamed kernel's shapes, here
@@ -349,6 +350,13 @@ def test_host_buffers(engine, orc, torch_dev):
         tb = torch.from_numpy(b).pin_memory()
         tc = torch.zeros(int(np.prod(nc)), dtype=torch.float32).pin_memory()
         engine.ttv_host(q, len(na), ta, na, wa, pia, tb, [nq], tc, nc, wc, pic)
+        assert orc.rel_error(tc.numpy(), ref, absn) <= 1e-5
+        # pinned A (read in place) with pageable C (copied back) and vice versa
+        c2 = np.zeros(int(np.prod(nc)), np.float32)
+        engine.ttv_host(q, len(na), ta, na, wa, pia, b, [nq], c2, nc, wc, pic)
+        assert orc.rel_error(c2, ref, absn) <= 1e-5
+        tc.zero_()
+        engine.ttv_host(q, len(na), a, na, wa, pia, b, [nq], tc, nc, wc, pic)
         assert orc.rel_error(tc.numpy(), ref, absn) <= 1e-5
 
 

@@ -1018,6 +1018,13 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     if (a_pinned) {
         if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.comp)) != cudaSuccess)
             return cuda_fail(e, "copy of b");
+        // page-locked C too: the kernels store C in place over the link while they
+        // read A (the link carries both directions at once), no copy after them
+        cudaPointerAttributes atc{};
+        const bool c_pinned = cudaPointerGetAttributes(&atc, c) == cudaSuccess && atc.type == cudaMemoryTypeHost &&
+                              atc.devicePointer != nullptr;
+        cudaGetLastError();
+        void* cdst = c_pinned ? atc.devicePointer : hc.cbuf;
         tlibg_options o2{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, 0};
         if (opt) o2 = *opt;
         if (o2.kind == KIND_STREAM || o2.kind == KIND_ROW_TILE || o2.kind == KIND_COL_BULK) o2.kind = -1;
@@ -1030,10 +1037,10 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         void* part = nullptr;
         if ((st = get_scratch(hc.comp, partial_bytes(pl), &part))) return st;
         uint64_t launches = 0;
-        e = launch_plan(pl, at.devicePointer, hc.bbuf, hc.cbuf, part, hc.comp, &launches);
+        e = launch_plan(pl, at.devicePointer, hc.bbuf, cdst, part, hc.comp, &launches);
         g_launches += launches;
         if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
-        if ((e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
+        if (!c_pinned && (e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
             return cuda_fail(e, "copy of C");
         if ((e = cudaStreamSynchronize(hc.comp)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
         if (read_and_clear_device_error())
