@@ -53,7 +53,8 @@ template <typename TA, int V> __host__ __device__ constexpr int min_ctas()
 // Narrow loads: 64 bytes in flight (at most 16 loads).  Measured on GB300 over
 // the symmetric sweep: rows of 645 doubles (fp64 scalar loads, 8 in flight)
 // 5.70 TB/s against 5.31 with 128 bytes (16 loads: 111 registers, 2 CTAs per
-// SM) and 4.73 with 96; fp32 scalar loads keep 16 either way.
+// SM), 4.73 with 96 and 5.16 with 32; rows of 645 floats 5.72 with 64 or 128
+// bytes (16 loads either way), 5.25 with 32.
 #ifndef TLIBG_NARROW_INFLIGHT
 #define TLIBG_NARROW_INFLIGHT 64
 #endif
