@@ -564,9 +564,22 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
         if (force_split > 0) {
             nseg = (uint64_t)force_split;
         } else if (cn.S < 2 * slots) {
-            nseg = cdiv(2 * slots, cn.S);
+            // Lane groups take the (row, segment) items round-robin, so a launch lasts
+            // ceil(items / slots) rounds of one segment each.  Two rounds is the rule;
+            // another round count r in 1..4 (with the most segments that fill r rounds)
+            // replaces it when rounds x segment length drops by more than 2 %: 1024 rows
+            // of 2^18 floats at 32 lanes took 10 segments = 3 rounds, the third a tenth
+            // full (5.04 TB/s), where 9 fill two.
             const uint64_t min_len = (uint64_t)V * G * 4;
-            nseg = std::min<uint64_t>(nseg, std::max<uint64_t>(1, cn.nq / min_len));
+            const uint64_t max_seg = std::max<uint64_t>(1, cn.nq / min_len);
+            auto cost = [&](uint64_t ns) { return cdiv(cn.S * ns, slots) * cdiv(cn.nq, ns); };
+            uint64_t best = std::max<uint64_t>(1, std::min<uint64_t>(max_seg, (2 * slots) / cn.S));
+            const uint64_t base = cost(best);
+            for (uint64_t r = 1; r <= 4; ++r) {
+                const uint64_t ns = std::min<uint64_t>(max_seg, (r * slots) / cn.S);
+                if (ns >= 1 && (double)cost(ns) < 0.98 * (double)base && cost(ns) < cost(best)) best = ns;
+            }
+            nseg = best;
         }
         nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
         uint64_t seg_len = cdiv(cn.nq, nseg);
