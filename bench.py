@@ -1,7 +1,7 @@
 """Benchmark of the GB300 TTV engine (one JSON line on stdout).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sym|asym]
+                    [--workload sym|asym|precision|batch]
 
 Workload (default ``sym``): the symmetric sweep -- orders p = 2..7, every
 extent n = floor(2^(28/p)) (integer arithmetic: 16384, 645, 128, 48, 25, 16),
@@ -17,10 +17,13 @@ Inputs are seeded synthetic data (uniform[-1, 1]); A is larger than the
 Arms:
   ours       the engine, device-resident inputs (value) and end to end
              through the host-pointer entry point with pinned host buffers
-             (e2e); roofline of the dominant kernel; the CPU oracle port
-             timed on a bounded sample (cpu_baseline)
-  reference  the reference's algorithm for this path (par_loop / subtensor /
-             all) restated in C with OpenMP (oracle port), on all host cores
+             (e2e); roofline of the dominant kernel; accuracy against the
+             oracle's fp64 truth (fp32 and fp64); the asymmetric sweep,
+             the precision configuration and the batched configuration as
+             sub-objects; the reference on the host cores (cpu_baseline)
+  reference  the reference's own par_loop / subtensor / all path on the
+             host cores, compiled from its headers with OpenBLAS
+             (oracle/_ref/libttvref_blas.so), on the same TTVs
 """
 from __future__ import annotations
 
@@ -176,20 +179,6 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def traffic_per_element(kernel):
-    """DRAM bytes per A element of a kernel from a committed ncu summary, or None.
-    profiles/dram_traffic.txt lines: kernel=<label> elements=<N> dram_bytes=<B>"""
-    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
-    try:
-        for ln in open(path):
-            kv = dict(x.split("=", 1) for x in ln.split() if "=" in x)
-            if kv.get("kernel") == kernel:
-                return float(kv["dram_bytes"]) / float(kv["elements"])
-    except (OSError, ValueError, KeyError):
-        pass
-    return None
-
-
 def aggregate(ms_total, bytes_step, steps, world, dist=None, device=None):
     """Max of the timed region over ranks, and the whole-job throughput: every
     rank processed bytes_step per step (replicas, no data-path collective)."""
@@ -205,30 +194,38 @@ def aggregate(ms_total, bytes_step, steps, world, dist=None, device=None):
 # --------------------------------------------------------------------------
 # the engine arm
 # --------------------------------------------------------------------------
-def run_ours(args, rank, world, local_rank):
-    import torch
-    import ttv_gb300 as T
+def kernel_label(T, c):
+    """Kernel family and template of the plan a case runs (for the breakdown)."""
+    dt = c["dtype"]
+    pl = T.plan(c["q"], c["na"], c["pia"], dtype=T.F32 if dt == "f32" else T.F64)
+    fam = {T.KIND_ROW: "row_kernel", T.KIND_COL: "col_kernel",
+           T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel",
+           T.KIND_COL_THIN: "col_thin_kernel", T.KIND_ROW_TILE: "row_tile_kernel",
+           T.KIND_COL_BULK: "col_bulk_kernel"}[pl["kind"]]
+    if pl["kind"] == T.KIND_COL and pl["vec"] == 1:
+        fam = "col_strided_kernel"   # scalar loads, two outputs per thread
+    templ = "" if pl["kind"] in (T.KIND_STREAM, T.KIND_ROW_TILE, T.KIND_COL_BULK) else f",V{pl['vec']}"
+    acc = ",kahan" if pl["accumulate"] == T.ACC_COMPENSATED and dt != "f64" else ""
+    return f"{fam}<{dt}{templ}{acc}>" + ("+combine" if pl["split"] > 1 else "")
 
-    dev = torch.device("cuda", local_rank)
-    torch.cuda.set_device(dev)
-    cases = WORKLOADS[args.workload][0]()
+
+def prepare_sweep(T, torch, dev, cases, seed):
+    """Device inputs (one A, b and C per dtype, sized for the largest case) and
+    the C-ABI argument block of every case, built once."""
     dtypes = sorted({c["dtype"] for c in cases})
     maxN = max(int(np.prod(c["na"])) for c in cases)
     maxM = max(int(np.prod(c["na"])) // c["na"][c["q"] - 1] for c in cases)
     maxB = max(max(c["na"]) for c in cases)
     tdt = {"f32": torch.float32, "f64": torch.float64}
     g = torch.Generator(device=dev)
-    g.manual_seed(1234 + rank)
+    g.manual_seed(seed)
     A, Bv, Cv = {}, {}, {}
     for dt in dtypes:
         A[dt] = (torch.rand(maxN, generator=g, device=dev, dtype=tdt[dt]) * 2 - 1)
         Bv[dt] = (torch.rand(maxB, generator=g, device=dev, dtype=tdt[dt]) * 2 - 1)
         Cv[dt] = torch.empty(maxM, device=dev, dtype=tdt[dt])
     lib = T.library()
-    stream = torch.cuda.current_stream(dev)
-    sh = stream.cuda_stream
-
-    # per-case argument blocks, built once
+    sh = torch.cuda.current_stream(dev).cuda_stream
     prepared = []
     for c in cases:
         na, pia, q = c["na"], c["pia"], c["q"]
@@ -240,26 +237,47 @@ def run_ours(args, rank, world, local_rank):
         fn = lib.tlibg_ttv_f32 if dt == "f32" else lib.tlibg_ttv_f64
         argv = (q, len(na), A[dt].data_ptr(), *[T._p(k) for k in keep[:3]], Bv[dt].data_ptr(),
                 T._p(keep[3]), Cv[dt].data_ptr(), *[T._p(k) for k in keep[4:]], sh)
-        pl = T.plan(q, na, pia, dtype=T.F32 if dt == "f32" else T.F64)
-        fam = {T.KIND_ROW: "row_kernel", T.KIND_COL: "col_kernel",
-               T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel",
-               T.KIND_COL_THIN: "col_thin_kernel", T.KIND_ROW_TILE: "row_tile_kernel",
-               T.KIND_COL_BULK: "col_bulk_kernel"}[pl["kind"]]
-        if pl["kind"] == T.KIND_COL and pl["vec"] == 1:
-            fam = "col_strided_kernel"   # scalar loads, two outputs per thread
-        kname = fam + f"<{dt}" + ("" if pl["kind"] in (T.KIND_STREAM, T.KIND_ROW_TILE, T.KIND_COL_BULK) else f",V{pl['vec']}") + \
-            (",kahan" if pl["accumulate"] == T.ACC_COMPENSATED and dt != "f64" else "") + ">"
-        prepared.append((fn, argv, keep, case_bytes(c), kname, c))
+        prepared.append((fn, argv, keep, case_bytes(c), kernel_label(T, c), c))
+    return {"A": A, "B": Bv, "C": Cv, "prepared": prepared, "dtypes": dtypes}
 
-    def one_pass(evs=None):
-        for i, (fn, argv, _keep, _b, _k, _c) in enumerate(prepared):
-            if evs is not None:
-                evs[i][0].record(stream)
-            st = fn(*argv)
-            if st:
-                raise RuntimeError(f"ttv failed: {T._last_error()}")
-            if evs is not None:
-                evs[i][1].record(stream)
+
+def one_pass(T, prepared, stream, evs=None):
+    for i, (fn, argv, _keep, _b, _k, _c) in enumerate(prepared):
+        if evs is not None:
+            evs[i][0].record(stream)
+        st = fn(*argv)
+        if st:
+            raise RuntimeError(f"ttv failed: {T._last_error()}")
+        if evs is not None:
+            evs[i][1].record(stream)
+
+
+def kernel_breakdown(prepared, per_case_ms, peak):
+    per_kernel = {}
+    for i, (_fn, _a, _kp, nb, kname, c) in enumerate(prepared):
+        d = per_kernel.setdefault(kname, {"ms": 0.0, "bytes": 0, "launches": 0, "elements": 0})
+        d["ms"] += per_case_ms[i]
+        d["bytes"] += nb
+        d["launches"] += 1
+        d["elements"] += int(np.prod(c["na"]))
+    tot = sum(x["ms"] for x in per_kernel.values())
+    breakdown = {k: {"GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1),
+                     "frac": round(v["bytes"] / (v["ms"] / 1e3) / 1e9 / peak, 3),
+                     "share": round(v["ms"] / tot, 3), "cases": v["launches"]}
+                 for k, v in per_kernel.items()}
+    return per_kernel, breakdown
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import ttv_gb300 as T
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    cases = WORKLOADS[args.workload][0]()
+    sw = prepare_sweep(T, torch, dev, cases, 1234 + rank)
+    A, Bv, Cv, prepared, dtypes = sw["A"], sw["B"], sw["C"], sw["prepared"], sw["dtypes"]
+    stream = torch.cuda.current_stream(dev)
 
     dist = None
     if world > 1:
@@ -270,7 +288,7 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
 
     for _ in range(args.warmup):
-        one_pass()
+        one_pass(T, prepared, stream)
     torch.cuda.synchronize()
     if T.device_error() != 0:
         raise RuntimeError("device error word set during warm-up")
@@ -285,7 +303,7 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         t0.record(stream)
         for k in range(K):
-            one_pass(evs[k])
+            one_pass(T, prepared, stream, evs[k])
         t1.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -295,33 +313,23 @@ def run_ours(args, rank, world, local_rank):
     ms_step = ms_total / K
 
     # per-kernel breakdown from the per-case events (same timed region)
-    per_kernel = {}
     per_case_ms = [0.0] * len(prepared)
     for k in range(K):
         for i, (e0, e1) in enumerate(evs[k]):
             per_case_ms[i] += e0.elapsed_time(e1) / K
-    for i, (_fn, _a, _kp, nb, kname, c) in enumerate(prepared):
-        d = per_kernel.setdefault(kname, {"ms": 0.0, "bytes": 0, "launches": 0, "elements": 0})
-        d["ms"] += per_case_ms[i]
-        d["bytes"] += nb
-        d["launches"] += 1
-        d["elements"] += int(np.prod(c["na"]))
+    peak, peak_kind = measured_peak()
+    per_kernel, breakdown = kernel_breakdown(prepared, per_case_ms, peak)
     dom = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
     dk = per_kernel[dom]
-    peak, peak_kind = measured_peak()
     achieved = dk["bytes"] / dk["launches"] / (dk["ms"] / dk["launches"] / 1e3) / 1e9
-    tpe = traffic_per_element(dom)
+    tr = traffic_per_launch(dom, dk["elements"] / dk["launches"])
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
                 "measured" else "fallback 6.8 TB/s", "unit": "GB/s",
                 "frac": round(achieved / peak, 4),
-                "traffic": (round(tpe * dk["elements"] / dk["launches"])
-                            if tpe is not None else None),
+                "traffic": tr[0] if tr else None,
+                "traffic_source": tr[1] if tr else None,
                 "algorithmic_bytes_per_launch": round(dk["bytes"] / dk["launches"])}
-    breakdown = {k: {"GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1),
-                     "frac": round(v["bytes"] / (v["ms"] / 1e3) / 1e9 / peak, 3),
-                     "share": round(v["ms"] / sum(x["ms"] for x in per_kernel.values()), 3),
-                     "cases": v["launches"]} for k, v in per_kernel.items()}
     per_dtype = {}
     for i, (_fn, _a, _kp, nb, _kn, c) in enumerate(prepared):
         d = per_dtype.setdefault(c["dtype"], [0, 0.0])
@@ -357,20 +365,99 @@ def run_ours(args, rank, world, local_rank):
                                        dtype=T.F32 if c["dtype"] == "f32" else T.F64)}
                        for i, (_f, _a, _k, nb, kn, c) in enumerate(prepared)], f, indent=0)
     if rank == 0:
-        out["accuracy"] = accuracy_sample(T, torch, dev, A, Bv, Cv, prepared)
+        out["accuracy"] = accuracy_sample(T, torch, sw)
         if not args.no_e2e:
-            out["e2e"] = run_e2e(T, torch, prepared, A, Bv, dtypes, args)
+            out["e2e"] = run_e2e(T, torch, sw, args)
         if not args.no_cpu and world == 1:
-            out["cpu_baseline"] = run_cpu_baseline(prepared, args)
-        if not args.no_batch and args.workload != "case":
-            A.clear()
-            Bv.clear()
-            Cv.clear()
+            out["cpu_baseline"] = run_cpu_baseline(cases, args)
+        A.clear()
+        Bv.clear()
+        Cv.clear()
+        sw.clear()
+        torch.cuda.empty_cache()
+        if args.workload == "sym" and not args.no_sub:
+            out["asym"] = run_sweep_sub(T, torch, dev, "asym", args)
             torch.cuda.empty_cache()
+            out["precision"] = run_precision_sub(T, torch, dev, args)
+            torch.cuda.empty_cache()
+        if not args.no_batch and args.workload != "case":
             out["batched"] = run_batched(T, torch, dev, args, n=args.batch_problems)
     return out
 
 
+def run_sweep_sub(T, torch, dev, workload, args):
+    """Another sweep as a sub-object of the line: GB/s over the sweep, the
+    fraction of the measured peak, per-kernel shares and the oracle error on
+    one case per order."""
+    cases = WORKLOADS[workload][0]()
+    sw = prepare_sweep(T, torch, dev, cases, 4321)
+    prepared = sw["prepared"]
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        one_pass(T, prepared, stream)
+    torch.cuda.synchronize()
+    K = max(3, min(args.steps, 10))
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in prepared] for _ in range(K)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(K):
+        one_pass(T, prepared, stream, evs[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if T.device_error() != 0:
+        raise RuntimeError(f"device error word set during the {workload} sweep")
+    bytes_step = sum(p[3] for p in prepared)
+    ms = t0.elapsed_time(t1) / K
+    per_case_ms = [sum(evs[k][i][0].elapsed_time(evs[k][i][1]) for k in range(K)) / K
+                   for i in range(len(prepared))]
+    peak, _ = measured_peak()
+    _per_kernel, breakdown = kernel_breakdown(prepared, per_case_ms, peak)
+    gbs = bytes_step / (ms / 1e3) / 1e9
+    worst = sorted(((nb / (per_case_ms[i] / 1e3) / 1e9, c) for i, (_f, _a, _k, nb, _n, c)
+                    in enumerate(prepared)), key=lambda t: t[0])[:3]
+    q1 = {}
+    for i, (_f, _a, _k, nb, _n, c) in enumerate(prepared):
+        if c["q"] == 1 and len(c["na"]) <= 4:
+            q1["x".join(str(n) for n in c["na"])] = round(nb / (per_case_ms[i] / 1e3) / 1e9, 1)
+    acc = accuracy_sample(T, torch, sw, per_order=True)
+    res = {"workload": WORKLOADS[workload][1], "ttvs": len(prepared), "bytes_per_pass": bytes_step,
+           "ms_per_pass": round(ms, 3), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4),
+           "passes": K, "kernels": breakdown, "q1_long_rows_GBps": q1,
+           "slowest_cases": [{"GB/s": round(v, 1), "na": c["na"], "q": c["q"]} for v, c in worst],
+           "accuracy": acc}
+    sw.clear()
+    return res
+
+
+def run_precision_sub(T, torch, dev, args):
+    """The precision configuration as a sub-object (see run_precision)."""
+    full = run_precision(args)
+    return {"workload": full["config"]["workload"], "variants_GBps": full["variants_GBps"],
+            "frac_compensated": full["roofline"]["frac"], "errors": full["precision"],
+            "bars": full["bars"]}
+
+
+def traffic_per_launch(kernel, elements):
+    """DRAM bytes of one launch of a kernel from a committed ncu summary, or None.
+    profiles/dram_traffic.txt lines: kernel=<label> elements=<N> dram_bytes=<B>
+    [note=...]; a capture of the exact case (same element count) is taken as is,
+    another case is scaled by the elements of A."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    best = None
+    try:
+        for ln in open(path):
+            kv = dict(x.split("=", 1) for x in ln.split() if "=" in x)
+            if kv.get("kernel") != kernel.split("+")[0]:
+                continue
+            n, byts = float(kv["elements"]), float(kv["dram_bytes"])
+            if abs(n - elements) < 0.5:
+                return round(byts), f"ncu capture of a sweep launch ({int(n)} elements)"
+            best = (round(byts / n * elements),
+                    f"ncu capture of {int(n)} elements scaled to {int(elements)}")
+    except (OSError, ValueError, KeyError):
+        pass
+    return best
 def run_batched(T, torch, dev, args, n=4096, seed=4096):
     """Batched configuration: 4096 uneven fp32 TTVs (orders 3-5, extents log-uniform in
     [8, 512], <= 2^22 elements each, random q and layout) per launch.  Learned-selected
@@ -392,6 +479,7 @@ def run_batched(T, torch, dev, args, n=4096, seed=4096):
            else "absent (learned mode falls back to the fixed rule)"}
     K = max(3, args.steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = measured_peak()
 
     def timed(fn):
         for _ in range(3):
@@ -410,12 +498,18 @@ def run_batched(T, torch, dev, args, n=4096, seed=4096):
             ms = timed(bt.launch)
             res[name] = {"ms": round(ms, 3), "TTVs/s": round(n / ms * 1e3, 1),
                          "GB/s": round(nbytes / ms / 1e6, 1),
+                         "frac": round(nbytes / ms / 1e6 / peak, 4),
                          "gpu_launches_per_batch": (T.launch_count() - l0) // (K + 3)}
+            if name == "learned":
+                res[name]["variants_used"] = {str(k): v for k, v in sorted(
+                    __import__("collections").Counter(bt.variants()).items())}
     ms = timed(lambda: B.ttv_percall(probs))
     res["plain_per_call"] = {"ms": round(ms, 3), "TTVs/s": round(n / ms * 1e3, 1),
                              "GB/s": round(nbytes / ms / 1e6, 1)}
     res["speedup_learned_vs_plain"] = round(res["plain_per_call"]["ms"] / res["learned"]["ms"], 3)
     res["speedup_learned_vs_fixed_rule"] = round(res["fixed_rule"]["ms"] / res["learned"]["ms"], 3)
+    res["l2"] = ("13.5 GB of A per launch, 100x L2: consecutive launches find no problem "
+                 "resident (no flush)")
     # accuracy of the learned launch on a sample of problems
     import oracle
     errs = []
@@ -434,8 +528,7 @@ def run_precision(args):
     import torch
     import oracle
     import ttv_gb300 as T
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
+    dev = torch.device("cuda", torch.cuda.current_device())
     rng = np.random.default_rng(5)
     problems = [([64, 1 << 22], [1, 2], 2), ([16, 1 << 20, 16], [1, 2, 3], 2)]
     res = {}
@@ -492,34 +585,81 @@ def run_precision(args):
             "bars": {"fp32": 1e-5, "bf16a": "2e-3 vs the fp32 A (rounding of A: 2^-8 per element)"}}
 
 
-def accuracy_sample(T, torch, dev, A, Bv, Cv, prepared):
-    """max rel error vs the oracle's fp64 truth on one case per order (fp32)."""
-    import oracle
-    errs = []
-    seen = set()
-    for fn, argv, keep, nb, kname, c in prepared:
-        key = (len(c["na"]), c["dtype"])
-        if c["dtype"] != "f32" or key in seen:
+def accuracy_cases(prepared, per_order=False):
+    """Indices of the cases checked against the oracle: one per (order, dtype,
+    layout), q rotating with the order so every kernel family is visited
+    (per_order: one per order)."""
+    picked, seen = [], set()
+    for i, (_fn, _argv, _keep, _nb, _kname, c) in enumerate(prepared):
+        p = len(c["na"])
+        lay = 0 if c["pia"][0] == 1 else 1
+        key = (p,) if per_order else (p, c["dtype"], lay)
+        if per_order:   # even orders: q = 1 (the long rows), odd: the middle mode
+            want_q = 1 if p % 2 == 0 else p // 2 + 1
+        else:           # first, last and middle modes over the orders and layouts
+            want_q = (2 * (p - 2) + lay) % p + 1
+        if key in seen or c["q"] != want_q:
             continue
         seen.add(key)
+        picked.append(i)
+    return picked
+
+
+def accuracy_sample(T, torch, sw, per_order=False):
+    """max rel error vs the oracle's fp64 truth (fp32 and fp64 separately)."""
+    import oracle
+    prepared, A, Bv, Cv = sw["prepared"], sw["A"], sw["B"], sw["C"]
+    errs = {}
+    idx = accuracy_cases(prepared, per_order)
+    host = {dt: A[dt].cpu().numpy() for dt in A}
+    hostb = {dt: Bv[dt].cpu().numpy() for dt in Bv}
+    for i in idx:
+        fn, argv, keep, nb, kname, c = prepared[i]
+        Cv[c["dtype"]].fill_(float("nan"))
         st = fn(*argv)
-        assert st == 0
+        assert st == 0, T._last_error()
         torch.cuda.synchronize()
         P, nq, S = canonical(c)
         N = P * nq * S
-        a = A["f32"][:N].cpu().numpy()
-        b = Bv["f32"][:nq].cpu().numpy()
-        ref, absn = oracle.truth(S, nq, P, a, b)
-        errs.append(oracle.rel_error(Cv["f32"][:S * P].cpu().numpy(), ref, absn))
-    return {"max_rel_err_fp32": float(max(errs)) if errs else None,
-            "cases": len(errs), "metric": "max|c-ref|/sum|a*b| vs fp64 oracle"}
+        ref, absn = oracle.truth(S, nq, P, host[c["dtype"]][:N], hostb[c["dtype"]][:nq])
+        err = oracle.rel_error(Cv[c["dtype"]][:S * P].cpu().numpy(), ref, absn)
+        errs.setdefault(c["dtype"], []).append(err)
+    out = {f"max_rel_err_fp{dt[1:]}": float(max(v)) for dt, v in errs.items()}
+    out.update({"cases": len(idx), "cases_per_dtype": {dt: len(v) for dt, v in errs.items()},
+                "bars": {"fp32": 1e-5, "fp64": 1e-13},
+                "metric": "max|c-ref|/sum|a*b| vs the oracle's double-double truth"})
+    return out
 
 
-def run_e2e(T, torch, prepared, A, Bv, dtypes, args):
-    """Same sweep through the host-pointer C ABI entry point, pinned buffers."""
+def link_peak(torch, nbytes=1 << 30):
+    """Pinned host <-> device copy bandwidth of this machine (GB/s), one copy engine
+    per direction, best of 3."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, fn in (("h2d", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        best = None
+        for _ in range(3):
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = round(nbytes / best / 1e6, 1)
+    del h, d
+    return out
+
+
+def run_e2e(T, torch, sw, args):
+    """Same sweep through the host-pointer C ABI entry point, pinned buffers,
+    timed over --e2e-steps passes; the host link's own copy bandwidth beside it."""
     lib = T.library()
+    prepared, A, Bv = sw["prepared"], sw["A"], sw["B"]
     host = {}
-    for dt in dtypes:
+    for dt in sw["dtypes"]:
         host[dt] = (A[dt].cpu().pin_memory(), Bv[dt].cpu().pin_memory(),
                     torch.empty(max(int(np.prod(c["na"])) // c["na"][c["q"] - 1]
                                     for *_x, c in prepared), dtype=A[dt].dtype).pin_memory())
@@ -549,102 +689,165 @@ def run_e2e(T, torch, prepared, A, Bv, dtypes, args):
               for *_x, c in prepared)
     d2h = sum(esize(c["dtype"]) * (int(np.prod(c["na"])) // c["na"][c["q"] - 1])
               for *_x, c in prepared)
-    return {"value": round(nbytes * steps / dt_s / 1e9, 1), "unit": "GB/s",
+    host.clear()
+    link = link_peak(torch)
+    v = nbytes * steps / dt_s / 1e9
+    return {"value": round(v, 1), "unit": "GB/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
-            "api": "tlibg_ttv_host (host pointers, pinned)"}
+            "api": "tlibg_ttv_host (host pointers, pinned)",
+            "link_GBps": link, "frac_of_link_h2d": round(v / link["h2d"], 3)}
 
 
+# --------------------------------------------------------------------------
+# the reference on the host cores (cpu_baseline and the reference arm)
+# --------------------------------------------------------------------------
 def cpu_inputs(cases, seed=99):
     rng = np.random.default_rng(seed)
     maxN = max(int(np.prod(c["na"])) for c in cases)
     maxB = max(max(c["na"]) for c in cases)
+    maxM = max(int(np.prod(c["na"])) // c["na"][c["q"] - 1] for c in cases)
     data = {}
     for dt in sorted({c["dtype"] for c in cases}):
         npdt = np.float32 if dt == "f32" else np.float64
         a = rng.random(maxN, dtype=npdt)
         a *= 2
         a -= 1
-        data[dt] = (a, (rng.random(maxB, dtype=npdt) * 2 - 1).astype(npdt))
+        data[dt] = (a, (rng.random(maxB, dtype=npdt) * 2 - 1).astype(npdt),
+                    np.zeros(maxM, dtype=npdt))
     return data
 
 
-def run_cpu_sweep(cases, data, passes):
-    import oracle
-    t = time.perf_counter()
-    nbytes = 0
-    for _ in range(passes):
+def host_info():
+    info = {"nproc": os.cpu_count(), "omp_num_threads": os.environ.get("OMP_NUM_THREADS")}
+    try:
+        with open("/proc/cpuinfo") as f:
+            txt = f.read()
+        for key in ("model name", "CPU part", "CPU implementer"):
+            for ln in txt.splitlines():
+                if ln.startswith(key):
+                    info[key.replace(" ", "_")] = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for ln in r.stdout.splitlines():
+            k = ln.split(":", 1)[0].strip()
+            if k in ("Model name", "Socket(s)", "Core(s) per socket", "Thread(s) per core"):
+                info[k] = ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
+
+
+class CpuReference:
+    """The reference's par_loop / subtensor / all call on the host cores: its
+    OpenBLAS build (the configured path) where one was linked, else its plain
+    build, else the oracle's C restatement (only if neither exists)."""
+
+    def __init__(self):
+        import oracle
+        self.O = oracle
+        if not os.path.exists(oracle.LIB_PATH) or not (oracle.ref_available() or
+                                                       oracle.ref_blas_available()):
+            try:
+                oracle.build()
+            except (OSError, subprocess.CalledProcessError):
+                oracle.build(with_ref=False)
+        if oracle.ref_blas_available():
+            self.kind, self.blas = "reference", True
+            self.what = ("the reference's own par_loop/subtensor/all (its headers compiled by "
+                         "oracle/Makefile with -DUSE_OPENBLAS into oracle/_ref/libttvref_blas.so, "
+                         f"BLAS {oracle.blas_info()}), OpenMP + OpenBLAS threads on all host cores")
+        elif oracle.ref_available():
+            self.kind, self.blas = "reference", False
+            self.what = ("the reference's own par_loop/subtensor/all without BLAS (no OpenBLAS on "
+                         "this host: its cases 2-7 run its serial gemv loops), OpenMP on all host "
+                         "cores")
+        else:
+            self.kind, self.blas = "port", None
+            self.what = ("the reference's par_loop/subtensor/all algorithm restated in C "
+                         "(oracle/ttv_oracle.c orc_canon, a restructured port), OpenMP on all host "
+                         "cores; the reference headers are absent on this host")
+        self.cores = oracle.num_threads()
+
+    def calls(self, cases, data):
+        O = self.O
+        out = []
         for c in cases:
             P, nq, S = canonical(c)
-            a, b = data[c["dtype"]]
-            oracle.canon(S, nq, P, a[:P * nq * S], b[:nq])
-            nbytes += case_bytes(c)
-    return nbytes / (time.perf_counter() - t) / 1e9
+            a, b, cbuf = data[c["dtype"]]
+            na, pia, q = c["na"], c["pia"], c["q"]
+            nc, pic = O.output_shape(na, q), O.output_layout(pia, q)
+            out.append((c, P, nq, S, (q, a[:P * nq * S], na, O.strides(na, pia), pia, b[:nq], [nq],
+                                      nc, O.strides(nc, pic), pic, cbuf[:P * S])))
+        return out
+
+    def run(self, call):
+        c, P, nq, S, meta = call
+        q, av, na, wa, pia, bv, nb, nc, wc, pic, cv = meta
+        if self.blas is None:
+            cv[:] = self.O.canon(S, nq, P, av, bv)
+            return
+        st, msg, _ = self.O.ref_ttv("par_loop/subtensor/all", q, av, na, wa, pia, bv, nb, nc, wc,
+                                    pic, c=cv, blas=self.blas)
+        if st:
+            raise RuntimeError(msg)
+
+    def check(self, call):
+        """Error of one result against the oracle's truth (the timed build is correct)."""
+        c, P, nq, S, meta = call
+        self.run(call)
+        ref, absn = self.O.truth(S, nq, P, meta[1], meta[5])
+        return self.O.rel_error(meta[10], ref, absn)
 
 
-def run_cpu_baseline(prepared, args):
-    """The oracle port (reference algorithm, OpenMP) on a bounded sample."""
-    import oracle
-    cases = [x[5] for x in prepared]
-    sample = cases[::max(1, len(cases) // 36)]
-    data = cpu_inputs(sample)
-    v = run_cpu_sweep(sample, data, 1)
-    return {"value": round(v, 2), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"{len(sample)} of the {len(cases)} TTVs of the sweep (every "
-                      f"{max(1, len(cases) // 36)}th), one pass, oracle/ttv_oracle.c "
-                      "orc_canon (reference par_loop/subtensor/all loops, OpenMP)"}
+def run_cpu_pass(ref, calls):
+    t = time.perf_counter()
+    nbytes = 0
+    for call in calls:
+        ref.run(call)
+        nbytes += case_bytes(call[0])
+    return nbytes, time.perf_counter() - t
+
+
+def run_cpu_baseline(cases, args):
+    """The reference on the host cores, one pass over the same TTVs as the GPU step."""
+    ref = CpuReference()
+    data = cpu_inputs(cases)
+    calls = ref.calls(cases, data)
+    err = ref.check(calls[len(calls) // 2])
+    nbytes, el = run_cpu_pass(ref, calls)
+    return {"value": round(nbytes / el / 1e9, 2), "unit": "GB/s", "cores": ref.cores,
+            "kind": ref.kind, "sample": f"all {len(cases)} TTVs of the step, one pass: {ref.what}",
+            "s_per_pass": round(el, 3), "max_rel_err_checked_case": err, "host": host_info()}
 
 
 # --------------------------------------------------------------------------
 # the reference arm
 # --------------------------------------------------------------------------
 def run_reference(args):
-    import oracle
-    oracle.build(with_ref=False) if not os.path.exists(oracle.LIB_PATH) else None
     cases = WORKLOADS[args.workload][0]()
-    # bounded per-step sample of the workload: every 3rd TTV of the sweep
-    sample = cases[::3] if len(cases) > 6 else cases
-    data = cpu_inputs(sample)
-    for _ in range(args.warmup):
-        run_cpu_sweep(sample[:2], data, 1)
-    # the reference itself (compiled from its own headers by oracle/Makefile) where it
-    # exists on this host, else the C restatement of its algorithm
-    use_ref = False
-    try:
-        use_ref = oracle.ref_available() and oracle.ref() is not None
-    except OSError:
-        use_ref = False
-    calls = []
-    for c in sample:
-        P, nq, S = canonical(c)
-        a, b = data[c["dtype"]]
-        na, pia, q = c["na"], c["pia"], c["q"]
-        nc, pic = oracle.output_shape(na, q), oracle.output_layout(pia, q)
-        meta = (q, a[:P * nq * S], na, oracle.strides(na, pia), pia, b[:nq], [nq], nc,
-                oracle.strides(nc, pic), pic, np.zeros(P * S, dtype=a.dtype))
-        calls.append((c, P, nq, S, a, b, meta))
+    ref = CpuReference()
+    data = cpu_inputs(cases)
+    calls = ref.calls(cases, data)
+    err = ref.check(calls[len(calls) // 2])
+    # warm-up passes; a pass that would make the run take more than a few minutes
+    # is cut to a regular sample of the TTVs (every k-th), and the line says so
+    sample = calls
+    for w in range(max(1, args.warmup)):
+        nb, el = run_cpu_pass(ref, sample)
+        if w == 0 and el * (args.steps + args.warmup) > 240 and len(sample) > 6:
+            k = int(np.ceil(el * (args.steps + args.warmup) / 240))
+            sample = calls[::k]
     t = time.perf_counter()
     nbytes = 0
     for _ in range(args.steps):
-        for c, P, nq, S, a, b, meta in calls:
-            if use_ref:
-                q, av, na, wa, pia, bv, nb, nc, wc, pic, cv = meta
-                st, msg, _ = oracle.ref_ttv("par_loop/subtensor/all", q, av, na, wa, pia, bv, nb, nc,
-                                            wc, pic, c=cv)
-                if st:
-                    raise RuntimeError(msg)
-            else:
-                oracle.canon(S, nq, P, a[:P * nq * S], b[:nq])
-            nbytes += case_bytes(c)
+        nb, _el = run_cpu_pass(ref, sample)
+        nbytes += nb
     el = time.perf_counter() - t
     v = nbytes / el / 1e9
-    cores = oracle.num_threads()
-    if use_ref:
-        kind, what = "reference", ("the reference's own par_loop/subtensor/all (its headers compiled "
-                                   "by oracle/Makefile into oracle/_ref), OpenMP on all host cores")
-    else:
-        kind, what = "port", ("the reference's par_loop/subtensor/all algorithm restated in C "
-                              "(oracle/ttv_oracle.c orc_canon), OpenMP on all host cores; the "
-                              "reference itself is not built on this host (its sources are absent)")
+    same = len(sample) == len(calls)
     return {"metric": METRIC, "value": round(v, 2), "unit": "GB/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(el / args.steps * 1e3, 2), "higher_is_better": True,
@@ -652,9 +855,12 @@ def run_reference(args):
             "dtype": "f32+f64" if args.workload == "sym" else "f32", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": WORKLOADS[args.workload][1],
-                       "sample_per_step": f"{len(sample)} of {len(cases)} TTVs (every 3rd)"},
-            "cpu_baseline": {"value": round(v, 2), "unit": "GB/s", "cores": cores,
-                             "kind": kind, "sample": f"{len(sample)} TTVs per step: {what}"},
+                       "sample_per_step": (f"all {len(cases)} TTVs" if same else
+                                           f"{len(sample)} of {len(cases)} TTVs (regular sample)"),
+                       "same_ttvs_as_gpu_step": same},
+            "cpu_baseline": {"value": round(v, 2), "unit": "GB/s", "cores": ref.cores,
+                             "kind": ref.kind, "sample": f"{len(sample)} TTVs per step: {ref.what}",
+                             "max_rel_err_checked_case": err, "host": host_info()},
             "e2e": {"value": round(v, 2), "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
@@ -678,10 +884,12 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="sym")
     ap.add_argument("--batch-problems", type=int, default=4096,
                     help="problems per launch of the batched configuration")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="skip the asymmetric and precision sub-objects of the default line")
     ap.add_argument("--detail", default=None, help="write per-TTV timings and plans (JSON)")
     ap.add_argument("--case", default=None,
                     help="one TTV instead of a sweep, e.g. 'na=645,645,128 pia=1,2,3 q=2 "

@@ -193,12 +193,14 @@ size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode);
  * The split-n_q partial sums live in one fixed array of
  * TLIBG_NOALLOC_SCRATCH_BYTES compiled into the library, which every device
  * that loads the library holds until the process exits.  The call never
- * allocates or frees memory.
- *  - Problems whose split reduction needs more scratch than the array are
- *    refused with TLIBG_ERR_UNSUPPORTED and a message giving both sizes.
- *  - The first call on each device looks up the array's device address (once,
- *    with that device current); make that first call before any stream
- *    capture.
+ * allocates or frees memory (tlibg_device_alloc_count does not move).
+ *  - When the planner's split needs more scratch than the array, the call
+ *    plans again with fewer segments (the most that fit), then with none;
+ *    problems that fit neither way are refused with TLIBG_ERR_UNSUPPORTED and
+ *    a message giving both sizes.
+ *  - The first call on each device (and again after a new context, e.g. after
+ *    cudaDeviceReset) looks up the array's device address with that device
+ *    current; make that first call before any stream capture.
  *  - All calls share the one array: calls that overlap on the GPU (different
  *    streams, or host threads) race on it and must be serialised by the caller.
  *    Nothing in it needs to start at zero; each call writes every slot it reads.
@@ -311,6 +313,10 @@ size_t tlibg_last_error(char* buf, size_t len);
 int tlibg_device_error(void);
 /* Number of kernels this library launched since load (all entry points). */
 uint64_t tlibg_launch_count(void);
+/* Number of device allocations (cudaMalloc) this library made since load:
+ * split scratch, host-path staging buffers, batch descriptors, training
+ * buffers.  tlibg_ttv_f32_noalloc never adds to it. */
+uint64_t tlibg_device_alloc_count(void);
 /* Library version string. */
 const char* tlibg_version(void);
 

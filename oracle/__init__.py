@@ -4,13 +4,22 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
 and reference arm import this package.  It is the checker, never the product:
 the GPU engine in ``ttv_gb300`` neither imports nor links it.
 
-Two libraries sit behind this module:
+Three libraries sit behind this module:
 
 * ``liboracle.so`` -- ``ttv_oracle.c``, a plain-C restatement of the reference
   algorithm (bassoy/ttv ``include/tlib``), built on every host;
 * ``_ref/libttvref.so`` -- the reference itself compiled from its own headers
-  through ``ref_shim.cpp``; only built where the reference sources exist and
-  used to pin the restatement.
+  through ``ref_shim.cpp`` without BLAS (its plain loops); pins the
+  restatement bit for bit;
+* ``_ref/libttvref_blas.so`` -- the same headers with ``-DUSE_OPENBLAS``
+  against the OpenBLAS that NumPy's wheel ships (``cblas_shim/cblas.h`` maps
+  the standard CBLAS names onto its renamed symbols): the reference's
+  configured BLAS path, timed as the CPU baseline.
+
+The reference headers are compiled from ``baseline/_ref/include`` (git-ignored;
+``make -C oracle stage-ref`` copies them there from a reference checkout, and
+the copy travels with the repository to hosts without one), or from the
+directory named by ``TTV_REFERENCE_INCLUDE``.
 """
 from __future__ import annotations
 
@@ -23,7 +32,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libttvref.so")
-REF_INCLUDE = os.environ.get("TTV_REFERENCE_INCLUDE", "/root/reference/include")
+REF_BLAS_PATH = os.path.join(HERE, "_ref", "libttvref_blas.so")
+REF_BLAS_CFG = os.path.join(HERE, "_ref", "blas.cfg")
+REF_INCLUDE = os.environ.get("TTV_REFERENCE_INCLUDE",
+                             os.path.join(os.path.dirname(HERE), "baseline", "_ref", "include"))
 
 _sz = C.c_size_t
 _psz = C.POINTER(C.c_size_t)
@@ -40,13 +52,73 @@ _lib = None
 _ref = None
 
 
+def find_blas():
+    """OpenBLAS to build the reference's BLAS path against: (library path, symbol
+    prefix, symbol suffix, ILP64) of the copy NumPy's wheel bundles, or None."""
+    import ctypes.util
+    import glob
+    try:
+        import numpy
+        libdir = os.path.join(os.path.dirname(os.path.dirname(numpy.__file__)), "numpy.libs")
+        cands = sorted(glob.glob(os.path.join(libdir, "lib*openblas*.so*")))
+    except ImportError:
+        cands = []
+    sysblas = ctypes.util.find_library("openblas")
+    if sysblas:
+        cands.append(sysblas)
+    for path in cands:
+        try:
+            L = C.CDLL(path)
+        except OSError:
+            continue
+        for prefix, suffix, ilp64 in (("scipy_", "64_", True), ("", "64_", True), ("scipy_", "", False),
+                                      ("", "", False)):
+            names = [f"{prefix}{n}{suffix}" for n in ("cblas_sgemv", "cblas_dgemv",
+                                                      "openblas_set_num_threads",
+                                                      "openblas_get_num_threads")]
+            if all(hasattr(L, n) for n in names):
+                if not os.path.isabs(path):
+                    continue   # a bare soname cannot be linked by path; skip it
+                return path, prefix, suffix, ilp64
+    return None
+
+
+def blas_info():
+    """What libttvref_blas.so was linked against (the text of _ref/blas.cfg), or None."""
+    try:
+        with open(REF_BLAS_CFG) as f:
+            return f.read().strip() or None
+    except OSError:
+        return None
+
+
 def build(with_ref: bool | None = None) -> None:
-    """Compile liboracle.so (and _ref/libttvref.so when the reference exists)."""
+    """Compile liboracle.so and, where the reference headers are available (a
+    reference checkout, or the staged copy in baseline/_ref/include), the two
+    builds of the reference: _ref/libttvref.so and _ref/libttvref_blas.so."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if with_ref is None:
-        with_ref = os.path.isdir(REF_INCLUDE)
-    if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_INCLUDE={REF_INCLUDE}"], check=True)
+    if with_ref is False:
+        return
+    # refresh the staged headers where a reference checkout exists (no-op elsewhere)
+    subprocess.run(["make", "-s", "-C", HERE, "stage-ref"], capture_output=True)
+    if not os.path.isdir(os.path.join(REF_INCLUDE, "tlib")):
+        if with_ref:
+            raise FileNotFoundError(f"reference headers not found in {REF_INCLUDE}")
+        return
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_INCLUDE={REF_INCLUDE}"], check=True)
+    blas = find_blas()
+    os.makedirs(os.path.dirname(REF_BLAS_CFG), exist_ok=True)
+    cfg = "" if blas is None else f"{blas[0]} prefix={blas[1]} suffix={blas[2]} ilp64={int(blas[3])}"
+    if blas_info() != (cfg or None):
+        with open(REF_BLAS_CFG, "w") as f:
+            f.write(cfg + "\n")
+    if blas is None:
+        if os.path.exists(REF_BLAS_PATH):
+            os.remove(REF_BLAS_PATH)
+        return
+    subprocess.run(["make", "-s", "-C", HERE, "ref-blas", f"REF_INCLUDE={REF_INCLUDE}",
+                    f"BLAS_LIB={blas[0]}", f"BLAS_PREFIX={blas[1]}", f"BLAS_SUFFIX={blas[2]}",
+                    f"BLAS_ILP64={int(blas[3])}"], check=True)
 
 
 def lib() -> C.CDLL:
@@ -92,29 +164,50 @@ def ref_available() -> bool:
     return os.path.exists(REF_PATH)
 
 
+def ref_blas_available() -> bool:
+    return os.path.exists(REF_BLAS_PATH)
+
+
+def _bind_ref(path):
+    L = C.CDLL(path)
+    for name in ("ref_ttv_f32", "ref_ttv_f64"):
+        f = getattr(L, name)
+        f.restype = C.c_int
+        f.argtypes = [C.c_int, _sz, _sz, _vp, _psz, _psz, _psz, _vp, _psz, _vp, _psz, _psz,
+                      _psz, C.c_char_p, _sz]
+    L.ref_output_shape.argtypes = [_psz, _sz, _sz, _psz]
+    L.ref_output_layout.argtypes = [_psz, _sz, _sz, _psz]
+    L.ref_strides.argtypes = [_psz, _psz, _sz, _psz]
+    L.ref_k_order_layout.argtypes = [_sz, _sz, _psz]
+    L.ref_is_valid_shape.argtypes = [_psz, _sz]
+    L.ref_is_valid_layout.argtypes = [_psz, _sz]
+    L.ref_is_valid_strides.argtypes = [_psz, _sz, _psz]
+    L.ref_inverse_mode.restype = _sz
+    L.ref_inverse_mode.argtypes = [_psz, _sz, _sz]
+    return L
+
+
 def ref() -> C.CDLL:
-    """The reference compiled from source (only where it could be built)."""
+    """The reference compiled from source without BLAS (only where it could be built)."""
     global _ref
     if _ref is None:
         if not ref_available():
-            raise FileNotFoundError("oracle/_ref/libttvref.so not built (reference sources absent)")
-        L = C.CDLL(REF_PATH)
-        for name in ("ref_ttv_f32", "ref_ttv_f64"):
-            f = getattr(L, name)
-            f.restype = C.c_int
-            f.argtypes = [C.c_int, _sz, _sz, _vp, _psz, _psz, _psz, _vp, _psz, _vp, _psz, _psz,
-                          _psz, C.c_char_p, _sz]
-        L.ref_output_shape.argtypes = [_psz, _sz, _sz, _psz]
-        L.ref_output_layout.argtypes = [_psz, _sz, _sz, _psz]
-        L.ref_strides.argtypes = [_psz, _psz, _sz, _psz]
-        L.ref_k_order_layout.argtypes = [_sz, _sz, _psz]
-        L.ref_is_valid_shape.argtypes = [_psz, _sz]
-        L.ref_is_valid_layout.argtypes = [_psz, _sz]
-        L.ref_is_valid_strides.argtypes = [_psz, _sz, _psz]
-        L.ref_inverse_mode.restype = _sz
-        L.ref_inverse_mode.argtypes = [_psz, _sz, _sz]
-        _ref = L
+            raise FileNotFoundError("oracle/_ref/libttvref.so not built (reference headers absent)")
+        _ref = _bind_ref(REF_PATH)
     return _ref
+
+
+_ref_blas = None
+
+
+def ref_blas() -> C.CDLL:
+    """The reference compiled from source with -DUSE_OPENBLAS (its configured BLAS path)."""
+    global _ref_blas
+    if _ref_blas is None:
+        if not ref_blas_available():
+            raise FileNotFoundError("oracle/_ref/libttvref_blas.so not built (no OpenBLAS found)")
+        _ref_blas = _bind_ref(REF_BLAS_PATH)
+    return _ref_blas
 
 
 # --------------------------------------------------------------------------
@@ -206,13 +299,15 @@ def ttv(policy, q, a, na, wa, pia, b, nb, nc, wc, pic, c=None):
     return st, c
 
 
-def ref_ttv(policy, q, a, na, wa, pia, b, nb, nc, wc, pic, c=None):
-    """Run the reference compiled from source; returns (status, message, c)."""
+def ref_ttv(policy, q, a, na, wa, pia, b, nb, nc, wc, pic, c=None, blas=False):
+    """Run the reference compiled from source (blas=True: its OpenBLAS build);
+    returns (status, message, c)."""
     a = np.ascontiguousarray(a)
     dt = a.dtype
     if c is None:
         c = np.zeros(int(np.prod(nc)) if nc else 1, dtype=dt)
-    f = ref().ref_ttv_f32 if dt == np.float32 else ref().ref_ttv_f64
+    R = ref_blas() if blas else ref()
+    f = R.ref_ttv_f32 if dt == np.float32 else R.ref_ttv_f64
     keep = [sizes(v) for v in (na, wa, pia, nb, nc, wc, pic)]
     msg = C.create_string_buffer(512)
     pol = POLICIES.get(policy, policy)

@@ -480,25 +480,38 @@ static inline void dd_add(double* hi, double* lo, double x, double xe)
     *hi = h;
 }
 
+/* Per output the products are added in ascending i, each into a double-double
+ * sum; rows (P == 1) one output at a time, columns (P > 1) in blocks of
+ * ORC_TRUTH_JB neighbouring outputs that walk their rows together (the same
+ * additions in the same order per output, read along the contiguous prefix). */
+#define ORC_TRUTH_JB 64
 #define ORC_DEFINE_TRUTH(NAME, TA, TB, LOADA, EXACT_PRODUCT)                                \
 void NAME(uint64_t S, uint64_t nq, uint64_t P, const TA* a, const TB* b, double* ref,        \
           double* absn)                                                                     \
 {                                                                                           \
-    _Pragma("omp parallel for schedule(static)")                                            \
-    for (uint64_t o = 0; o < S * P; ++o) {                                                  \
-        const uint64_t s = o / P, j = o % P;                                                \
-        const TA* ap = a + s * nq * P + j;                                                  \
-        double hi = 0.0, lo = 0.0, an = 0.0;                                                \
+    const uint64_t nblk = (P + ORC_TRUTH_JB - 1) / ORC_TRUTH_JB;                            \
+    _Pragma("omp parallel for schedule(dynamic, 4)")                                        \
+    for (uint64_t t = 0; t < S * nblk; ++t) {                                               \
+        const uint64_t s = t / nblk, j0 = (t % nblk) * ORC_TRUTH_JB;                        \
+        const uint64_t jn = (P - j0) < ORC_TRUTH_JB ? (P - j0) : ORC_TRUTH_JB;              \
+        double hi[ORC_TRUTH_JB], lo[ORC_TRUTH_JB], an[ORC_TRUTH_JB];                        \
+        for (uint64_t j = 0; j < jn; ++j) hi[j] = lo[j] = an[j] = 0.0;                      \
+        const TA* ap = a + s * nq * P + j0;                                                 \
         for (uint64_t i = 0; i < nq; ++i) {                                                 \
-            double av = LOADA(ap[i * P]);                                                   \
-            double bv = (double)b[i];                                                       \
-            double pr = av * bv;                                                            \
-            double pe = EXACT_PRODUCT ? 0.0 : fma(av, bv, -pr);                             \
-            dd_add(&hi, &lo, pr, pe);                                                       \
-            an += fabs(pr);                                                                 \
+            const double bv = (double)b[i];                                                 \
+            const TA* row = ap + i * P;                                                     \
+            for (uint64_t j = 0; j < jn; ++j) {                                             \
+                double av = LOADA(row[j]);                                                  \
+                double pr = av * bv;                                                        \
+                double pe = EXACT_PRODUCT ? 0.0 : fma(av, bv, -pr);                         \
+                dd_add(&hi[j], &lo[j], pr, pe);                                             \
+                an[j] += fabs(pr);                                                          \
+            }                                                                               \
         }                                                                                   \
-        ref[o] = hi + lo;                                                                   \
-        absn[o] = an;                                                                       \
+        for (uint64_t j = 0; j < jn; ++j) {                                                 \
+            ref[s * P + j0 + j] = hi[j] + lo[j];                                            \
+            absn[s * P + j0 + j] = an[j];                                                   \
+        }                                                                                   \
     }                                                                                       \
 }
 

@@ -6,7 +6,9 @@
 //   ttv_gpu_kat validate   argument errors only (no device needed): the
 //                          exception text equals the reference's
 //   ttv_gpu_kat kat        the KAT grid on the GPU (ranks 2-4, extents
-//                          {2, 4, 8}, every layout and q), float and double
+//                          {2, 4, 8}, every layout and q), float and double,
+//                          each call with one of the six (slicing, fusion)
+//                          pairs of the reference's tests in turn
 //   ttv_gpu_kat tensor     the device tensor interface (A(q) * b, ttv(q, A, b))
 //                          on the KAT grid of rank 3, host-pointer calls of the
 //                          gpu policy, and (with the reference headers) the
@@ -138,6 +140,30 @@ static void init_kat(std::size_t q, std::vector<T>& a, const sizes& na, const si
     }
 }
 
+// The low-level call through the gpu policy with slicing / fusion pair k of
+// {slice, subtensor} x {none, outer, all}: the engine treats them as the
+// scheduling hints they are on the CPU and computes the same C.
+static std::size_t pair_index = 0;
+static std::size_t pair_seen[6] = {};
+
+template <class T>
+static void call_with_pair(std::size_t k, std::size_t q, std::size_t p, const T* a, const sizes& na,
+                           const sizes& wa, const sizes& pia, const T* b, const sizes& nb, T* c,
+                           const sizes& nc, const sizes& wc, const sizes& pic)
+{
+    ++pair_seen[k];
+    const auto ep = execution_policy::gpu;
+    const auto* n = na.data();
+    switch (k) {
+    case 0: ttv(ep, slicing_policy::subtensor, fusion_policy::all, q, p, a, n, wa.data(), pia.data(), b, nb.data(), c, nc.data(), wc.data(), pic.data()); break;
+    case 1: ttv(ep, slicing_policy::subtensor, fusion_policy::none, q, p, a, n, wa.data(), pia.data(), b, nb.data(), c, nc.data(), wc.data(), pic.data()); break;
+    case 2: ttv(ep, slicing_policy::subtensor, fusion_policy::outer, q, p, a, n, wa.data(), pia.data(), b, nb.data(), c, nc.data(), wc.data(), pic.data()); break;
+    case 3: ttv(ep, slicing_policy::slice, fusion_policy::all, q, p, a, n, wa.data(), pia.data(), b, nb.data(), c, nc.data(), wc.data(), pic.data()); break;
+    case 4: ttv(ep, slicing_policy::slice, fusion_policy::none, q, p, a, n, wa.data(), pia.data(), b, nb.data(), c, nc.data(), wc.data(), pic.data()); break;
+    default: ttv(ep, slicing_policy::slice, fusion_policy::outer, q, p, a, n, wa.data(), pia.data(), b, nb.data(), c, nc.data(), wc.data(), pic.data()); break;
+    }
+}
+
 template <class T>
 static int kat_rank(std::size_t rank)
 {
@@ -176,8 +202,9 @@ static int kat_rank(std::size_t rank)
                 const sizes nb{na[q - 1]};
                 cudaMemcpy(da, a.data(), nn * sizeof(T), cudaMemcpyHostToDevice);
                 cudaMemcpy(db, b.data(), b.size() * sizeof(T), cudaMemcpyHostToDevice);
-                ttv(execution_policy::gpu, slicing_policy::subtensor, fusion_policy::all, q, rank, da,
-                    na.data(), wa.data(), pia.data(), db, nb.data(), dc, nc.data(), wc.data(), pic.data());
+                // every (slicing, fusion) pair the reference's own tests pass
+                // (gtest_tlib_ttv.cpp:192-425), in turn over the grid's calls
+                call_with_pair(pair_index++ % 6, q, rank, da, na, wa, pia, db, nb, dc, nc, wc, pic);
                 const std::size_t ncn = nn / na[q - 1];
                 std::vector<T> c(ncn);
                 cudaMemcpy(c.data(), dc, ncn * sizeof(T), cudaMemcpyDeviceToHost);
@@ -290,6 +317,12 @@ int main(int argc, char** argv)
     }
     int bad = 0;
     for (std::size_t r = 2; r <= 4; ++r) bad += kat_rank<float>(r) + kat_rank<double>(r);
-    std::printf("%s kat (%d mismatches)\n", bad ? "FAILED" : "PASSED", bad);
+    for (std::size_t k = 0; k < 6; ++k)
+        if (pair_seen[k] == 0) {
+            std::printf("slicing / fusion pair %zu never called\n", k);
+            ++bad;
+        }
+    std::printf("%s kat (%d mismatches; %zu calls over 6 slicing/fusion pairs; %s)\n", bad ? "FAILED" : "PASSED",
+                bad, pair_index, TLIBG_WITH_REFERENCE ? "reference headers" : "standalone");
     return bad ? 1 : 0;
 }

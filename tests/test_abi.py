@@ -227,8 +227,9 @@ def _compile_cpp(tmp_path, standalone):
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("g++ missing")
-    ref_inc = os.environ.get("TTV_REFERENCE_INCLUDE", "/root/reference/include")
-    if not standalone and not os.path.isdir(ref_inc):
+    import oracle
+    ref_inc = oracle.REF_INCLUDE   # the staged reference headers (or TTV_REFERENCE_INCLUDE)
+    if not standalone and not os.path.isdir(os.path.join(ref_inc, "tlib")):
         pytest.skip("reference headers absent")
     exe = str(tmp_path / ("kat_sa" if standalone else "kat_ref"))
     cuda_inc = "/usr/local/cuda/include"

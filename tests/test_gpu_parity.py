@@ -90,22 +90,29 @@ def test_kat_grid(engine, torch_dev, rank):
                                                   err_msg=f"{na} {pia} q={q} {dt}")
 
 
-def test_cpp_kat_through_policy(engine, cuda, tmp_path):
-    """The same KAT through the C++ `execution_policy::gpu` drop-in."""
+@pytest.mark.parametrize("standalone", [False, True], ids=["reference_headers", "standalone"])
+def test_cpp_kat_through_policy(engine, cuda, tmp_path, standalone):
+    """The same KAT through the C++ `execution_policy::gpu` drop-in, every
+    (slicing, fusion) pair of the reference's tests.  With the reference
+    headers (staged in baseline/_ref/include) the call goes through the
+    reference's own tlib::ttv::ttv (ttv.h:54-92: its checks, then its dispatch
+    to detail::ttv at ttv.h:91), which resolves to the gpu overloads."""
     from test_abi import _compile_cpp
     import subprocess
-    exe = _compile_cpp(tmp_path, standalone=True)
+    exe = _compile_cpp(tmp_path, standalone=standalone)
     r = subprocess.run([exe, "kat"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "PASSED" in r.stdout, r.stdout + r.stderr
+    assert ("reference headers" if not standalone else "standalone") in r.stdout
 
 
-def test_cpp_device_tensor_interface(engine, cuda, tmp_path):
+@pytest.mark.parametrize("standalone", [False, True], ids=["reference_headers", "standalone"])
+def test_cpp_device_tensor_interface(engine, cuda, tmp_path, standalone):
     """tlib/ttv_gpu_tensor.h: A(q) * b and ttv(q, A, b) on device tensors, the gpu
-    policy on host pointers (the engine's host path) and, where the reference
-    headers exist, the reference's own tensor<T> through the gpu policy."""
+    policy on host pointers (the engine's host path) and, with the reference
+    headers, the reference's own tensor<T> through the gpu policy."""
     from test_abi import _compile_cpp
     import subprocess
-    exe = _compile_cpp(tmp_path, standalone=True)
+    exe = _compile_cpp(tmp_path, standalone=standalone)
     r = subprocess.run([exe, "tensor"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "PASSED" in r.stdout, r.stdout + r.stderr
 

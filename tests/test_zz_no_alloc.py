@@ -6,9 +6,13 @@ multi-tenant processes, and latency-critical loops that cannot absorb the
 implicit device synchronisation of cudaMalloc/cudaFree.  For them the split
 reduction's partial sums live in one fixed array compiled into the library
 (TLIBG_NOALLOC_SCRATCH_BYTES).  Here its results are checked against the
-regular tlibg_ttv_f32 on the same inputs, on two calls in a row with different
-data (stale partial sums of the first call would show in the second), and a
-problem needing more scratch than the array holds must be refused.
+oracle's double-double truth and against the regular tlibg_ttv_f32 on the same
+inputs, on two calls in a row with different data (stale partial sums of the
+first call would show in the second); a call on a shape and stream the process
+has not used before must leave the library's device-allocation count where it
+was; a plan whose split needs more scratch than the array (an installed plan
+hint) is planned again with fewer segments; and a problem that fits no plan
+must be refused.
 
 The file is named to be collected last, so a run that stops at the first
 failure has already run every other test.
@@ -56,8 +60,15 @@ CASES = [
 ]
 
 
+def oracle_error(orc, engine, q, na, pia, A, b, c):
+    """max |c - truth| / sum_k |a_ik b_k| against the oracle's fp64 truth."""
+    P, nq, S = orc.canonical(na, pia, q)
+    ref, absn = orc.truth(S, nq, P, A.cpu().numpy(), b.cpu().numpy())
+    return orc.rel_error(c.cpu().numpy(), ref, absn)
+
+
 @pytest.mark.parametrize("na,pia,q", CASES)
-def test_noalloc_matches_regular_entry_point(engine, cuda, na, pia, q):
+def test_noalloc_matches_regular_entry_point(engine, orc, cuda, na, pia, q):
     import torch
     lib = bind(engine)
     assert split_scratch_bytes(engine, q, na, pia) <= LIMIT
@@ -82,7 +93,63 @@ def test_noalloc_matches_regular_entry_point(engine, cuda, na, pia, q):
         err = ((c_new.double() - c_ref.double()).abs().view(S, P) / absn.clamp_min(1e-300)).max()
         assert not torch.isnan(c_new).any(), f"round {round_}: unwritten outputs"
         assert float(err) <= 1e-5, f"round {round_}: {float(err):.3e}"
+        e_orc = oracle_error(orc, engine, q, na, pia, A, b, c_new)
+        assert e_orc <= 1e-5, f"round {round_}: {e_orc:.3e} against the oracle"
     assert engine.device_error() == 0
+
+
+def test_noalloc_allocates_nothing(engine, orc, cuda):
+    """A shape and a stream this process has not used: the regular entry point
+    allocates split scratch for the new stream, the allocation-free one does not."""
+    import torch
+    lib = bind(engine)
+    na, pia, q = [96, 3 << 17], [1, 2], 2          # split reduction (thin prefix, long q)
+    assert split_scratch_bytes(engine, q, na, pia) > 0
+    g = torch.Generator(device=cuda)
+    g.manual_seed(11)
+    A = torch.rand(int(np.prod(na)), generator=g, device=cuda) * 2 - 1
+    b = torch.rand(na[1], generator=g, device=cuda) * 2 - 1
+    c = torch.full((na[0],), float("nan"), device=cuda)
+    fresh = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    before = engine.device_alloc_count()
+    for _ in range(2):
+        assert call(engine, lib.tlibg_ttv_f32_noalloc, q, na, pia, A, b, c, fresh.cuda_stream) == 0
+    fresh.synchronize()
+    assert engine.device_alloc_count() == before
+    assert oracle_error(orc, engine, q, na, pia, A, b, c) <= 1e-5
+    # the regular entry point on the same fresh stream does allocate its scratch
+    c2 = torch.full((na[0],), float("nan"), device=cuda)
+    assert call(engine, lib.tlibg_ttv_f32, q, na, pia, A, b, c2, fresh.cuda_stream) == 0
+    fresh.synchronize()
+    assert engine.device_alloc_count() > before
+    assert engine.device_error() == 0
+
+
+def test_noalloc_caps_an_oversize_split(engine, orc, cuda):
+    """An installed plan hint asks for more segments than the array holds: the
+    call plans again with the most segments that fit and still matches the
+    oracle; the regular entry point keeps the hint."""
+    import torch
+    lib = bind(engine)
+    na, pia, q = [1 << 14, 1 << 13], [1, 2], 2
+    engine.plan_hint(engine.F32, 1 << 14, 1 << 13, 1, kind=engine.KIND_COL, split=128)
+    try:
+        assert engine.plan(q, na, pia)["split"] == 128
+        assert split_scratch_bytes(engine, q, na, pia) > LIMIT
+        g = torch.Generator(device=cuda)
+        g.manual_seed(12)
+        A = torch.rand(int(np.prod(na)), generator=g, device=cuda) * 2 - 1
+        b = torch.rand(na[1], generator=g, device=cuda) * 2 - 1
+        c = torch.full((na[0],), float("nan"), device=cuda)
+        st = call(engine, lib.tlibg_ttv_f32_noalloc, q, na, pia, A, b, c,
+                  torch.cuda.current_stream().cuda_stream)
+        assert st == 0, engine._last_error()
+        torch.cuda.synchronize()
+        assert oracle_error(orc, engine, q, na, pia, A, b, c) <= 1e-5
+    finally:
+        engine.clear_plan_hint(engine.F32, 1 << 14, 1 << 13, 1)
+    assert engine.plan(q, na, pia)["split"] != 128
 
 
 def test_noalloc_refuses_oversize_scratch(engine, cuda):

@@ -27,7 +27,8 @@ import os
 __all__ = [
     "TTVError", "UnsupportedError", "ttv", "ttv_ex", "ttv_host", "ttv_array", "ttvs", "plan",
     "output_shape", "output_layout", "strides", "k_order_layout", "inverse_mode",
-    "library", "library_path", "launch_count", "device_error", "F32", "F64", "BF16A",
+    "library", "library_path", "launch_count", "device_error", "device_alloc_count",
+    "plan_hint", "clear_plan_hint", "F32", "F64", "BF16A",
     "ACC_COMPENSATED", "ACC_PLAIN", "ACC_DOUBLE_FLOAT", "KIND_ROW", "KIND_COL", "KIND_STREAM",
     "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE", "KIND_COL_BULK",
 ]
@@ -111,6 +112,10 @@ def library() -> C.CDLL:
         L.tlibg_last_error.argtypes = [C.c_char_p, _sz]
         L.tlibg_device_error.restype = C.c_int
         L.tlibg_launch_count.restype = C.c_uint64
+        L.tlibg_device_alloc_count.restype = C.c_uint64
+        L.tlibg_plan_hint.restype = C.c_int
+        L.tlibg_plan_hint.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64,
+                                      C.POINTER(Options)]
         L.tlibg_version.restype = C.c_char_p
         _lib = L
     return _lib
@@ -308,6 +313,23 @@ def inverse_mode(pi, mode):
     if r == 0:
         raise TTVError(_last_error())
     return r
+
+
+def device_alloc_count() -> int:
+    """Device allocations (cudaMalloc) the engine made since load."""
+    return int(library().tlibg_device_alloc_count())
+
+
+def plan_hint(dtype, P, nq, S, **options):
+    """Install autotuned options for the canonical problem (dtype, P, n_q, S):
+    later calls that leave every choice to the planner use them."""
+    o = _options(**options)
+    _raise(library().tlibg_plan_hint(dtype, P, nq, S, C.byref(o)))
+
+
+def clear_plan_hint(dtype=0, P=0, nq=0, S=0):
+    """Remove one plan hint, or all of them (the default)."""
+    _raise(library().tlibg_plan_hint(dtype, P, nq, S, None))
 
 
 def launch_count() -> int:

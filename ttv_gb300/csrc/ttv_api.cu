@@ -21,6 +21,15 @@ namespace {
 
 thread_local std::string t_last_error;
 std::atomic<uint64_t> g_launches{0};
+std::atomic<uint64_t> g_device_allocs{0};
+
+// Every device allocation of the library goes through here (counted).
+cudaError_t device_malloc(void** p, size_t bytes)
+{
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) ++g_device_allocs;
+    return e;
+}
 
 int fail(int code, const std::string& msg)
 {
@@ -450,6 +459,7 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
 {
     Plan pl;
     pl.dtype = dtype;
+    pl.sms = sms;
     pl.P = cn.P;
     pl.nq = cn.nq;
     pl.S = cn.S;
@@ -744,7 +754,7 @@ int get_scratch(cudaStream_t stream, size_t bytes, void** out)
             s.bytes = 0;
         }
         size_t want = std::max(bytes, (size_t)1 << 20);
-        cudaError_t e = cudaMalloc(&s.ptr, want);
+        cudaError_t e = device_malloc(&s.ptr, want);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return fail(TLIBG_ERR_NOMEM, std::string("tlibg: cannot allocate split scratch: ") + cudaGetErrorString(e));
@@ -916,7 +926,7 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
     for (size_t r = k + 1; r < p; ++r) cn.S *= na[pia[r] - 1];
     cn.nq = na[q - 1];
     DevInfo d = dev_info();
-    const int sms = d.ok ? d.sms : 152;
+    const int sms = d.ok ? d.sms : PLAN_SMS_WITHOUT_DEVICE;
     Plan pl;
     // plan for 256-byte aligned device buffers (what cudaMalloc returns)
     static const uint4 probe_a[1] = {};
@@ -994,7 +1004,7 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         if (*p_) cudaFree(*p_);
         *p_ = nullptr;
         *have = 0;
-        cudaError_t ee = cudaMalloc(p_, need);
+        cudaError_t ee = device_malloc(p_, need);
         if (ee != cudaSuccess) {
             cudaGetLastError();
             return fail(TLIBG_ERR_NOMEM, "tlibg: cannot allocate device staging buffers");
@@ -1010,7 +1020,7 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         }
         hc.abytes = 0;
         for (int i = 0; i < 2; ++i)
-            if (cudaMalloc(&hc.abuf[i], need_a) != cudaSuccess) {
+            if (device_malloc(&hc.abuf[i], need_a) != cudaSuccess) {
                 cudaGetLastError();
                 return fail(TLIBG_ERR_NOMEM, "tlibg: cannot allocate device staging buffers");
             }
@@ -1202,6 +1212,8 @@ int tlibg_device_error(void)
 
 uint64_t tlibg_launch_count(void) { return g_launches.load(); }
 
+uint64_t tlibg_device_alloc_count(void) { return g_device_allocs.load(); }
+
 const char* tlibg_version(void) { return "tlibg 0.1 (sm_103a)"; }
 
 }  // extern "C"
@@ -1221,18 +1233,46 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[TLIBG_NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch, resolved once per device with that
-// device current.  In host code the array's name is only a host-side stand-in
-// for the symbol, never a device address, so kernels get this pointer.
+// cuCtxGetCurrent through the runtime's driver entry point (the library does
+// not link the driver library itself).
+typedef int (*CtxGetCurrentFn)(void**);
+
+CtxGetCurrentFn ctx_get_current()
+{
+    static CtxGetCurrentFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<CtxGetCurrentFn>(f);
+    }();
+    return fn;
+}
+
+// Device address of g_noalloc_scratch, resolved once per (device, context)
+// with that device current.  In host code the array's name is only a
+// host-side stand-in for the symbol, never a device address, so kernels get
+// this pointer.  The context is part of the key: after cudaDeviceReset (or any
+// new primary context) the module is loaded again and the array may live at
+// another address.
 int noalloc_scratch(void** out)
 {
     static std::mutex mu;
-    static std::map<int, void*> addr;
+    static std::map<std::pair<int, uintptr_t>, void*> addr;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    // cudaSetDevice makes the device's primary context current (initialising it
+    // if need be), so the context read below is the one the kernels run in
+    if ((e = cudaSetDevice(dev)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    void* ctx = nullptr;
+    if (CtxGetCurrentFn f = ctx_get_current()) f(&ctx);
+    const auto key = std::make_pair(dev, reinterpret_cast<uintptr_t>(ctx));
     std::lock_guard<std::mutex> lk(mu);
-    auto it = addr.find(dev);
+    auto it = addr.find(key);
     if (it != addr.end()) {
         *out = it->second;
         return TLIBG_OK;
@@ -1241,7 +1281,7 @@ int noalloc_scratch(void** out)
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr)
         return cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress");
-    addr[dev] = p;
+    addr[key] = p;
     *out = p;
     return TLIBG_OK;
 }
@@ -1253,6 +1293,7 @@ extern "C" int tlibg_ttv_f32_noalloc(size_t q, size_t p, const float* a, const s
                                      const size_t* nb, float* c, const size_t* nc,
                                      const size_t* wc, const size_t* pic, void* stream)
 {
+    NvtxRange nvtx("tlibg_ttv_f32_noalloc");
     Canon cn;
     int st = analyse(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, &cn);
     if (st) return st;
@@ -1262,16 +1303,37 @@ extern "C" int tlibg_ttv_f32_noalloc(size_t q, size_t p, const float* a, const s
     if (!d.ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
     st = check_device_pointers(a, b, c);
     if (st) return st;
+    const size_t limit = (size_t)TLIBG_NOALLOC_SCRATCH_BYTES;
     Plan pl;
     st = make_plan(F32, cn, a, b, nullptr, d.sms, &pl);
     if (st) return st;
-    const size_t need = partial_bytes(pl);
-    if (need > (size_t)TLIBG_NOALLOC_SCRATCH_BYTES)
-        return fail(TLIBG_ERR_UNSUPPORTED,
-                    "tlibg_ttv_f32_noalloc: this problem's split reduction needs " + std::to_string(need) +
-                        " bytes of scratch, more than the fixed " +
-                        std::to_string((size_t)TLIBG_NOALLOC_SCRATCH_BYTES) +
-                        "-byte buffer; use tlibg_ttv_f32");
+    size_t need = partial_bytes(pl);
+    if (need > limit) {
+        // The planner's split needs more scratch than the array holds: plan again
+        // with the split capped at the most segments whose partials fit (the
+        // kernels' own lower bound on segments still applies), then without a
+        // split; refuse only if neither plan fits.
+        const size_t per_seg = (size_t)(cn.S * cn.P) * 2 * sizeof(float);
+        const size_t cap = per_seg ? limit / per_seg : 0;
+        bool found = false;
+        for (size_t k : {cap, (size_t)1}) {
+            if (k < 1) continue;
+            tlibg_options o{TLIBG_ACC_COMPENSATED, -1, 0, 0, (int)std::min<size_t>(k, 1u << 30), 0};
+            Plan alt;
+            if (make_plan_inner(F32, cn, a, b, &o, d.sms, &alt) != TLIBG_OK) continue;
+            if (partial_bytes(alt) <= limit) {
+                pl = alt;
+                need = partial_bytes(alt);
+                found = true;
+                break;
+            }
+        }
+        if (!found)
+            return fail(TLIBG_ERR_UNSUPPORTED,
+                        "tlibg_ttv_f32_noalloc: this problem's split reduction needs " + std::to_string(need) +
+                            " bytes of scratch, more than the fixed " + std::to_string(limit) +
+                            "-byte buffer; use tlibg_ttv_f32");
+    }
     void* part = nullptr;
     if (need) {
         st = noalloc_scratch(&part);
@@ -1329,6 +1391,7 @@ int internal_check_device_pointers(const void* a, const void* b, const void* c)
     return check_device_pointers(a, b, c);
 }
 int internal_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
+cudaError_t internal_malloc(void** p, size_t bytes) { return device_malloc(p, bytes); }
 void internal_count_launches(uint64_t n) { g_launches += n; }
 
 }  // namespace tlibg

@@ -840,11 +840,11 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         return create_fail(bt, TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: more than 2^32 work units");
 
     cudaError_t e = cudaSuccess;
-    if ((e = cudaMalloc(&bt->d_prob, count * sizeof(BProb))) != cudaSuccess ||
-        (e = cudaMalloc(&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
-        (e = cudaMalloc(&bt->d_map, std::max<uint64_t>(total_units, 1) * sizeof(uint32_t))) != cudaSuccess ||
-        (e = cudaMalloc(&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
-        (!model.empty() && (e = cudaMalloc(&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
+    if ((e = internal_malloc((void**)&bt->d_prob, count * sizeof(BProb))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_map, std::max<uint64_t>(total_units, 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
+        (!model.empty() && (e = internal_malloc((void**)&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
         cudaGetLastError();
         return create_fail(bt, TLIBG_ERR_NOMEM, std::string("tlibg_batch_create: ") + cudaGetErrorString(e));
     }

@@ -41,6 +41,9 @@ int internal_check_device_pointers(const void* a, const void* b, const void* c);
 int internal_fail(int code, const std::string& msg);
 int internal_ok();
 int internal_cuda_fail(cudaError_t e, const char* where);
+// cudaMalloc, counted by tlibg_device_alloc_count (every device allocation of
+// the library goes through it).
+cudaError_t internal_malloc(void** p, size_t bytes);
 void internal_count_launches(uint64_t n);
 
 }  // namespace tlibg

@@ -993,15 +993,16 @@ cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_
     cudaError_t err;
     {
         const uint64_t outputs = plan.S * plan.P;
+        const uint64_t sms = plan.sms > 0 ? (uint64_t)plan.sms : (uint64_t)PLAN_SMS_WITHOUT_DEVICE;
         // threads per output: one when the outputs alone fill the GPU, else enough
         // to give each thread about eight segments
         uint32_t tpo = 1;
-        if (outputs < (uint64_t)152 * BLOCK * 4 && plan.split >= 16) {
+        if (outputs < sms * BLOCK * 4 && plan.split >= 16) {
             tpo = 1;
             while (tpo * 2 <= (uint32_t)BLOCK && tpo * 2 * 8 <= (uint32_t)plan.split) tpo *= 2;
         }
         const uint64_t opb = BLOCK / tpo;
-        int g = (int)std::min<uint64_t>(152 * 16, (outputs + opb - 1) / opb);
+        int g = (int)std::min<uint64_t>(sms * 16, (outputs + opb - 1) / opb);
         if (g < 1) g = 1;
         switch (plan.dtype) {
         case F32:

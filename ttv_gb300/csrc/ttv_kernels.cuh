@@ -13,6 +13,9 @@ enum Kind {
 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
+// SM count assumed by tlibg_plan when no device is present (a GB300: 2 dies x
+// 76 SMs); every launch plans with the current device's own count.
+constexpr int PLAN_SMS_WITHOUT_DEVICE = 152;
 constexpr int BSTAGE_BYTES = 16384;   // bytes of b staged per CTA by the column kernel
 constexpr int STREAM_STAGE_BYTES = 16384;   // streamed kernel: bytes of A per shared-memory stage
 constexpr int STREAM_CONSUMERS = 256;       // streamed kernel: consumer threads per CTA
@@ -64,6 +67,7 @@ struct Plan {
     uint64_t items = 0;          // work items (ROW: rows x segments; COL: tiles x segments)
     uint64_t items_per_cta = 0;  // COL: contiguous block of items per CTA
     int grid = 1;
+    int sms = 0;                 // streaming multiprocessors of the device planned for
     size_t smem = 0;
     bool f64_combine = false;    // combine split partials in fp64 (fp32 storage, nq > 2^20)
     // streamed kernel (kind == KIND_STREAM): A as rows of L elements, R rows per chunk

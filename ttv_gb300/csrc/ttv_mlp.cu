@@ -165,7 +165,7 @@ int workspace(cudaStream_t st, size_t rows, Work** out)
         w.buf = nullptr;
         w.rows = 0;
         const size_t floats = rows * (6 * MLP_H + MLP_IN + 2) + 4;
-        cudaError_t e = cudaMalloc(&w.buf, floats * sizeof(float));
+        cudaError_t e = internal_malloc((void**)&w.buf, floats * sizeof(float));
         if (e != cudaSuccess) return internal_cuda_fail(e, "cost-model workspace");
         w.rows = rows;
     }
@@ -249,9 +249,9 @@ int tlibg_mlp_train(float* params, float* m, float* v, const float* x, const flo
     float *grad = nullptr, *loss = nullptr;
     int* idx = nullptr;
     cudaError_t e;
-    if ((e = cudaMalloc(&grad, MLP_PARAMS * sizeof(float))) != cudaSuccess) return internal_cuda_fail(e, "train grad");
-    if ((e = cudaMalloc(&loss, sizeof(float))) != cudaSuccess) return internal_cuda_fail(e, "train loss");
-    if ((e = cudaMalloc(&idx, n * sizeof(int))) != cudaSuccess) return internal_cuda_fail(e, "train idx");
+    if ((e = internal_malloc((void**)&grad, MLP_PARAMS * sizeof(float))) != cudaSuccess) return internal_cuda_fail(e, "train grad");
+    if ((e = internal_malloc((void**)&loss, sizeof(float))) != cudaSuccess) return internal_cuda_fail(e, "train loss");
+    if ((e = internal_malloc((void**)&idx, n * sizeof(int))) != cudaSuccess) return internal_cuda_fail(e, "train idx");
     std::vector<int> perm(n);
     uint64_t state = seed * 6364136223846793005ull + 1442695040888963407ull;
     auto next = [&state]() {

@@ -23,7 +23,7 @@ import numpy as np
 
 from . import F32, F64, KIND_COL, KIND_COL_BULK, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_TILE, KIND_STREAM, \
     ACC_DOUBLE_FLOAT, \
-    _options, library, output_layout, output_shape, plan, strides, ttv
+    clear_plan_hint, output_layout, output_shape, plan, plan_hint, strides, ttv
 
 L2_FLUSH_BYTES = 256 << 20
 
@@ -108,21 +108,12 @@ def tune_problem(dtype, na, pia, q, A, b, c, reps=5, flush=None):
 
 def install(entries):
     """Install tuned options as plan hints: [{'dtype', 'P', 'nq', 'S', 'options'}]."""
-    import ctypes as C
-    L = library()
-    L.tlibg_plan_hint.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
     for e in entries:
-        o = _options(**e["options"])
-        st = L.tlibg_plan_hint(e["dtype"], e["P"], e["nq"], e["S"], C.addressof(o))
-        if st:
-            raise RuntimeError("tlibg_plan_hint failed")
+        plan_hint(e["dtype"], e["P"], e["nq"], e["S"], **e["options"])
 
 
 def clear_hints():
-    import ctypes as C
-    L = library()
-    L.tlibg_plan_hint.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
-    L.tlibg_plan_hint(0, 0, 0, 0, None)
+    clear_plan_hint()
 
 
 def main():
