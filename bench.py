@@ -201,10 +201,12 @@ def kernel_label(T, c):
     fam = {T.KIND_ROW: "row_kernel", T.KIND_COL: "col_kernel",
            T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel",
            T.KIND_COL_THIN: "col_thin_kernel", T.KIND_ROW_TILE: "row_tile_kernel",
-           T.KIND_COL_BULK: "col_bulk_kernel"}[pl["kind"]]
+           T.KIND_COL_BULK: "col_bulk_kernel", T.KIND_ROW_PANEL: "row_panel_kernel"}[pl["kind"]]
     if pl["kind"] == T.KIND_COL and pl["vec"] == 1:
         fam = "col_strided_kernel"   # scalar loads, two outputs per thread
     templ = "" if pl["kind"] in (T.KIND_STREAM, T.KIND_ROW_TILE, T.KIND_COL_BULK) else f",V{pl['vec']}"
+    if pl["kind"] == T.KIND_ROW_PANEL:
+        templ += f",R{pl['group']}"
     acc = ",kahan" if pl["accumulate"] == T.ACC_COMPENSATED and dt != "f64" else ""
     return f"{fam}<{dt}{templ}{acc}>" + ("+combine" if pl["split"] > 1 else "")
 
@@ -380,6 +382,8 @@ def run_ours(args, rank, world, local_rank):
             torch.cuda.empty_cache()
             out["precision"] = run_precision_sub(T, torch, dev, args)
             torch.cuda.empty_cache()
+            out["ttvs"] = run_ttvs_sub(T, torch, dev, args)
+            torch.cuda.empty_cache()
         if not args.no_batch and args.workload != "case":
             out["batched"] = run_batched(T, torch, dev, args, n=args.batch_problems)
     return out
@@ -436,6 +440,62 @@ def run_precision_sub(T, torch, dev, args):
     return {"workload": full["config"]["workload"], "variants_GBps": full["variants_GBps"],
             "frac_compensated": full["roofline"]["frac"], "errors": full["precision"],
             "bars": full["bars"]}
+
+
+def run_ttvs_sub(T, torch, dev, args, na=(128, 128, 128, 128)):
+    """The multi-vector chain (ttvpy.ttvs) on an order-4 fp32 tensor of 2^28
+    elements, every q: the fused chain (A read once) against the first TTV of
+    the reference's optimal order alone (the largest vector's mode, which
+    reads A once too) and the step-by-step chain; error vs the oracle."""
+    import oracle
+    na = list(na)
+    g = torch.Generator(device=dev)
+    g.manual_seed(28)
+    A = (torch.rand(int(np.prod(na)), generator=g, device=dev) * 2 - 1).view(*na)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    K = max(3, min(args.steps, 10))
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(K):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
+
+    res, tot = {}, {"fused": 0.0, "first_ttv": 0.0, "step_by_step": 0.0}
+    nbytes = 0
+    for q in range(1, 5):
+        bs = [torch.rand(na[m], generator=g, device=dev) * 2 - 1 for m in range(4) if m != q - 1]
+        first_mode = max((m for m in range(1, 5) if m != q), key=lambda m: (na[m - 1], m))
+        bfirst = bs[first_mode - 1 if first_mode < q else first_mode - 2]
+        c1 = torch.empty([n for i, n in enumerate(na) if i != first_mode - 1], device=dev)
+        ms_f = timed(lambda: T.ttvs(q, A, bs))
+        ms_1 = timed(lambda: T.ttv_array(first_mode, A, bfirst, out=c1))
+        ms_s = timed(lambda: T.ttvs(q, A, bs, fused=False))
+        c = T.ttvs(q, A, bs).cpu().numpy()
+        ref, absn = oracle.ttvs_truth(q, A.view(-1).cpu().numpy(), na, [4, 3, 2, 1],
+                                      [b.cpu().numpy() for b in bs])
+        b_chain = 4 * (A.numel() + na[q - 1])
+        b_first = 4 * (A.numel() + c1.numel())
+        res[f"q{q}"] = {"fused_GBps": round(b_chain / ms_f / 1e6, 1),
+                        "first_ttv_GBps": round(b_first / ms_1 / 1e6, 1),
+                        "fused_ms": round(ms_f, 4), "first_ttv_ms": round(ms_1, 4),
+                        "step_by_step_ms": round(ms_s, 4),
+                        "max_rel_err": oracle.rel_error(c, ref, absn)}
+        tot["fused"] += ms_f
+        tot["first_ttv"] += ms_1
+        tot["step_by_step"] += ms_s
+        nbytes += b_chain
+    return {"workload": "ttvs (every mode but q) on a 128^4 fp32 tensor (2^28 elements), "
+                        "q = 1..4, last-order layout",
+            "fused_GBps": round(nbytes / tot["fused"] / 1e6, 1),
+            "fused_over_first_ttv_time": round(tot["fused"] / tot["first_ttv"], 4),
+            "step_by_step_over_fused_time": round(tot["step_by_step"] / tot["fused"], 3),
+            "per_q": res, "bar": 1e-5}
 
 
 def traffic_per_launch(kernel, elements):

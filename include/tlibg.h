@@ -66,6 +66,10 @@ extern "C" {
                                    /*   alignment                                                   */
 #define TLIBG_KIND_COL_BULK 6      /* column GEMV (P > 1) fed by a TMA producer warp: 4 KB runs of  */
                                    /*   each row in a 3-stage shared-memory ring, any alignment     */
+#define TLIBG_KIND_ROW_PANEL 7     /* long q-fastest rows, few of them (P == 1, 16-byte aligned      */
+                                   /*   rows): a CTA holds a segment of b in registers and streams  */
+                                   /*   that segment of a block of rows, so b is read once per row  */
+                                   /*   block instead of once per row; `group` = rows in flight     */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */
@@ -181,6 +185,24 @@ int tlibg_output_layout(const size_t* pia, size_t p, size_t q, size_t* pic);
 int tlibg_strides(const size_t* n, const size_t* pi, size_t p, size_t* w);
 int tlibg_k_order_layout(size_t p, size_t k, size_t* pi);
 size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode);
+
+/* ---------------------------------------------------------------------------
+ * Multi-vector chain: contract every mode of A except q, each with its vector.
+ * Replaces: ttvpy.ttvs(q, A, bs, order) -- ttvpy/src/wrapped_ttv.cpp:85-199,
+ * which runs p - 1 TTVs one after another.  bs (HOST array of p - 1 DEVICE
+ * pointers) holds the vectors in mode order without mode q (bs[r] belongs to
+ * mode r + 1 for r < q - 1, else mode r + 2); nbs (HOST) their lengths; c
+ * (DEVICE) receives na[q-1] elements.  A is any dense layout (na, wa, pia as
+ * in the single call).  The chain reads A once, whatever order the reference
+ * would contract in: Kronecker weights of the prefix and suffix modes, a row
+ * contraction over the prefix, a column contraction over the suffix -- no
+ * host synchronisation; intermediates in the stream's cached scratch.  Same
+ * messages as ttvpy for bad q, order or vector lengths.  dtype TLIBG_BF16A:
+ * A bfloat16, vectors and c float.
+ * ------------------------------------------------------------------------- */
+int tlibg_ttvs(int dtype, size_t q, size_t p,
+               const void* a, const size_t* na, const size_t* wa, const size_t* pia,
+               const void* const* bs, const size_t* nbs, void* c, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free fp32 TTV.  No counterpart in the reference.

@@ -144,6 +144,10 @@ def lib() -> C.CDLL:
             f = getattr(L, name)
             f.restype = None
             f.argtypes = [_u64, _u64, _u64, _vp, _vp, _vp, _vp]
+        for name in ("orc_truth_ttvs_f32", "orc_truth_ttvs_f64", "orc_truth_ttvs_bf16a"):
+            f = getattr(L, name)
+            f.restype = None
+            f.argtypes = [_u64, _u64, _u64, _vp, _vp, _vp, _vp, _vp]
         L.orc_is_valid_shape.argtypes = [_psz, _sz]
         L.orc_is_valid_layout.argtypes = [_psz, _sz]
         L.orc_is_valid_strides.argtypes = [_psz, _sz, _psz]
@@ -340,6 +344,40 @@ def truth(S, nq, P, a, b, kind=None):
     else:
         lib().orc_truth_f64(S, nq, P, _data(a), _data(b.astype(np.float64)), _data(ref_),
                             _data(absn))
+    return ref_, absn
+
+
+def kron_weights(na, pia, q, bs):
+    """Kronecker weights (wS, wP) in double of the suffix and prefix modes of
+    the canonical view w.r.t. q; bs in mode order without mode q."""
+    vec = {}
+    r = 0
+    for m in range(1, len(na) + 1):
+        if m == q:
+            continue
+        vec[m] = np.asarray(bs[r], dtype=np.float64)
+        r += 1
+    k = list(pia).index(q)
+    wP = np.ones(1)
+    for m in pia[:k]:           # prefix modes, fastest first: each new mode is slower
+        wP = np.kron(vec[m], wP)
+    wS = np.ones(1)
+    for m in pia[k + 1:]:
+        wS = np.kron(vec[m], wS)
+    return wS, wP
+
+
+def ttvs_truth(q, a, na, pia, bs, kind=None):
+    """Double-double truth of the chain ttvs(q, A, bs) (every mode but q
+    contracted) and sum |a w| per output, for A dense in layout pia."""
+    P, nq, S = canonical(na, pia, q)
+    wS, wP = kron_weights(na, pia, q, bs)
+    a = np.ascontiguousarray(a)
+    ref_ = np.empty(nq, dtype=np.float64)
+    absn = np.empty(nq, dtype=np.float64)
+    f = (lib().orc_truth_ttvs_bf16a if (kind == "bf16a" or a.dtype == np.uint16) else
+         lib().orc_truth_ttvs_f32 if a.dtype == np.float32 else lib().orc_truth_ttvs_f64)
+    f(S, nq, P, _data(a), _data(wS), _data(wP), _data(ref_), _data(absn))
     return ref_, absn
 
 

@@ -528,3 +528,38 @@ static inline double load_bf16(uint16_t v)
 ORC_DEFINE_TRUTH(orc_truth_f32, float, float, load_f32, 1)
 ORC_DEFINE_TRUTH(orc_truth_f64, double, double, load_f64, 0)
 ORC_DEFINE_TRUTH(orc_truth_bf16a, uint16_t, float, load_bf16, 1)
+
+/* ------------------------------------------------------------------------ */
+/* truth of the multi-vector chain (ttvpy.ttvs, wrapped_ttv.cpp:85-199):     */
+/* every mode but q contracted.  In the canonical (S, nq, P) view of A,      */
+/* c[i] = sum_s sum_j A[s, i, j] wS[s] wP[j] with wS, wP the Kronecker       */
+/* products of the suffix and prefix vectors (given in double).  Each        */
+/* product a * (wS wP) is added exactly (TwoProduct) into a double-double    */
+/* sum per output; absn = sum |a wS wP|.                                     */
+/* ------------------------------------------------------------------------ */
+#define ORC_DEFINE_TRUTH_TTVS(NAME, TA, LOADA, EXACT_PRODUCT)                               \
+void NAME(uint64_t S, uint64_t nq, uint64_t P, const TA* a, const double* wS,               \
+          const double* wP, double* ref, double* absn)                                      \
+{                                                                                           \
+    _Pragma("omp parallel for schedule(dynamic, 1)")                                        \
+    for (uint64_t i = 0; i < nq; ++i) {                                                     \
+        double hi = 0.0, lo = 0.0, an = 0.0;                                                \
+        for (uint64_t s = 0; s < S; ++s) {                                                  \
+            const TA* row = a + (s * nq + i) * P;                                           \
+            for (uint64_t j = 0; j < P; ++j) {                                              \
+                const double w = wS[s] * wP[j];                                             \
+                const double av = LOADA(row[j]);                                            \
+                const double pr = av * w;                                                   \
+                const double pe = fma(av, w, -pr);                                          \
+                dd_add(&hi, &lo, pr, pe);                                                   \
+                an += fabs(pr);                                                             \
+            }                                                                               \
+        }                                                                                   \
+        ref[i] = hi + lo;                                                                   \
+        absn[i] = an;                                                                       \
+    }                                                                                       \
+}
+
+ORC_DEFINE_TRUTH_TTVS(orc_truth_ttvs_f32, float, load_f32, 1)
+ORC_DEFINE_TRUTH_TTVS(orc_truth_ttvs_f64, double, load_f64, 0)
+ORC_DEFINE_TRUTH_TTVS(orc_truth_ttvs_bf16a, uint16_t, load_bf16, 1)

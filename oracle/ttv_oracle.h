@@ -92,4 +92,13 @@ int orc_num_threads(void);
 #ifdef __cplusplus
 }
 #endif
+/* truth of the multi-vector chain (every mode but q), canonical (S, nq, P)
+ * view of A, Kronecker weights wS (S) and wP (P) in double */
+void orc_truth_ttvs_f32(uint64_t S, uint64_t nq, uint64_t P, const float* a, const double* wS,
+                        const double* wP, double* ref, double* absn);
+void orc_truth_ttvs_f64(uint64_t S, uint64_t nq, uint64_t P, const double* a, const double* wS,
+                        const double* wP, double* ref, double* absn);
+void orc_truth_ttvs_bf16a(uint64_t S, uint64_t nq, uint64_t P, const uint16_t* a, const double* wS,
+                          const double* wP, double* ref, double* absn);
+
 #endif

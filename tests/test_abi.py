@@ -271,12 +271,64 @@ def test_ttvs_contraction_order(engine, monkeypatch):
         for d, bj in sorted(zip(dims, B), key=lambda t: -t[0]):
             D = torch.tensordot(D, bj, dims=([d], [0]))
         for order in ("forward", "backward", "optimal"):
-            Cq = engine.ttvs(q, A, B, order)
+            Cq = engine.ttvs(q, A, B, order, fused=False)
             assert torch.equal(Cq, D), (q, order)
     with pytest.raises(ValueError, match="multiplication order"):
         engine.ttvs(1, A, B, "sideways")
     with pytest.raises(ValueError, match="number of input vectors"):
         engine.ttvs(1, A, B[:2])
+
+
+def test_ttvs_entry_point_checks(engine):
+    """tlibg_ttvs refuses bad calls with ttvpy's messages before touching memory."""
+    import ctypes as C
+    lib = engine.library()
+    buf = (C.c_float * 64)()
+    vec = (C.c_void_p * 3)(C.addressof(buf), C.addressof(buf), C.addressof(buf))
+
+    def call(q, p, na, nbs, pia=None):
+        pia = pia or list(range(1, p + 1))
+        wa = engine.strides(na, pia) if p else [1]
+        keep = [engine._sizes(v) for v in (na or [1], wa, pia or [1], nbs or [1])]
+        st = lib.tlibg_ttvs(engine.F32, q, p, C.addressof(buf), engine._p(keep[0]), engine._p(keep[1]),
+                            engine._p(keep[2]), vec, engine._p(keep[3]), C.addressof(buf), None)
+        return st, engine._last_error()
+
+    assert call(1, 0, [], []) == (engine.ERR_ARGUMENT, "Error calling ttvpy::ttvs: input tensor "
+                                  "order should be greater than zero.")
+    st, msg = call(5, 4, [2, 3, 4, 5], [2, 3, 4])
+    assert st == engine.ERR_ARGUMENT and "contraction mode should be greater than zero" in msg
+    st, msg = call(2, 4, [2, 3, 4, 5], [2, 4, 4])
+    assert st == engine.ERR_ARGUMENT and msg == ("Error calling ttvpy::ttvs: vector dimension is not "
+                                                 "compatible with the dimension of a tensor mode.")
+    st, msg = call(1, 1, [7], [])
+    assert st == engine.ERR_ARGUMENT and "order 1" in msg
+    # a valid call gets as far as the device (none here)
+    import torch
+    if not torch.cuda.is_available():
+        st, msg = call(2, 4, [2, 3, 4, 5], [2, 4, 5])
+        assert st in (engine.ERR_CUDA, engine.ERR_ARGUMENT), msg
+
+
+def test_ttvs_truth_matches_einsum(orc):
+    """The oracle's chain truth (Kronecker weights, double-double sum) against
+    float64 tensordot chains, for first- and last-order layouts."""
+    rng = np.random.default_rng(8)
+    na = [5, 3, 4, 6]
+    A = rng.uniform(-1, 1, int(np.prod(na)))
+    for pia in ([1, 2, 3, 4], [4, 3, 2, 1], [2, 4, 1, 3]):
+        # the tensor with layout pia: element (i1..i4) at sum i_r w_r
+        wa = orc.strides(na, pia)
+        T = np.zeros(na)
+        for idx in np.ndindex(*na):
+            T[idx] = A[sum(i * w for i, w in zip(idx, wa))]
+        for q in range(1, 5):
+            bs = [rng.uniform(-1, 1, na[m]) for m in range(4) if m != q - 1]
+            D = T
+            for d, bj in sorted(zip([m for m in range(4) if m != q - 1], bs), key=lambda t: -t[0]):
+                D = np.tensordot(D, bj, axes=([d], [0]))
+            ref, absn = orc.ttvs_truth(q, A, na, pia, bs)
+            assert np.allclose(ref, D, rtol=0, atol=1e-13), (pia, q)
 
 
 def test_validate_only_entry_point(engine):

@@ -571,6 +571,64 @@ def test_row_tile_kernel(engine, orc, torch_dev):
                    kind=engine.KIND_ROW_TILE)
 
 
+def test_row_panel_kernel(engine, orc, torch_dev):
+    """Long q-fastest rows through the row-panel kernel (b's segment held in
+    registers across a block of rows): n_q a few segments long, not a multiple
+    of the segment, S from 1 to past the row-block split, rows in flight 1 and
+    2, fp32 (compensated and plain), fp64 (mix, native), bf16-stored A; the
+    planner takes it by default from 2^20 elements of b; refused for rows
+    without 16-byte vectors."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(77)
+    cases = [(4096 * 3 + 4, 1), (4096 * 5, 7), (4096 * 2 + 36, 64), (1 << 16, 513), (70000, 3)]
+    for nq, S in cases:
+        na, pia, q = [nq, S], [1, 2], 1
+        N = nq * S
+        for dt in (np.float32, np.float64):
+            if nq % (16 // np.dtype(dt).itemsize):
+                continue
+            tdt = torch.float32 if dt == np.float32 else torch.float64
+            a = rng.uniform(-1, 1, N).astype(dt)
+            b = rng.uniform(-1, 1, nq).astype(dt)
+            da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+            dc = torch.empty(S, dtype=tdt, device=dev)
+            truth = orc.truth(S, nq, 1, a, b)
+            seg = 4096 if dt == np.float32 else 2048
+            if nq <= seg:
+                continue
+            for acc in (engine.ACC_COMPENSATED, engine.ACC_PLAIN):
+                for rr in (1, 2):
+                    dc.fill_(float("nan"))
+                    engine.ttv(q, 2, da, na, [1, nq], pia, db, [nq], dc, [S], [1], [1],
+                               kind=engine.KIND_ROW_PANEL, group=rr, accumulate=acc, sync=True)
+                    err = orc.rel_error(dc.cpu().numpy(), *truth)
+                    assert err <= TOL[dt], (nq, S, dt, acc, rr, err)
+    # bf16-stored A (segments of 8192 elements)
+    for nq, S in ((8192 * 2 + 8, 5), (1 << 15, 40)):
+        a32 = rng.uniform(-1, 1, nq * S).astype(np.float32)
+        b = rng.uniform(-1, 1, nq).astype(np.float32)
+        abf = torch.from_numpy(a32).to(torch.bfloat16)
+        bits = abf.view(torch.int16).numpy().view(np.uint16).copy()
+        dc = torch.empty(S, dtype=torch.float32, device=dev)
+        engine.ttv(1, 2, abf.to(dev).view(torch.int16), [nq, S], [1, nq], [1, 2],
+                   torch.from_numpy(b).to(dev), [nq], dc, [S], [1], [1],
+                   dtype=engine.BF16A, kind=engine.KIND_ROW_PANEL, sync=True)
+        refb, absnb = orc.truth(S, nq, 1, bits, b, kind="bf16a")
+        assert orc.rel_error(dc.cpu().numpy(), refb, absnb) <= 1e-5
+    # the planner's default for long rows; the asymmetric sweep's order-3 case q = 1
+    assert engine.plan(1, [1 << 24, 4, 4], [1, 2, 3])["kind"] == engine.KIND_ROW_PANEL
+    assert engine.plan(1, [1 << 16, 64], [1, 2])["kind"] == engine.KIND_ROW
+    na = [1 << 22, 6]
+    a = rng.uniform(-1, 1, (1 << 22) * 6).astype(np.float32)
+    b = rng.uniform(-1, 1, 1 << 22).astype(np.float32)
+    c, err = check(orc, engine, torch, dev, 1, na, [1, 2], a, b)
+    # refused where it does not apply
+    with pytest.raises(engine.TTVError):
+        engine.ttv(1, 2, torch.zeros(8190 * 4, device=dev), [8190, 4], [1, 8190], [1, 2],
+                   torch.zeros(8190, device=dev), [8190], torch.zeros(4, device=dev), [4], [1], [1],
+                   kind=engine.KIND_ROW_PANEL)
+
+
 def test_short_contraction_column_kernel(engine, orc, torch_dev):
     """Column form with n_q <= 4 and vector loads: two tiles per thread, every row
     loaded before any product; odd and even tile counts, one slice and many,

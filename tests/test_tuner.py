@@ -28,7 +28,10 @@ def test_candidates_row_form(T):
     assert sorted({c["group"] for c in cands if c.get("kind") == T.KIND_ROW}) == [1, 2, 4, 8, 16, 32]
     # long rows: no streamed or row-tile candidates (a row must fit a 16 KB stage / 64 elements)
     long_ = TU.candidates(T.F32, 1, 1 << 16, 64)
-    assert {c.get("kind") for c in long_[1:]} == {T.KIND_ROW}
+    assert {c.get("kind") for c in long_[1:]} == {T.KIND_ROW, T.KIND_ROW_PANEL}
+    # the row-panel kernel needs rows of whole 16-byte vectors longer than one segment
+    assert T.KIND_ROW_PANEL not in {c.get("kind") for c in TU.candidates(T.F32, 1, (1 << 16) + 1, 64)}
+    assert T.KIND_ROW_PANEL not in {c.get("kind") for c in TU.candidates(T.F32, 1, 4096, 64)}
     # fp64 adds the double-float accumulation to every row candidate
     f64 = TU.candidates(T.F64, 1, 48, 1 << 20)
     assert {c.get("accumulate") for c in f64 if c.get("kind") == T.KIND_ROW} == {0, T.ACC_DOUBLE_FLOAT}

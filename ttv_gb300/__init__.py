@@ -30,7 +30,7 @@ __all__ = [
     "library", "library_path", "launch_count", "device_error", "device_alloc_count",
     "plan_hint", "clear_plan_hint", "F32", "F64", "BF16A",
     "ACC_COMPENSATED", "ACC_PLAIN", "ACC_DOUBLE_FLOAT", "KIND_ROW", "KIND_COL", "KIND_STREAM",
-    "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE", "KIND_COL_BULK",
+    "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE", "KIND_COL_BULK", "KIND_ROW_PANEL",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -38,8 +38,8 @@ LIB_PATH = os.path.join(HERE, "libttvgpu.so")
 
 F32, F64, BF16A = 0, 1, 2
 ACC_COMPENSATED, ACC_PLAIN, ACC_DOUBLE_FLOAT = 0, 1, 2
-KIND_ROW, KIND_COL, KIND_STREAM, KIND_COL_REALIGN, KIND_COL_THIN, KIND_ROW_TILE, KIND_COL_BULK = \
-    0, 1, 2, 3, 4, 5, 6
+KIND_ROW, KIND_COL, KIND_STREAM, KIND_COL_REALIGN, KIND_COL_THIN, KIND_ROW_TILE, KIND_COL_BULK, \
+    KIND_ROW_PANEL = 0, 1, 2, 3, 4, 5, 6, 7
 OK, ERR_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = range(6)
 
 
@@ -112,6 +112,9 @@ def library() -> C.CDLL:
         L.tlibg_last_error.argtypes = [C.c_char_p, _sz]
         L.tlibg_device_error.restype = C.c_int
         L.tlibg_launch_count.restype = C.c_uint64
+        L.tlibg_ttvs.restype = C.c_int
+        L.tlibg_ttvs.argtypes = [C.c_int, _sz, _sz, _vp, _psz, _psz, _psz, C.POINTER(_vp), _psz,
+                                 _vp, _vp]
         L.tlibg_device_alloc_count.restype = C.c_uint64
         L.tlibg_plan_hint.restype = C.c_int
         L.tlibg_plan_hint.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64,
@@ -377,11 +380,16 @@ def ttv_array(q, A, b, *, out=None, stream=None, **opts):
     return out
 
 
-def ttvs(q, A, bs, order="optimal", *, stream=None, **opts):
+def ttvs(q, A, bs, order="optimal", *, stream=None, fused=True, **opts):
     """``ttvpy.ttvs(q, A, bs, order)``: contract every mode except q with the
     vectors bs (one per mode r != q, in mode order), in "forward",
     "backward" or "optimal" (largest vector first) order
-    (wrapped_ttv.cpp:85-199).  Returns a vector of length A.shape[q-1]."""
+    (wrapped_ttv.cpp:85-199).  Returns a vector of length A.shape[q-1].
+
+    By default the chain runs fused in the engine (``tlibg_ttvs``): A is read
+    once whatever the order, which then only names the reference's rounding
+    sequence.  ``fused=False`` (or any kernel option) runs the reference's
+    step-by-step chain, one engine TTV per vector in the given order."""
     if order not in ("optimal", "backward", "forward"):
         raise ValueError("Error calling ttvpy::ttvs: multiplication order should be either "
                          "'optimal', 'backward' or 'forward'.")
@@ -401,6 +409,8 @@ def ttvs(q, A, bs, order="optimal", *, stream=None, **opts):
     if nb[:q - 1] != na[:q - 1] or nb[q - 1:] != na[q:]:
         raise ValueError("Error calling ttvpy::ttvs: vector dimension is not compatible with the "
                          "dimension of a tensor mode.")
+    if fused and not opts and p > 1:
+        return _ttvs_fused(q, A, bs, stream)
     # modes contracted, as (one-based mode of A, vector)
     pairs = [(r, bs[r - 1]) for r in range(1, q)] + [(r, bs[r - 2]) for r in range(q + 1, p + 1)]
     if order == "backward":
@@ -418,3 +428,24 @@ def ttvs(q, A, bs, order="optimal", *, stream=None, **opts):
         C_ = ttv_array(cur, C_, bj, stream=stream, **opts)
         remaining.remove(r)
     return C_
+
+
+def _ttvs_fused(q, A, bs, stream):
+    torch = _torch()
+    p = A.dim()
+    if not A.is_contiguous():
+        A = A.contiguous()
+    dt = BF16A if A.dtype == torch.bfloat16 else (F64 if A.dtype == torch.float64 else F32)
+    vdt = torch.float64 if dt == F64 else torch.float32
+    vecs = [bj.to(device=A.device, dtype=vdt).contiguous() for bj in bs]
+    na = list(A.shape)
+    pia = list(range(p, 0, -1))
+    wa = list(A.stride())
+    out = torch.empty(na[q - 1], dtype=vdt, device=A.device)
+    keep = [_sizes(v) for v in (na, wa, pia, [int(v.shape[0]) for v in vecs])]
+    ptrs = (_vp * len(vecs))(*[v.data_ptr() for v in vecs])
+    a_ptr = A.view(torch.int16) if dt == BF16A else A
+    st = library().tlibg_ttvs(dt, q, p, _ptr(a_ptr), _p(keep[0]), _p(keep[1]), _p(keep[2]), ptrs,
+                              _p(keep[3]), out.data_ptr(), _stream_handle(stream))
+    _raise(st)
+    return out

@@ -454,6 +454,47 @@ int make_row_tile_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int s
     return TLIBG_OK;
 }
 
+// Row-panel kernel: items (segment of b, block of rows); row blocks only as
+// many as it takes to give the grid about two items per CTA.
+// Rows in flight: two for fp32 (64 registers, no spill); one for fp64 and
+// bf16-stored A, whose second row spills.
+#ifndef TLIBG_ROW_PANEL_RR
+#define TLIBG_ROW_PANEL_RR(dtype) ((dtype) == F32 ? 2 : 1)
+#endif
+int make_row_panel_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
+{
+    const int vmax = (int)(16 / elem_size_a(pl.dtype));
+    if (opt && opt->vec > 0 && opt->vec != vmax)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-panel kernel loads 16 bytes per vector");
+    if (opt && opt->split > 0)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-panel kernel splits the contracted mode into "
+                                        "segments of its own");
+    const int rr = (opt && opt->group > 0) ? opt->group : TLIBG_ROW_PANEL_RR(pl.dtype);
+    if (rr != 1 && rr != 2)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: rows in flight of the row-panel kernel must be 1 or 2");
+    pl.kind = KIND_ROW_PANEL;
+    pl.vec = vmax;
+    pl.group = rr;
+    pl.rows_m = rr;
+    const uint64_t L = row_panel_seg(pl.dtype);
+    const uint64_t nseg = cdiv(cn.nq, L);
+    const int cps = std::max(1, plan_ctas_per_sm(pl));
+    const uint64_t grid_full = (uint64_t)sms * cps;
+    uint64_t nrb = 1;
+    if (nseg < 2 * grid_full) nrb = std::min<uint64_t>(cn.S, cdiv(2 * grid_full, nseg));
+    const uint64_t rbk = cdiv(cn.S, nrb);
+    nrb = cdiv(cn.S, rbk);
+    pl.seg_len = L;
+    pl.split = (int)nseg;
+    pl.items = nseg * nrb;
+    pl.items_per_cta = rbk;
+    pl.grid = (int)std::min<uint64_t>(grid_full, pl.items);
+    pl.f64_combine = (pl.dtype != F64) && cn.nq > (uint64_t(1) << 20);
+    pl.smem = plan_smem_bytes(pl);
+    *out = pl;
+    return TLIBG_OK;
+}
+
 int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
                     int sms, Plan* out)
 {
@@ -489,6 +530,22 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     if (opt && opt->kind == KIND_COL_BULK && cn.P == 1)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: the TMA-staged column kernel needs prefix P > 1");
     if (opt && opt->kind == KIND_COL_BULK) return make_col_bulk_plan(pl, cn, opt, sms, out);
+    // Long q-fastest rows with 16-byte loads (at least two segments of b): the
+    // row-panel kernel holds b's segment in registers across a block of rows.
+    // Default from 2^20 elements of b (4 MB fp32): rows that long come few to a
+    // tensor, and b no longer shares L2 with the stream of A.
+    const bool panel_ok = cn.P == 1 && cn.nq % (16 / ea) == 0 && aligned(a, 16) && aligned(b, 16) &&
+                          cn.nq > row_panel_seg(dtype);
+    if (opt && opt->kind == KIND_ROW_PANEL) {
+        if (!panel_ok)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-panel kernel needs prefix P == 1, rows of "
+                                            "16-byte vectors on 16-byte aligned A and b, and n_q longer "
+                                            "than one segment of b");
+        return make_row_panel_plan(pl, cn, opt, sms, out);
+    }
+    const bool kernel_choice_free = !(opt && (opt->kind >= 0 || opt->group > 0 || opt->vec > 0 || opt->split > 0));
+    if (panel_ok && cn.nq >= (uint64_t(1) << 20) && kernel_choice_free)
+        return make_row_panel_plan(pl, cn, opt, sms, out);
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
         opt->kind != KIND_COL_THIN && opt->kind != KIND_ROW_TILE && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
@@ -1392,6 +1449,7 @@ int internal_check_device_pointers(const void* a, const void* b, const void* c)
 }
 int internal_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
 cudaError_t internal_malloc(void** p, size_t bytes) { return device_malloc(p, bytes); }
+int internal_scratch(cudaStream_t stream, size_t bytes, void** out) { return get_scratch(stream, bytes, out); }
 void internal_count_launches(uint64_t n) { g_launches += n; }
 
 }  // namespace tlibg

@@ -44,6 +44,9 @@ int internal_cuda_fail(cudaError_t e, const char* where);
 // cudaMalloc, counted by tlibg_device_alloc_count (every device allocation of
 // the library goes through it).
 cudaError_t internal_malloc(void** p, size_t bytes);
+// The calling stream's cached device scratch (grow-only, per device and
+// stream), at least `bytes` long; 256-byte aligned.
+int internal_scratch(cudaStream_t stream, size_t bytes, void** out);
 void internal_count_launches(uint64_t n);
 
 }  // namespace tlibg

@@ -715,6 +715,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 #include "ttv_strided.cuh"
 #include "ttv_rowtile.cuh"
 #include "ttv_colbulk.cuh"
+#include "ttv_rowpanel.cuh"
 
 namespace tlibg {
 
@@ -741,6 +742,10 @@ static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
     if (kind == KIND_COL_BULK) return col_bulk_kernel<TA, T, KAHAN>;
+    if (kind == KIND_ROW_PANEL) {
+        if (vec != VMAX) return nullptr;
+        return rows_m == 2 ? row_panel_kernel<TA, T, VMAX, KAHAN, 2> : row_panel_kernel<TA, T, VMAX, KAHAN, 1>;
+    }
     if (kind == KIND_ROW_TILE) {
         switch (rows_m) {
         case 1: return row_tile_kernel<TA, T, KAHAN, 1>;
@@ -854,6 +859,7 @@ size_t plan_smem_bytes(const Plan& p)
                (size_t)ROWT_WARPS * ROWT_NS * rowt_slot_bytes(p.nq, ea, p.rows_m);
     }
     if (p.kind == KIND_COL && p.rows_m == 1) return 0;   // short contraction: b in registers
+    if (p.kind == KIND_ROW_PANEL) return 0;               // b in registers, static reduction buffer
     if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements
         return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.group > 1 && p.nq <= (uint64_t)ROW_SPLIT_MAX)
                    ? ROW_SPLIT_MAX * 8 : 0;
@@ -960,6 +966,8 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
         k.ntiles = plan.S;
     } else if (plan.kind == KIND_COL_BULK) {
         k.ntiles = (plan.P + col_bulk_tile(plan.dtype) - 1) / col_bulk_tile(plan.dtype);   // tiles per slice
+    } else if (plan.kind == KIND_ROW_PANEL) {
+        k.ntiles = (plan.S + plan.items_per_cta - 1) / plan.items_per_cta;   // row blocks per segment
     } else if (plan.kind == KIND_COL && plan.rows_m == 1) {
         k.ntiles = 0;   // pairs of tiles of BLOCK * V outputs are the items
     } else if (plan.kind == KIND_COL || plan.kind == KIND_COL_REALIGN) {

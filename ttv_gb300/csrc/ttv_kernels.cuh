@@ -9,7 +9,7 @@ namespace tlibg {
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
 enum Kind {
     KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4, KIND_ROW_TILE = 5,
-    KIND_COL_BULK = 6
+    KIND_COL_BULK = 6, KIND_ROW_PANEL = 7
 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
@@ -40,6 +40,10 @@ __host__ __device__ inline size_t rowt_slot_bytes(uint64_t nq, size_t ea, int R)
 {
     return (size_t)((32 * (uint64_t)R * nq * ea + 16 + 15) & ~uint64_t(15));
 }
+// Row-panel kernel: vectors of b each thread holds in registers; a segment is
+// RP_K * BLOCK vectors.
+constexpr int RP_K = 4;
+inline uint64_t row_panel_seg(int dtype) { return (uint64_t)RP_K * BLOCK * (dtype == F64 ? 2 : (dtype == BF16A ? 8 : 4)); }
 // Outputs per tile of the TMA-staged column kernel (4 KB of A per row).
 inline uint64_t col_bulk_tile(int dtype) { return (uint64_t)CB_ROW_BYTES / (dtype == F64 ? 8 : (dtype == BF16A ? 2 : 4)); }
 // Rows per lane of a row tile: enough that a tile holds about 4 KB of A.
@@ -60,12 +64,13 @@ struct Plan {
     int kahan = 1;        // compensated fp32 accumulation
     int rows_m = 0;       // ROW: 1 or 2 = short-row kernel (at most rows_m vectors per lane of a row);
                           // COL: 1 = short-contraction kernel (n_q <= CS_MAXQ, two tiles per thread);
-                          // ROW_TILE: rows per lane (1, 2 or 4)
+                          // ROW_TILE: rows per lane (1, 2 or 4); ROW_PANEL: rows in flight (1 or 2)
     int mo = 1;           // COL with scalar loads: outputs per thread, 32 apart (strided kernel when > 1)
     uint64_t P = 1, nq = 1, S = 1;
     uint64_t seg_len = 1;
-    uint64_t items = 0;          // work items (ROW: rows x segments; COL: tiles x segments)
-    uint64_t items_per_cta = 0;  // COL: contiguous block of items per CTA
+    uint64_t items = 0;          // work items (ROW: rows x segments; COL: tiles x segments;
+                                 //   ROW_PANEL: segments x row blocks)
+    uint64_t items_per_cta = 0;  // COL: contiguous block of items per CTA; ROW_PANEL: rows per row block
     int grid = 1;
     int sms = 0;                 // streaming multiprocessors of the device planned for
     size_t smem = 0;

@@ -21,7 +21,8 @@ import sys
 
 import numpy as np
 
-from . import F32, F64, KIND_COL, KIND_COL_BULK, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_TILE, KIND_STREAM, \
+from . import F32, F64, KIND_COL, KIND_COL_BULK, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_PANEL, KIND_ROW_TILE, \
+    KIND_STREAM, \
     ACC_DOUBLE_FLOAT, \
     clear_plan_hint, output_layout, output_shape, plan, plan_hint, strides, ttv
 
@@ -43,6 +44,9 @@ def candidates(dtype, P, nq, S):
         if nq <= 64:
             for acc in accs:
                 out.append({"kind": KIND_ROW_TILE, "accumulate": acc})
+        if nq % (16 // es) == 0 and nq > 1024 * (16 // es):   # longer than one segment of b
+            for rr in (1, 2):
+                out.append({"kind": KIND_ROW_PANEL, "group": rr})
     else:
         min_split = -(-nq // (16384 // es))
         kinds = (KIND_COL, KIND_COL_REALIGN) if P % (16 // es) else (KIND_COL,)
