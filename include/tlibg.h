@@ -69,7 +69,7 @@ extern "C" {
 #define TLIBG_KIND_ROW_PANEL 7     /* long q-fastest rows, few of them (P == 1, 16-byte aligned      */
                                    /*   rows): a CTA holds a segment of b in registers and streams  */
                                    /*   that segment of a block of rows, so b is read once per row  */
-                                   /*   block instead of once per row; `group` = rows in flight     */
+                                   /*   block; `group` = rows in flight.  On request only           */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */
@@ -252,7 +252,12 @@ typedef struct tlibg_problem {
 #define TLIBG_SELECT_LEARNED   1  /* cost-model MLP scores every variant on the device         */
 #define TLIBG_SELECT_FIXED     2  /* every problem runs `variant`                              */
 #define TLIBG_SELECT_GIVEN     3  /* per-problem `variants` (e.g. from exhaustive tuning)      */
-#define TLIBG_NVARIANT 8
+/* Variants of a batched problem: v = 2 g + s for v < 8 (row form: 1 << g lanes
+ * per row; column form: 1 << g warps along q; s = 1: q split into up to four
+ * segments); v = 8: q-fastest rows of at most 64 elements staged through
+ * shared memory by TMA bulk copies, one lane per row (row form only; a
+ * column problem given it runs the fixed rule's variant). */
+#define TLIBG_NVARIANT 9
 
 typedef struct tlibg_batch_options {
     int select;            /* TLIBG_SELECT_*; LEARNED without a model falls back to GIVEN, then HEURISTIC */
@@ -275,8 +280,10 @@ int tlibg_batch_launch(tlibg_batch* batch, void* stream);
 /* Changes the forced variant of a TLIBG_SELECT_FIXED batch created with
  * no_graph (the autotuner's loop over variants). */
 int tlibg_batch_set_variant(tlibg_batch* batch, int variant);
-/* SM clock cycles each problem's work units took in the last launch of a
- * batch created with record_costs (the autotuner's per-problem cost inside
+/* SM cycles each problem's work units took in the last launch of a batch
+ * created with record_costs: the units' clock cycles divided by the units
+ * resident per SM (CTAs, or warps for staged rows), so that costs of either
+ * executor add up to the launch time (the autotuner's per-problem cost inside
  * a mixed batch; synchronises). */
 int tlibg_batch_costs(tlibg_batch* batch, uint64_t* cycles, void* stream);
 /* The variant each problem ran with in the last launch (synchronises). */
@@ -307,9 +314,9 @@ unsigned int tlibg_batch_device_error(void);
  * buffers are device pointers unless stated.
  * ------------------------------------------------------------------------- */
 #define TLIBG_MLP_FEATURES 8
-#define TLIBG_MLP_IN 16
+#define TLIBG_MLP_IN 17
 #define TLIBG_MLP_HIDDEN 64
-#define TLIBG_MLP_PARAMS 9473
+#define TLIBG_MLP_PARAMS 9537
 /* loss = (1/n) sum 0.5 (f(x)-y)^2 and its gradient (grad[TLIBG_MLP_PARAMS], loss[1]) */
 int tlibg_mlp_loss_grad(const float* params, const float* x, const float* y, size_t n, float* grad,
                         float* loss, void* stream);

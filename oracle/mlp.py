@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-IN, H = 16, 64
+IN, H = 17, 64
 SIZES = [("W1", (IN, H)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)),
          ("b3", (H,)), ("W4", (H,)), ("b4", (1,))]
 NPARAMS = sum(int(np.prod(s)) for _, s in SIZES)

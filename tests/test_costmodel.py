@@ -34,9 +34,9 @@ def test_oracle_gradient_matches_finite_differences():
 
 def test_layout_constants(engine):
     from ttv_gb300 import batch as B
-    assert M.NPARAMS == B.MLP_PARAMS == 9473
+    assert M.NPARAMS == B.MLP_PARAMS == 9537
     hdr = open(os.path.join(ROOT, "include", "tlibg.h")).read()
-    assert "#define TLIBG_MLP_PARAMS 9473" in hdr
+    assert "#define TLIBG_MLP_PARAMS 9537" in hdr
     assert B.init_params(0).size == M.NPARAMS
 
 
@@ -53,16 +53,17 @@ def test_features_and_fixed_rule_on_cpu(engine):
     np.testing.assert_allclose(f[0], [3 / 8, 0.5, 4 / 24, 5 / 24, 6 / 24, 0, np.log2(3) / 16, 1],
                                rtol=1e-6)
     assert list(kind) == [1, 0, 0]   # column, row (q first), row (q first in layout 3,2,1)
-    assert all(0 <= h < 8 for h in heur)
+    assert all(0 <= h < B.NVARIANT for h in heur)
 
 
 def test_mlp_inputs_rows():
     from ttv_gb300 import batch as B
     f = np.arange(16, dtype=np.float32).reshape(2, 8)
     x = B.mlp_inputs(f)
-    assert x.shape == (16, 16)
+    nv = B.NVARIANT
+    assert x.shape == (2 * nv, 8 + nv)
     assert np.all(x[3, :8] == f[0]) and x[3, 8 + 3] == 1 and x[3, 8:].sum() == 1
-    assert np.all(x[9, :8] == f[1]) and x[9, 8 + 1] == 1
+    assert np.all(x[nv + 1, :8] == f[1]) and x[nv + 1, 8 + 1] == 1
 
 
 # ---------------------------------------------------------------- GPU
@@ -130,6 +131,8 @@ def test_learned_selection_beats_fixed_rule(engine, cuda):
     if not (os.path.exists(CM.DB_PATH) and os.path.exists(B.MODEL_PATH)):
         pytest.skip("no committed tuning database / trained model")
     d = np.load(CM.DB_PATH)
+    if d["times"].shape[1] != B.NVARIANT or np.load(B.MODEL_PATH)["params"].size != B.MLP_PARAMS:
+        pytest.skip("tuning database / model made for another variant set")
     te = d["is_test"]
     feats, times, heur = d["features"][te], d["times"][te], d["heuristic"][te]
     m = np.load(B.MODEL_PATH)

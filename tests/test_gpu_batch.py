@@ -57,24 +57,34 @@ def test_batch_every_mode(engine, orc, cuda):
             torch.cuda.synchronize()
             check_all(orc, probs, host)
         v = bt.variants()
-        assert v.shape == (150,) and v.min() >= 0 and v.max() < 8
-    # every forced variant (direct launches)
-    for var in range(8):
+        assert v.shape == (150,) and v.min() >= 0 and v.max() < B.NVARIANT
+    # every forced variant (direct launches); the staged rows only where they apply
+    _, kind, heur = B.features(probs)
+    short_rows = np.array([k == engine.KIND_ROW and na[q - 1] <= 64 for k, (na, _p, q) in zip(kind, host)])
+    assert short_rows.sum() >= 5
+    for var in range(B.NVARIANT):
         reset(probs)
         with B.Batch(probs, select=B.SELECT_FIXED, variant=var, no_graph=True) as bt:
             bt.launch()
             torch.cuda.synchronize()
             check_all(orc, probs, host)
-            assert set(bt.variants()) == {var}
-    # per-problem given variants
+            got = bt.variants()
+            if var == B.VARIANT_STAGED:
+                assert np.array_equal(got, np.where(short_rows, var, heur))
+            else:
+                assert set(got) == {var}
+    # per-problem given variants (staged rows given to column problems run the fixed rule)
     rng = np.random.default_rng(1)
-    given = rng.integers(0, 8, len(probs))
+    given = rng.integers(0, B.NVARIANT, len(probs))
+    given[short_rows] = B.VARIANT_STAGED
     reset(probs)
     with B.Batch(probs, select=B.SELECT_GIVEN, variants=given) as bt:
         bt.launch()
         torch.cuda.synchronize()
         check_all(orc, probs, host)
-        assert np.array_equal(bt.variants(), given)
+        ran = bt.variants()
+        ok = (given != B.VARIANT_STAGED) | short_rows
+        assert np.array_equal(ran[ok], given[ok]) and np.array_equal(ran[~ok], heur[~ok])
     # learned selection with an (untrained) installed model: any choice is correct
     B.set_cost_model(B.init_params(3))
     try:
@@ -133,7 +143,7 @@ def test_batch_large_problems_split(engine, orc, cuda):
         c = torch.full((N // na[q - 1],), float("nan"), device=cuda)
         probs.append(B.Problem(q, na, pia, a, b, c))
         host.append((na, pia, q))
-    for var in range(8):
+    for var in range(B.NVARIANT):
         reset(probs)
         with B.Batch(probs, select=B.SELECT_FIXED, variant=var) as bt:
             bt.launch()
@@ -156,7 +166,7 @@ def test_one_shot_and_errors(engine, orc, cuda):
     bad._keep[3][0] = 7   # nb != na[q-1]
     with pytest.raises(engine.TTVError, match="contraction dimension of A and B are not equal"):
         B.Batch([probs[1], bad])
-    with pytest.raises(engine.TTVError, match="variant must be in 0..7"):
+    with pytest.raises(engine.TTVError, match="variant must be in 0..8"):
         B.Batch(probs, select=B.SELECT_FIXED, variant=9)
 
 
@@ -177,7 +187,13 @@ def test_recorded_costs(engine, orc, cuda):
         torch.cuda.synchronize()
         c2 = bt.costs()
         check_all(orc, probs, host)
-    assert (c1 > 0).all() and (c2 > 0).all()
+        reset(probs)
+        bt.set_variant(B.VARIANT_STAGED)   # short rows staged, the rest their fixed rule
+        bt.launch()
+        torch.cuda.synchronize()
+        c3 = bt.costs()
+        check_all(orc, probs, host)
+    assert (c1 > 0).all() and (c2 > 0).all() and (c3 > 0).all()
     with B.Batch(probs) as bt:   # not recording: costs stay zero
         bt.launch()
         assert (bt.costs() == 0).all()

@@ -575,9 +575,9 @@ def test_row_panel_kernel(engine, orc, torch_dev):
     """Long q-fastest rows through the row-panel kernel (b's segment held in
     registers across a block of rows): n_q a few segments long, not a multiple
     of the segment, S from 1 to past the row-block split, rows in flight 1 and
-    2, fp32 (compensated and plain), fp64 (mix, native), bf16-stored A; the
-    planner takes it by default from 2^20 elements of b; refused for rows
-    without 16-byte vectors."""
+    2, fp32 (compensated and plain), fp64 (mix, native), bf16-stored A; on
+    request only (the planner keeps the row kernel); refused for rows without
+    16-byte vectors."""
     torch, dev = torch_dev
     rng = np.random.default_rng(77)
     cases = [(4096 * 3 + 4, 1), (4096 * 5, 7), (4096 * 2 + 36, 64), (1 << 16, 513), (70000, 3)]
@@ -615,13 +615,12 @@ def test_row_panel_kernel(engine, orc, torch_dev):
                    dtype=engine.BF16A, kind=engine.KIND_ROW_PANEL, sync=True)
         refb, absnb = orc.truth(S, nq, 1, bits, b, kind="bf16a")
         assert orc.rel_error(dc.cpu().numpy(), refb, absnb) <= 1e-5
-    # the planner's default for long rows; the asymmetric sweep's order-3 case q = 1
-    assert engine.plan(1, [1 << 24, 4, 4], [1, 2, 3])["kind"] == engine.KIND_ROW_PANEL
-    assert engine.plan(1, [1 << 16, 64], [1, 2])["kind"] == engine.KIND_ROW
+    # on request only: the planner keeps the row kernel for long rows
+    assert engine.plan(1, [1 << 24, 4, 4], [1, 2, 3])["kind"] == engine.KIND_ROW
     na = [1 << 22, 6]
     a = rng.uniform(-1, 1, (1 << 22) * 6).astype(np.float32)
     b = rng.uniform(-1, 1, 1 << 22).astype(np.float32)
-    c, err = check(orc, engine, torch, dev, 1, na, [1, 2], a, b)
+    c, err = check(orc, engine, torch, dev, 1, na, [1, 2], a, b, kind=engine.KIND_ROW_PANEL)
     # refused where it does not apply
     with pytest.raises(engine.TTVError):
         engine.ttv(1, 2, torch.zeros(8190 * 4, device=dev), [8190, 4], [1, 8190], [1, 2],

@@ -53,6 +53,7 @@ def test_hint_install_lookup_and_precedence(T):
     na, pia, q = [645, 645, 645], [1, 2, 3], 2
     base = T.plan(q, na, pia)
     base64 = T.plan(q, na, pia, dtype=T.F64)
+    other = T.plan(2, [644, 645, 645], [1, 2, 3])
     P, nq, S = base["P"], base["nq"], base["S"]
     want = {"kind": T.KIND_COL, "group": 4, "split": 3}
     assert (base["group"], base["split"]) != (4, 3)
@@ -64,7 +65,7 @@ def test_hint_install_lookup_and_precedence(T):
     same = T.plan(2, [645, 645, 645], [1, 2, 3])
     assert same["group"] == 4
     assert T.plan(q, na, pia, dtype=T.F64) == base64
-    assert T.plan(2, [644, 645, 645], [1, 2, 3])["group"] == base["group"]
+    assert T.plan(2, [644, 645, 645], [1, 2, 3]) == other
     # explicit options win over the hint
     forced = T.plan(q, na, pia, kind=T.KIND_COL, group=2, split=1)
     assert (forced["group"], forced["split"]) == (2, 1)

@@ -20,8 +20,9 @@ from . import F32, _check_buffers, _last_error, _options, _p, _raise, _sizes, li
     output_layout, output_shape, strides
 
 SELECT_HEURISTIC, SELECT_LEARNED, SELECT_FIXED, SELECT_GIVEN = 0, 1, 2, 3
-NVARIANT = 8
-MLP_FEATURES, MLP_IN, MLP_HIDDEN, MLP_PARAMS = 8, 16, 64, 9473
+NVARIANT = 9
+VARIANT_STAGED = 8   # q-fastest rows of at most 64 elements through shared memory
+MLP_FEATURES, MLP_IN, MLP_HIDDEN, MLP_PARAMS = 8, 17, 64, 9537
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 MODEL_PATH = os.path.join(DATA, "cost_model.npz")
 
@@ -139,7 +140,8 @@ class Batch:
         _raise(_lib().tlibg_batch_set_variant(self._h, int(v)))
 
     def costs(self, stream=None):
-        """SM clock cycles of each problem in the last launch (record_costs batches)."""
+        """SM cycles of each problem in the last launch (record_costs batches): its
+        units' clock cycles over the CTAs (staged rows: warps) resident per SM."""
         out = np.zeros(len(self.problems), np.uint64)
         _raise(_lib().tlibg_batch_costs(self._h, out.ctypes.data_as(C.POINTER(C.c_uint64)),
                                         _stream(stream)))
@@ -208,7 +210,7 @@ def batch_device_error() -> int:
 # cost model
 # --------------------------------------------------------------------------
 def set_cost_model(params, margin=0.0):
-    """Install (numpy float32 [9473]) or clear (None) the model SELECT_LEARNED uses;
+    """Install (numpy float32 [9537]) or clear (None) the model SELECT_LEARNED uses;
     a problem leaves the fixed rule only for a predicted gain beyond ``margin``."""
     if params is None:
         _raise(_lib().tlibg_set_cost_model(None, 0, 0.0))
@@ -224,6 +226,8 @@ def load_cost_model(path=MODEL_PATH, install=True):
         return None
     d = np.load(path)
     params = d["params"].astype(np.float32)
+    if params.size != MLP_PARAMS:   # trained for another variant set: not usable
+        return None
     margin = float(d["margin"]) if "margin" in d else 0.0
     if install:
         set_cost_model(params, margin)

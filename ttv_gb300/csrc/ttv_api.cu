@@ -532,8 +532,12 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     if (opt && opt->kind == KIND_COL_BULK) return make_col_bulk_plan(pl, cn, opt, sms, out);
     // Long q-fastest rows with 16-byte loads (at least two segments of b): the
     // row-panel kernel holds b's segment in registers across a block of rows.
-    // Default from 2^20 elements of b (4 MB fp32): rows that long come few to a
-    // tensor, and b no longer shares L2 with the stream of A.
+    // On request only: measured on GB300 against the row kernel (whose
+    // segment-major walk already has the rows of one b segment read together)
+    // on the asymmetric sweep's q = 1 rows, 10 back-to-back launches each:
+    // 4 x 2^26 floats 4.45 (rows in flight 1) / 4.37 (2) against 4.89 TB/s,
+    // 16 x 2^24 6.02 / 6.11 against 6.05, 64 x 2^22 5.80 / 5.88 against 6.10,
+    // 256 x 2^20 5.14 / 5.29 against 6.12.
     const bool panel_ok = cn.P == 1 && cn.nq % (16 / ea) == 0 && aligned(a, 16) && aligned(b, 16) &&
                           cn.nq > row_panel_seg(dtype);
     if (opt && opt->kind == KIND_ROW_PANEL) {
@@ -543,9 +547,6 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
                                             "than one segment of b");
         return make_row_panel_plan(pl, cn, opt, sms, out);
     }
-    const bool kernel_choice_free = !(opt && (opt->kind >= 0 || opt->group > 0 || opt->vec > 0 || opt->split > 0));
-    if (panel_ok && cn.nq >= (uint64_t(1) << 20) && kernel_choice_free)
-        return make_row_panel_plan(pl, cn, opt, sms, out);
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
         opt->kind != KIND_COL_THIN && opt->kind != KIND_ROW_TILE && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "

@@ -12,15 +12,22 @@
 //                 unit -> problem map and resets the queue
 //   batch_exec    persistent CTAs (SMs x occupancy) pop units from an atomic
 //                 counter; a unit is a block of rows (row form) or a tile of
-//                 the prefix over one segment of q (column form, b segment
-//                 staged by TMA); the CTA that completes a split problem's
-//                 last unit combines its partials in fixed segment order
+//                 the prefix over one segment of q (column form); the CTA
+//                 that completes a split problem's last unit combines its
+//                 partials in fixed segment order
+//   batch_rowtile persistent warps for the problems staged in shared memory
+//                 (variant 8: short q-fastest rows): each warp pops units of
+//                 tiles of 32 R rows, moves every tile into its own two-stage
+//                 ring with one TMA bulk copy and walks one row per lane from
+//                 shared memory (coalesced HBM reads, conflict-free walks)
 //
-// Variants (8): index v = 2*g + s.  Row form: lanes per row G = 1 << g;
-// column form: warps along q WI = 1 << g.  s = 1 splits q into up to 4
-// segments (two-phase, deterministic).
+// Variants (9): index v = 2*g + s for v < 8.  Row form: lanes per row
+// G = 1 << g; column form: warps along q WI = 1 << g.  s = 1 splits q into up
+// to 4 segments (two-phase, deterministic).  v = 8: row form with n_q <= 64,
+// rows staged through shared memory (batch_rowtile); not valid for columns.
 #include "ttv_device.cuh"
 #include "ttv_internal.h"
+#include "ttv_rowwalk.cuh"
 #include "ttv_mlp.cuh"
 
 #include <algorithm>
@@ -44,8 +51,15 @@ struct BProb {
     float* c;
     uint64_t P, nq, S;
     uint64_t seg_len;
-    uint64_t unit_begin;
-    uint64_t part_off;   // in BPair elements
+    uint64_t unit_begin;   // first unit of the problem in its executor's unit space
+    uint64_t part_off;     // in BPair elements
+    uint64_t tiles;        // column units: tiles per segment
+    uint64_t wbegin[2];    // weight (bytes of A) of the units before the problem's: [0] batch_exec,
+                           // [1] batch_rowtile (both prefixes for every problem)
+    uint64_t wunit;        // weight of one of the problem's units
+    IdxDiv pdiv;           // column units: output -> slice (division by P)
+    IdxDiv tdiv;           // column units: unit -> segment (division by tiles)
+    IdxDiv sdiv;           // row units: item -> row (division by the segment count)
     float feat[NFEAT];
     int kind;
     int vec;
@@ -55,15 +69,48 @@ struct BProb {
     uint32_t units;
     uint32_t valid_mask;
     int heuristic;               // the fixed rule's variant (kept unless the model beats it by the margin)
+    int staged;                  // this launch runs the problem in batch_rowtile (variant 8)
     unsigned int done;
     unsigned long long cycles;   // SM clock cycles spent on this problem's units (recording launches)
 };
 
 struct BCtl {
-    unsigned long long head;
-    unsigned long long total;
+    unsigned long long head;     // batch_exec's dynamic tail: next unit to hand out
+    unsigned long long total;    // batch_exec's units
+    unsigned long long head_r;   // the same for batch_rowtile
+    unsigned long long total_r;
+    unsigned long long wtot;     // batch_exec's total weight (bytes of A)
+    unsigned long long wtot_r;
     int record;                  // nonzero: accumulate per-problem unit cycles
 };
+
+// Share of each executor's weight handed out statically (contiguous unit
+// ranges of equal weight per CTA, or per warp for batch_rowtile, with no
+// atomics or queue latency); the rest goes through the atomic queue so that
+// the launch ends level.
+#ifndef TLIBG_BATCH_STATIC_PCT
+#define TLIBG_BATCH_STATIC_PCT 90
+#endif
+
+// Staged row units (variant 8, batch_rowtile): tiles of 32 R rows of at most
+// BRT_TILE_BYTES, BRT_TPU tiles per work unit, one two-stage ring per warp.
+constexpr int VARIANT_STAGED = 8;
+constexpr int BRT_WARPS = 4;
+constexpr int BRT_THREADS = BRT_WARPS * 32;
+constexpr int BRT_NS = 2;
+constexpr int BRT_MAX_NQ = 64;
+constexpr int BRT_TILE_BYTES = 8192;
+constexpr int BRT_SLOT = BRT_TILE_BYTES + 32;   // + the run's misalignment (< 16 bytes)
+constexpr int BRT_TPU = 8;
+constexpr size_t BRT_WARP_BYTES = (size_t)BRT_NS * (BRT_MAX_NQ * 4 + BRT_SLOT);
+constexpr size_t BRT_SMEM = 128 + BRT_WARPS * BRT_WARP_BYTES;
+// rows per lane of a tile: 32 R rows of n_q floats fill at most BRT_TILE_BYTES
+__host__ __device__ inline uint32_t brt_rows_per_lane(uint64_t nq) { return nq <= 16 ? 4u : (nq <= 32 ? 2u : 1u); }
+__host__ __device__ inline uint64_t brt_units(uint64_t nq, uint64_t S)
+{
+    const uint64_t tiles = (S + 32 * brt_rows_per_lane(nq) - 1) / (32 * brt_rows_per_lane(nq));
+    return (tiles + BRT_TPU - 1) / BRT_TPU;
+}
 
 constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
 
@@ -78,6 +125,11 @@ constexpr int BMAX_F32 = BSTAGE_BYTES / 4;
 
 __host__ __device__ inline void decode_variant(int kind, int v, uint64_t nq, int* group, uint32_t* nseg)
 {
+    if (v == VARIANT_STAGED) {   // one lane per row from shared memory, no split
+        *group = 1;
+        *nseg = 1;
+        return;
+    }
     const int gi = (v >> 1) & 3, si = v & 1;
     *group = kind == KIND_ROW ? (TLIBG_BATCH_ROW_G0 << gi) : (1 << gi);
     uint64_t ns = 1;
@@ -116,6 +168,11 @@ __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uin
 // --------------------------------------------------------------------------
 // selection: MLP score per (problem, variant), keep the argmin
 // --------------------------------------------------------------------------
+// One thread per (problem, variant slot); SELECT_LANES slots per problem (a
+// power of two >= NVARIANT, the unused ones score +inf).
+constexpr int SELECT_LANES = 16;
+static_assert(NVARIANT <= SELECT_LANES, "variant slots per problem");
+
 __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int n, const float* __restrict__ w,
                                                     float log2_count, float log2_keep)
 {
@@ -123,9 +180,9 @@ __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int 
     for (int p = threadIdx.x; p < MLP_PARAMS; p += blockDim.x) sw[p] = w[p];
     __syncthreads();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int pi = t / NVARIANT, v = t % NVARIANT;
+    const int pi = t / SELECT_LANES, v = t % SELECT_LANES;
     float score = INFINITY;
-    if (pi < n && ((pr[pi].valid_mask >> v) & 1u)) {
+    if (pi < n && v < NVARIANT && ((pr[pi].valid_mask >> v) & 1u)) {
         float x[MLP_IN];
 #pragma unroll
         for (int i = 0; i < NFEAT; ++i) x[i] = pr[pi].feat[i];
@@ -135,11 +192,11 @@ __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int 
     }
     int best = v;
     const int h = pi < n ? pr[pi].heuristic : 0;
-    // the fixed rule's predicted cost, broadcast within the problem's 8 lanes
-    const float h_score = __shfl_sync(0xffffffffu, score, (threadIdx.x & ~7u) + (unsigned)h);
-    // argmin over the 8 lanes of this problem (ties: lowest variant)
+    // the fixed rule's predicted cost, broadcast within the problem's lanes
+    const float h_score = __shfl_sync(0xffffffffu, score, (threadIdx.x & ~(unsigned)(SELECT_LANES - 1)) + (unsigned)h);
+    // argmin over the problem's lanes (ties: lowest variant)
 #pragma unroll
-    for (int off = 4; off > 0; off >>= 1) {
+    for (int off = SELECT_LANES / 2; off > 0; off >>= 1) {
         const float os = __shfl_xor_sync(0xffffffffu, score, off);
         const int ob = __shfl_xor_sync(0xffffffffu, best, off);
         if (os < score || (os == score && ob < best)) {
@@ -154,92 +211,163 @@ __global__ void __launch_bounds__(256) batch_select(BProb* __restrict__ pr, int 
 
 __global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
 {
+    // a variant a problem cannot run (the staged rows of a column problem) keeps its fixed rule
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) pr[i].variant = v;
+    if (i < n) pr[i].variant = ((pr[i].valid_mask >> v) & 1u) ? v : pr[i].heuristic;
 }
 
 // --------------------------------------------------------------------------
 // plan: units, prefix sums, unit -> problem map, queue reset (one CTA)
 // --------------------------------------------------------------------------
+constexpr int PLAN_SUMS = 5;   // batch_exec units, split partials, batch_rowtile units, their weights
+
 __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl,
-                                                   uint32_t* __restrict__ unit_map)
+                                                   uint32_t* __restrict__ unit_map, uint32_t* __restrict__ unit_map_r)
 {
-    __shared__ unsigned long long s_units[32], s_parts[32];
-    __shared__ unsigned long long carry_u, carry_p;
-    if (threadIdx.x == 0) {
-        carry_u = 0;
-        carry_p = 0;
-    }
+    __shared__ unsigned long long s_sum[PLAN_SUMS][32];
+    __shared__ unsigned long long carry[PLAN_SUMS];
+    if (threadIdx.x < PLAN_SUMS) carry[threadIdx.x] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int base = 0; base < n; base += blockDim.x) {
         const int i = base + threadIdx.x;
-        unsigned long long u = 0, pe = 0;
+        unsigned long long x[PLAN_SUMS] = {0, 0, 0, 0, 0};
         if (i < n) {
             BProb& P = pr[i];
+            if (!((P.valid_mask >> P.variant) & 1u)) P.variant = P.heuristic;   // not runnable: the fixed rule
+            P.staged = P.variant == VARIANT_STAGED ? 1 : 0;
             int group;
             uint32_t nseg;
             decode_variant(P.kind, P.variant, P.nq, &group, &nseg);
             uint64_t seg_len;
-            u = unit_count(P.kind, group, P.vec, P.P, P.nq, P.S, nseg, &seg_len);
+            const uint64_t u = unit_count(P.kind, group, P.vec, P.P, P.nq, P.S, nseg, &seg_len);
             nseg = (uint32_t)((P.nq + seg_len - 1) / seg_len);
             P.group = group;
             P.nseg = nseg;
             P.seg_len = seg_len;
-            P.units = (uint32_t)u;
             P.done = 0u;
             P.cycles = 0ull;
-            pe = nseg > 1 ? (unsigned long long)nseg * P.S * P.P : 0ull;
+            const uint64_t outputs = P.S * P.P;
+            const uint64_t abytes = 4 * outputs * P.nq;
+            if (P.kind == KIND_COL) {
+                const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * P.vec;
+                P.tiles = (outputs + TO - 1) / TO;
+                P.pdiv = make_idx_div(P.P, outputs);
+                P.tdiv = make_idx_div(P.tiles, P.tiles * nseg);
+            } else {
+                P.tiles = 0;
+                P.sdiv = make_idx_div(nseg, P.S * nseg);
+            }
+            if (P.staged) {
+                P.units = (uint32_t)brt_units(P.nq, P.S);
+                x[2] = P.units;
+            } else {
+                P.units = (uint32_t)u;
+                x[0] = u;
+                x[1] = nseg > 1 ? (unsigned long long)nseg * outputs : 0ull;
+            }
+            P.wunit = (abytes + P.units - 1) / (P.units ? P.units : 1);
+            x[P.staged ? 4 : 3] = P.wunit * P.units;
         }
         // inclusive warp scans, then across warps
-        unsigned long long xu = u, xp = pe;
+        unsigned long long y[PLAN_SUMS];
+#pragma unroll
+        for (int c = 0; c < PLAN_SUMS; ++c) y[c] = x[c];
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            const unsigned long long yu = __shfl_up_sync(0xffffffffu, xu, off);
-            const unsigned long long yp = __shfl_up_sync(0xffffffffu, xp, off);
-            if (lane >= off) {
-                xu += yu;
-                xp += yp;
+#pragma unroll
+            for (int c = 0; c < PLAN_SUMS; ++c) {
+                const unsigned long long o = __shfl_up_sync(0xffffffffu, y[c], off);
+                if (lane >= off) y[c] += o;
             }
         }
         if (lane == 31) {
-            s_units[warp] = xu;
-            s_parts[warp] = xp;
+#pragma unroll
+            for (int c = 0; c < PLAN_SUMS; ++c) s_sum[c][warp] = y[c];
         }
         __syncthreads();
         if (warp == 0) {
-            unsigned long long wu = lane < (int)(blockDim.x >> 5) ? s_units[lane] : 0ull;
-            unsigned long long wp = lane < (int)(blockDim.x >> 5) ? s_parts[lane] : 0ull;
 #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const unsigned long long yu = __shfl_up_sync(0xffffffffu, wu, off);
-                const unsigned long long yp = __shfl_up_sync(0xffffffffu, wp, off);
-                if (lane >= off) {
-                    wu += yu;
-                    wp += yp;
+            for (int c = 0; c < PLAN_SUMS; ++c) {
+                unsigned long long w = lane < (int)(blockDim.x >> 5) ? s_sum[c][lane] : 0ull;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const unsigned long long o = __shfl_up_sync(0xffffffffu, w, off);
+                    if (lane >= off) w += o;
                 }
+                s_sum[c][lane] = w;   // inclusive prefix over warps
             }
-            s_units[lane] = wu;   // inclusive prefix over warps
-            s_parts[lane] = wp;
         }
         __syncthreads();
-        const unsigned long long before_u = carry_u + (warp ? s_units[warp - 1] : 0ull) + xu - u;
-        const unsigned long long before_p = carry_p + (warp ? s_parts[warp - 1] : 0ull) + xp - pe;
+        unsigned long long before[PLAN_SUMS];
+#pragma unroll
+        for (int c = 0; c < PLAN_SUMS; ++c) before[c] = carry[c] + (warp ? s_sum[c][warp - 1] : 0ull) + y[c] - x[c];
         if (i < n) {
-            pr[i].unit_begin = before_u;
-            pr[i].part_off = before_p;
-            for (unsigned long long k = 0; k < u; ++k) unit_map[before_u + k] = (uint32_t)i;
+            BProb& P = pr[i];
+            P.part_off = before[1];
+            P.wbegin[0] = before[3];
+            P.wbegin[1] = before[4];
+            if (P.staged) {
+                P.unit_begin = before[2];
+                for (unsigned long long k = 0; k < x[2]; ++k) unit_map_r[before[2] + k] = (uint32_t)i;
+            } else {
+                P.unit_begin = before[0];
+                for (unsigned long long k = 0; k < x[0]; ++k) unit_map[before[0] + k] = (uint32_t)i;
+            }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            carry_u += s_units[(blockDim.x >> 5) - 1];
-            carry_p += s_parts[(blockDim.x >> 5) - 1];
-        }
+        if (threadIdx.x < PLAN_SUMS) carry[threadIdx.x] += s_sum[threadIdx.x][(blockDim.x >> 5) - 1];
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        ctl->total = carry_u;
-        ctl->head = 0ull;
+        ctl->total = carry[0];
+        ctl->total_r = carry[2];
+        ctl->wtot = carry[3];
+        ctl->wtot_r = carry[4];
+    }
+}
+
+// Static share of the work: boundary b of `parts` equal-weight ranges of an
+// executor's units (the first TLIBG_BATCH_STATIC_PCT percent of its weight);
+// boundary `parts` also starts the atomic queue of the rest.  One thread per
+// boundary, a binary search over the problems' weight prefix.
+__device__ __forceinline__ unsigned long long partition_boundary(const BProb* __restrict__ pr, int n, bool staged,
+                                                                 unsigned long long wstatic, unsigned long long total,
+                                                                 int parts, int b)
+{
+    const unsigned long long t = (unsigned long long)((double)wstatic * (double)b / (double)parts);
+    // first problem whose units of this executor end beyond weight t
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const BProb& P = pr[mid];
+        const bool mine = (P.staged != 0) == staged;
+        const unsigned long long end = P.wbegin[staged ? 1 : 0] + (mine ? (unsigned long long)P.wunit * P.units : 0ull);
+        if (end > t) hi = mid;
+        else lo = mid + 1;
+    }
+    if (lo >= n) return total;
+    // the first problem whose units end beyond t carries weight, so it is one of this executor's
+    const BProb& P = pr[lo];
+    const unsigned long long k = (t - P.wbegin[staged ? 1 : 0] + P.wunit - 1) / P.wunit;
+    return P.unit_begin + (k < P.units ? k : P.units);
+}
+
+__global__ void batch_partition(const BProb* __restrict__ pr, int n, BCtl* ctl, unsigned long long* __restrict__ cta_begin,
+                                int parts, unsigned long long* __restrict__ warp_begin, int parts_r)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t <= parts) {
+        const unsigned long long ws = ctl->wtot * TLIBG_BATCH_STATIC_PCT / 100;
+        const unsigned long long u = partition_boundary(pr, n, false, ws, ctl->total, parts, t);
+        cta_begin[t] = u;
+        if (t == parts) ctl->head = u;
+    } else if (t <= parts + 1 + parts_r) {
+        const int b = t - parts - 1;
+        const unsigned long long ws = ctl->wtot_r * TLIBG_BATCH_STATIC_PCT / 100;
+        const unsigned long long u = partition_boundary(pr, n, true, ws, ctl->total_r, parts_r, b);
+        warp_begin[b] = u;
+        if (b == parts_r) ctl->head_r = u;
     }
 }
 
@@ -330,7 +458,7 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
         for (int v = 0; v < V; ++v) acc[v].init();
         uint64_t row = 0, seg = 0;
         if (valid) {
-            row = item / P.nseg;
+            row = P.nseg == 1 ? item : idx_div(item, P.sdiv);
             seg = item - row * P.nseg;
             const uint64_t ib = seg * P.seg_len;
             const uint64_t ie = min(P.nq, ib + P.seg_len);
@@ -380,27 +508,21 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
     }
 }
 
-// column unit: tile of TO outputs over one segment; false if a staging wait expired
+// column unit: tile of TO outputs over one segment
 template <int V, bool KAHAN>
-__device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, float* sb, float* red,
-                                         uint64_t* bar, uint32_t& phase, int* abort_flag,
-                                         BPair* __restrict__ part)
+__device__ __forceinline__ void col_unit(const BProb& P, uint64_t lu, int WI, float* red, BPair* __restrict__ part)
 {
     const uint32_t WO = (BLOCK / 32) / WI;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t wi = warp % WI, wo = warp / WI;
     const uint64_t TO = (uint64_t)WO * 32u * V;
     const uint64_t outputs = P.S * P.P;
-    const uint64_t tiles = (outputs + TO - 1) / TO;
-    const uint64_t seg = lu / tiles, tile = lu - seg * tiles;
+    const uint64_t tiles = P.tiles;
+    const uint64_t seg = P.nseg == 1 ? 0 : idx_div(lu, P.tdiv), tile = lu - seg * tiles;
     const uint64_t ib = seg * P.seg_len;
     const uint64_t ie = min(P.nq, ib + P.seg_len);
-    // b is read through L1 (warp-uniform per row): no per-unit staging wait
+    // b is read through L1 (warp-uniform per row)
     const float* __restrict__ bs = P.b;
-    (void)sb;
-    (void)bar;
-    (void)phase;
-    (void)abort_flag;
     constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
 
     const uint64_t o0 = tile * TO + ((uint64_t)wo * 32u + lane) * V;
@@ -409,7 +531,7 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
 #pragma unroll
     for (int v = 0; v < V; ++v) acc[v].init();
     if (valid) {
-        const uint64_t s = o0 / P.P;
+        const uint64_t s = idx_div(o0, P.pdiv);
         const uint64_t j = o0 - s * P.P;
         const float* ap = P.a + (s * P.nq) * P.P + j;
         uint64_t i = ib + wi;
@@ -467,7 +589,6 @@ __device__ __forceinline__ bool col_unit(const BProb& P, uint64_t lu, int WI, fl
             }
         }
     }
-    return true;
 }
 
 template <bool KAHAN>
@@ -488,55 +609,76 @@ __device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __r
     }
 }
 
-template <bool KAHAN>
 // Resident CTAs per SM the executor is compiled for (registers capped so that
 // this many fit): more warps in flight per SM for the latency-bound units.
-// Measured on GB300 (4096 uneven problems, fixed rule): 1 -> 6.1 ms,
-// 5 -> 3.9 ms, 6 -> 3.7 ms, 7 and 8 -> 3.5 ms per launch, despite spills;
+// Measured on GB300 (4096 uneven problems, fixed rule, atomic queue): 1 -> 6.1
+// ms, 5 -> 3.9 ms, 6 -> 3.7 ms, 7 and 8 -> 3.5 ms per launch, despite spills;
 // with two short rows per round in the row units 6, 7 and 8 all give
 // 3.47-3.50 ms, 6 with the fewest spills.
 #ifndef TLIBG_BATCH_MIN_CTAS
 #define TLIBG_BATCH_MIN_CTAS 6
 #endif
-__global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS) batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map,
-                                                    BCtl* ctl, BPair* __restrict__ part)
+
+// Copy problem descriptor `pi` into shared memory (one warp, word by word).
+__device__ __forceinline__ void fetch_desc(BProb* dst, const BProb* __restrict__ pr, int pi, uint32_t lane)
+{
+    static_assert(sizeof(BProb) % 4 == 0, "descriptor copied in words");
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(pr + pi);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (uint32_t w = lane; w < sizeof(BProb) / 4; w += 32) d[w] = __ldcg(src + w);
+}
+
+// CTA loop: its static range of units [cta_begin[b], cta_begin[b + 1]) in
+// order, then units from the atomic queue.  Warp 0 fetches the next unit's
+// problem descriptor into the other of two shared-memory slots while the CTA
+// works on the current unit, so no unit waits on a descriptor load; one CTA
+// barrier per unit (two more for a split problem's completion count).
+template <bool KAHAN>
+__global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
+    batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map, BCtl* ctl, BPair* __restrict__ part,
+               const unsigned long long* __restrict__ cta_begin)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-    int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
-    float* sb = nullptr;   // column units read b through L1 (no staging buffer)
-    float* red = reinterpret_cast<float*>(smem_raw + 16);
-    __shared__ unsigned long long s_unit;
-    __shared__ int s_prob, s_last;
-
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        *abort_flag = 0;
-        fence_mbar_init();
-    }
+    float* red = reinterpret_cast<float*>(smem_raw);
+    __shared__ __align__(16) BProb s_desc[2];
+    __shared__ unsigned long long s_u[2];
+    __shared__ int s_p[2];
+    __shared__ int s_last;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total);
     const int record = *reinterpret_cast<volatile int*>(&ctl->record);
-    long long t_unit = 0;
-    unsigned long long next = 0;
-    if (threadIdx.x == 0) next = atomicAdd(&ctl->head, 1ull);
-    uint32_t phase = 0;
-    __syncthreads();
+    unsigned long long u_next = cta_begin[blockIdx.x];
+    const unsigned long long u_static_end = cta_begin[blockIdx.x + 1];
 
-    while (true) {
-        if (threadIdx.x == 0) {
-            s_unit = next;
-            if (next < total) {
-                s_prob = (int)unit_map[next];
-                next = atomicAdd(&ctl->head, 1ull);   // consumed on the next iteration
-            }
+    // warp 0: the unit after the current one and its descriptor, into `slot`
+    auto prepare = [&](int slot) {
+        unsigned long long u;
+        if (u_next < u_static_end) {
+            u = u_next++;
+        } else {
+            unsigned long long v = 0;
+            if (lane == 0) v = atomicAdd(&ctl->head, 1ull);
+            u = __shfl_sync(0xffffffffu, v, 0);
         }
-        __syncthreads();
-        const unsigned long long u = s_unit;
+        const int pi = u < total ? (int)__ldg(unit_map + u) : -1;
+        if (lane == 0) {
+            s_u[slot] = u;
+            s_p[slot] = pi;
+        }
+        if (pi >= 0) fetch_desc(&s_desc[slot], pr, pi, lane);
+    };
+    if (warp == 0) prepare(0);
+    __syncthreads();
+    long long t_unit = 0;
+    for (int k = 0;; ++k) {
+        const int slot = k & 1;
+        const unsigned long long u = s_u[slot];
         if (u >= total) break;
         if (record && threadIdx.x == 0) t_unit = clock64();
-        const BProb& P = pr[s_prob];
+        if (warp == 0) prepare(slot ^ 1);
+        const BProb& P = s_desc[slot];
+        const int pi = s_p[slot];
         const uint64_t lu = u - P.unit_begin;
-        bool ok = true;
         if (P.kind == KIND_ROW) {
             switch (P.vec) {
             case 4: row_unit<4, KAHAN>(P, lu, P.group, part); break;
@@ -545,17 +687,16 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS) batch_exec(BProb*
             }
         } else {
             switch (P.vec) {
-            case 4: ok = col_unit<4, KAHAN>(P, lu, P.group, sb, red, bar, phase, abort_flag, part); break;
-            case 2: ok = col_unit<2, KAHAN>(P, lu, P.group, sb, red, bar, phase, abort_flag, part); break;
-            default: ok = col_unit<1, KAHAN>(P, lu, P.group, sb, red, bar, phase, abort_flag, part); break;
+            case 4: col_unit<4, KAHAN>(P, lu, P.group, red, part); break;
+            case 2: col_unit<2, KAHAN>(P, lu, P.group, red, part); break;
+            default: col_unit<1, KAHAN>(P, lu, P.group, red, part); break;
             }
         }
-        if (!ok) return;   // every thread saw the same expired wait
         if (P.nseg > 1) {
             __syncthreads();   // this CTA's partial stores are issued
             if (threadIdx.x == 0) {
                 __threadfence();
-                const unsigned int old = atomicAdd(&pr[s_prob].done, 1u);
+                const unsigned int old = atomicAdd(&pr[pi].done, 1u);
                 s_last = (old + 1u == P.units);
             }
             __syncthreads();
@@ -565,8 +706,140 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS) batch_exec(BProb*
             }
         }
         __syncthreads();
-        if (record && threadIdx.x == 0)
-            atomicAdd(&pr[s_prob].cycles, (unsigned long long)(clock64() - t_unit));
+        if (record && threadIdx.x == 0) atomicAdd(&pr[pi].cycles, (unsigned long long)(clock64() - t_unit));
+    }
+}
+
+// --------------------------------------------------------------------------
+// staged row units: one lane per row from shared memory (variant 8)
+// --------------------------------------------------------------------------
+// Every warp works alone: its static range of units [warp_begin[w],
+// warp_begin[w + 1]), then units from the atomic queue; a unit is BRT_TPU
+// tiles of 32 R consecutive rows of one problem (contiguous in HBM).  Each
+// tile moves into the warp's two-stage ring with one TMA bulk copy (ragged
+// head and tail by plain loads), the problem's b beside it; the warp then
+// walks one row per lane from shared memory (even n_q from a lane-dependent
+// column, so the lanes' reads spread over the banks) while the next tile is in
+// flight.  Waits are bounded; an expired wait sets the batch error word and
+// the warp leaves once its copies in flight have landed (bounded).
+template <bool KAHAN>
+__global__ void __launch_bounds__(BRT_THREADS) batch_rowtile(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map_r,
+                                                             BCtl* ctl, const unsigned long long* __restrict__ warp_begin)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t gw = (uint64_t)blockIdx.x * BRT_WARPS + warp;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw) + warp * BRT_NS;
+    unsigned char* wbase = smem_raw + 128 + (size_t)warp * BRT_WARP_BYTES;
+    float* barea = reinterpret_cast<float*>(wbase);                        // [BRT_NS][BRT_MAX_NQ]
+    unsigned char* ring = wbase + (size_t)BRT_NS * BRT_MAX_NQ * 4;         // [BRT_NS][BRT_SLOT]
+    if (lane == 0) {
+        for (int s = 0; s < BRT_NS; ++s) mbar_init(full + s, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total_r);
+    const int record = *reinterpret_cast<volatile int*>(&ctl->record);
+    unsigned long long u_next = warp_begin[gw];
+    const unsigned long long u_static_end = warp_begin[gw + 1];
+
+    // issue side: the problem and tile range of the unit being issued
+    int iprob = -1;
+    uint64_t it = 0, it_end = 0;
+    auto advance = [&]() -> bool {
+        while (it >= it_end) {
+            unsigned long long u;
+            if (u_next < u_static_end) {
+                u = u_next++;
+            } else {
+                unsigned long long v = 0;
+                if (lane == 0) v = atomicAdd(&ctl->head_r, 1ull);
+                u = __shfl_sync(0xffffffffu, v, 0);
+            }
+            if (u >= total) return false;
+            iprob = (int)__ldg(unit_map_r + u);
+            const BProb& P = pr[iprob];
+            const uint64_t R = brt_rows_per_lane(P.nq);
+            const uint64_t tiles = (P.S + 32 * R - 1) / (32 * R);
+            it = (u - P.unit_begin) * BRT_TPU;
+            it_end = min(tiles, it + BRT_TPU);
+        }
+        return true;
+    };
+    int sprob[BRT_NS];
+    uint64_t stile[BRT_NS];
+    auto issue = [&](int s) {
+        const BProb& P = pr[iprob];
+        const uint32_t nq = (uint32_t)P.nq;
+        const uint64_t R = brt_rows_per_lane(nq);
+        const uint64_t r0 = it * 32 * R, r1 = min(P.S, r0 + 32 * R);
+        for (uint32_t e = lane; e < nq; e += 32) barea[s * BRT_MAX_NQ + e] = __ldg(P.b + e);
+        stream_issue<float>(P.a, r0 * nq, r1 * nq, ring + (size_t)s * BRT_SLOT, full + s, lane);
+        sprob[s] = iprob;
+        stile[s] = it;
+        ++it;
+    };
+    bool more = advance();
+    uint32_t issued = 0;
+#pragma unroll
+    for (int s = 0; s < BRT_NS; ++s)
+        if (more) {
+            issue(s);
+            ++issued;
+            more = advance();
+        }
+    for (uint32_t c = 0; c < issued; ++c) {
+        const int s = (int)(c % BRT_NS);
+        long long t0 = 0;
+        if (record && lane == 0) t0 = clock64();
+        const bool ok = mbar_wait_bounded(full + s, (c / BRT_NS) & 1u, &g_batch_error);
+        if (__any_sync(0xffffffffu, !ok)) {
+            // leave only after this warp's other copy in flight has landed (bounded)
+            if (c + 1 < issued) mbar_wait_bounded(full + ((c + 1) % BRT_NS), ((c + 1) / BRT_NS) & 1u, &g_batch_error);
+            return;
+        }
+        const int pi = sprob[s];
+        const BProb& P = pr[pi];
+        const uint32_t nq = (uint32_t)P.nq;
+        const uint32_t R = brt_rows_per_lane(nq);
+        const uint64_t r0 = stile[s] * 32 * R;
+        const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(P.a + r0 * nq) & 15u);
+        const float* rows = reinterpret_cast<const float*>(ring + (size_t)s * BRT_SLOT + mis);
+        const float* sb = barea + s * BRT_MAX_NQ;
+        const uint32_t rot = (nq & 1u) ? 0u : lane % nq;
+        float out[4];
+        auto walk = [&](auto RC) {
+            constexpr int RR = decltype(RC)::value;
+            Acc<float, KAHAN> acc[RR];
+#pragma unroll
+            for (int r = 0; r < RR; ++r) acc[r].init();
+            if (r0 + lane < P.S) {
+                // rows lane + 32 r of the tile; one past the end re-reads row `lane`
+                const float* rp[RR];
+#pragma unroll
+                for (int r = 0; r < RR; ++r)
+                    rp[r] = rows + (size_t)((r0 + lane + 32u * r < P.S) ? lane + 32u * r : lane) * nq;
+                rowt_dot_any<RR, false>(acc, rp, sb, (const float2*)nullptr, nq, rot);
+            }
+#pragma unroll
+            for (int r = 0; r < RR; ++r) out[r] = acc[r].value();
+        };
+        if (R == 4) walk(std::integral_constant<int, 4>{});
+        else if (R == 2) walk(std::integral_constant<int, 2>{});
+        else walk(std::integral_constant<int, 1>{});
+        __syncwarp();   // every lane is done with the stage
+        float* C = P.c;
+        const uint64_t S = P.S;
+        if (more) {
+            issue(s);
+            ++issued;
+            more = advance();
+        }
+        for (uint32_t r = 0; r < R; ++r) {
+            const uint64_t row = r0 + lane + 32u * r;
+            if (row < S) C[row] = out[r];
+        }
+        if (record && lane == 0) atomicAdd(&pr[pi].cycles, (unsigned long long)(clock64() - t0));
     }
 }
 
@@ -582,7 +855,7 @@ float g_model_margin = 0.f;   // minimum predicted relative gain to leave the fi
 size_t exec_smem_bytes()
 {
     const size_t red_floats = (size_t)(8 - 1) * 1 * 32 * 2 * 4;   // largest: WI = 8, V = 4
-    return 16 + red_floats * 4;
+    return red_floats * 4;
 }
 
 int exec_ctas_per_sm(bool kahan)
@@ -596,6 +869,25 @@ int exec_ctas_per_sm(bool kahan)
                            : reinterpret_cast<const void*>(batch_exec<false>);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, exec_smem_bytes()) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    c = std::max(1, n);
+    return c;
+}
+
+int rowtile_ctas_per_sm(bool kahan)
+{
+    static int cache[2] = {-1, -1};
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    int& c = cache[kahan ? 1 : 0];
+    if (c >= 0) return c;
+    const void* fn = kahan ? reinterpret_cast<const void*>(batch_rowtile<true>)
+                           : reinterpret_cast<const void*>(batch_rowtile<false>);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BRT_SMEM);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BRT_THREADS, BRT_SMEM) != cudaSuccess) {
         cudaGetLastError();
         n = 1;
     }
@@ -639,10 +931,15 @@ struct tlibg_batch {
     int select = TLIBG_SELECT_HEURISTIC;
     int fixed_variant = 0;
     bool kahan = true;
-    int grid = 0;
+    int grid = 0;                 // batch_exec CTAs
+    int grid_r = 0;               // batch_rowtile CTAs
+    int slots = 1, slots_r = 1;   // resident CTAs (batch_exec) / warps (batch_rowtile) per SM
     BProb* d_prob = nullptr;
     BCtl* d_ctl = nullptr;
     uint32_t* d_map = nullptr;
+    uint32_t* d_map_r = nullptr;
+    unsigned long long* d_cta_begin = nullptr;    // grid + 1 boundaries of batch_exec's static ranges
+    unsigned long long* d_warp_begin = nullptr;   // grid_r * BRT_WARPS + 1 of batch_rowtile's
     BPair* d_part = nullptr;
     float* d_model = nullptr;
     float log2_count = 0.f;
@@ -660,13 +957,22 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
         batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
         ++n;
     }
-    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map);
+    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map, bt->d_map_r);
+    const int wr = bt->grid_r * BRT_WARPS;
+    const int nb = bt->grid + 1 + wr + 1;
+    batch_partition<<<(nb + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_cta_begin, bt->grid,
+                                                      bt->d_warp_begin, wr);
     const size_t smem = exec_smem_bytes();
-    if (bt->kahan)
-        batch_exec<true><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
-    else
-        batch_exec<false><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
-    n += 2;
+    if (bt->kahan) {
+        batch_exec<true><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part, bt->d_cta_begin);
+        batch_rowtile<true><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl,
+                                                                       bt->d_warp_begin);
+    } else {
+        batch_exec<false><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part, bt->d_cta_begin);
+        batch_rowtile<false><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl,
+                                                                        bt->d_warp_begin);
+    }
+    n += 4;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
     internal_count_launches(n);
@@ -675,7 +981,7 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
 
 int launches_per_run(const tlibg_batch* bt)
 {
-    return bt->select == TLIBG_SELECT_FIXED ? 3 : 2;
+    return bt->select == TLIBG_SELECT_FIXED ? 5 : 4;
 }
 
 void release(tlibg_batch* bt)
@@ -686,6 +992,9 @@ void release(tlibg_batch* bt)
     if (bt->d_prob) cudaFree(bt->d_prob);
     if (bt->d_ctl) cudaFree(bt->d_ctl);
     if (bt->d_map) cudaFree(bt->d_map);
+    if (bt->d_map_r) cudaFree(bt->d_map_r);
+    if (bt->d_cta_begin) cudaFree(bt->d_cta_begin);
+    if (bt->d_warp_begin) cudaFree(bt->d_warp_begin);
     if (bt->d_part) cudaFree(bt->d_part);
     if (bt->d_model) cudaFree(bt->d_model);
     delete bt;
@@ -770,7 +1079,8 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
     if (bt->select < TLIBG_SELECT_HEURISTIC || bt->select > TLIBG_SELECT_GIVEN)
         return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: unknown selection mode");
     if (bt->select == TLIBG_SELECT_FIXED && (bt->fixed_variant < 0 || bt->fixed_variant >= NVARIANT))
-        return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: variant must be in 0..7");
+        return create_fail(bt, TLIBG_ERR_ARGUMENT,
+                           "tlibg_batch_create: variant must be in 0.." + std::to_string(NVARIANT - 1));
 
     std::vector<float> feat(count * NFEAT);
     std::vector<int> kinds(count), heur(count);
@@ -793,7 +1103,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
 
     // descriptors; unit map and partial scratch sized for the worst variant of each problem
     std::vector<BProb> hp(count);
-    uint64_t total_units = 0, max_part = 0;
+    uint64_t total_units = 0, max_part = 0, total_units_r = 0;
     for (size_t i = 0; i < count; ++i) {
         const tlibg_problem& x = probs[i];
         s = internal_check_device_pointers(x.a, x.b, x.c);
@@ -814,17 +1124,21 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         b.kind = kinds[i];
         b.vec = batch_vec(b.kind, cn, x.a, x.b);
         std::copy(feat.begin() + i * NFEAT, feat.begin() + (i + 1) * NFEAT, b.feat);
+        // the staged row variant takes short q-fastest rows only
         b.valid_mask = (1u << NVARIANT) - 1u;
+        if (!(b.kind == KIND_ROW && b.nq <= (uint64_t)BRT_MAX_NQ)) b.valid_mask &= ~(1u << VARIANT_STAGED);
         b.variant = heur[i];
         b.heuristic = heur[i];
         if (bt->select == TLIBG_SELECT_GIVEN) {
             const int v = opt->variants[i];
             if (v < 0 || v >= NVARIANT)
-                return create_fail(bt, TLIBG_ERR_ARGUMENT, "tlibg_batch_create: variants must be in 0..7");
+                return create_fail(bt, TLIBG_ERR_ARGUMENT,
+                                   "tlibg_batch_create: variants must be in 0.." + std::to_string(NVARIANT - 1));
             b.variant = v;
         }
         uint64_t mu = 0, mp = 0;
         for (int v = 0; v < NVARIANT; ++v) {
+            if (v == VARIANT_STAGED) continue;
             int g;
             uint32_t ns;
             decode_variant(b.kind, v, b.nq, &g, &ns);
@@ -835,29 +1149,37 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         }
         total_units += mu;
         max_part += mp;
+        if ((b.valid_mask >> VARIANT_STAGED) & 1u) total_units_r += brt_units(b.nq, b.S);
     }
-    if (total_units >= ((uint64_t)1 << 32))
+    bt->slots = exec_ctas_per_sm(bt->kahan);
+    bt->slots_r = rowtile_ctas_per_sm(bt->kahan) * BRT_WARPS;
+    bt->grid = sms * bt->slots;
+    bt->grid_r = sms * (bt->slots_r / BRT_WARPS);
+    if (total_units >= ((uint64_t)1 << 32) || total_units_r >= ((uint64_t)1 << 32))
         return create_fail(bt, TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: more than 2^32 work units");
 
     cudaError_t e = cudaSuccess;
     if ((e = internal_malloc((void**)&bt->d_prob, count * sizeof(BProb))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_map, std::max<uint64_t>(total_units, 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_map_r, std::max<uint64_t>(total_units_r, 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_cta_begin, (size_t)(bt->grid + 1) * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_warp_begin, (size_t)(bt->grid_r * BRT_WARPS + 1) * sizeof(unsigned long long))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
         (!model.empty() && (e = internal_malloc((void**)&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
         cudaGetLastError();
         return create_fail(bt, TLIBG_ERR_NOMEM, std::string("tlibg_batch_create: ") + cudaGetErrorString(e));
     }
     cudaMemcpyAsync(bt->d_prob, hp.data(), count * sizeof(BProb), cudaMemcpyHostToDevice, st);
-    BCtl hctl{0ull, 0ull, (opt && opt->record_costs) ? 1 : 0};
+    BCtl hctl{};
+    hctl.record = (opt && opt->record_costs) ? 1 : 0;
     cudaMemcpyAsync(bt->d_ctl, &hctl, sizeof(BCtl), cudaMemcpyHostToDevice, st);
     if (!model.empty() && bt->select == TLIBG_SELECT_LEARNED)
         cudaMemcpyAsync(bt->d_model, model.data(), MLP_PARAMS * sizeof(float), cudaMemcpyHostToDevice, st);
-    bt->grid = sms * exec_ctas_per_sm(bt->kahan);
     if (bt->select == TLIBG_SELECT_LEARNED) {
         // the scores depend only on the descriptors and the model: select once,
         // every launch replays plan + exec with the chosen variants
-        const int threads = bt->count * NVARIANT;
+        const int threads = bt->count * SELECT_LANES;
         batch_select<<<(threads + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_model, bt->log2_count,
                                                             bt->log2_keep);
         internal_count_launches(1);
@@ -925,7 +1247,8 @@ int tlibg_batch_set_variant(tlibg_batch* bt, int variant)
         return internal_fail(TLIBG_ERR_ARGUMENT,
                              "tlibg_batch_set_variant: only for TLIBG_SELECT_FIXED batches built with no_graph");
     if (variant < 0 || variant >= NVARIANT)
-        return internal_fail(TLIBG_ERR_ARGUMENT, "tlibg_batch_set_variant: variant must be in 0..7");
+        return internal_fail(TLIBG_ERR_ARGUMENT,
+                             "tlibg_batch_set_variant: variant must be in 0.." + std::to_string(NVARIANT - 1));
     bt->fixed_variant = variant;
     return internal_ok();
 }
@@ -950,7 +1273,10 @@ int tlibg_batch_costs(tlibg_batch* bt, uint64_t* cycles, void* stream)
     cudaError_t e = cudaMemcpyAsync(hp.data(), bt->d_prob, bt->count * sizeof(BProb), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return internal_cuda_fail(e, "tlibg_batch_costs");
-    for (int i = 0; i < bt->count; ++i) cycles[i] = hp[i].cycles;
+    // SM cycles: a unit's CTA (or, staged, warp) cycles over the CTAs (warps) resident per SM
+    for (int i = 0; i < bt->count; ++i)
+        cycles[i] = (hp[i].cycles + (uint64_t)(hp[i].staged ? bt->slots_r : bt->slots) / 2) /
+                    (uint64_t)(hp[i].staged ? bt->slots_r : bt->slots);
     return internal_ok();
 }
 

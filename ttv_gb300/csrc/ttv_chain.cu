@@ -39,25 +39,28 @@ struct KronArgs {
     void* wS;
 };
 
-template <typename T>
+// One weight per thread: the mixed-radix digits of its index pick one element
+// of each mode's vector.  I: 32-bit index arithmetic when P + S < 2^32 (one
+// 32-bit division per mode instead of a 64-bit one).
+template <typename T, typename I>
 __global__ void kron_kernel(KronArgs k)
 {
-    const uint64_t total = k.P + k.S;
-    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (uint64_t)gridDim.x * blockDim.x) {
-        const bool pre = idx < k.P;
-        uint64_t j = pre ? idx : idx - k.P;
+    const I P = (I)k.P, total = (I)(k.P + k.S);
+    for (I idx = (I)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
+        const bool pre = idx < P;
+        I j = pre ? idx : idx - P;
         const int m0 = pre ? 0 : k.np, m1 = pre ? k.np : k.np + k.ns;
         double w = 1.0;
         for (int m = m0; m < m1; ++m) {
-            const uint64_t d = j % k.ext[m];
-            j /= k.ext[m];
-            w *= (double)static_cast<const T*>(k.vec[m])[d];
+            const I e = (I)k.ext[m];
+            const I q = j / e;
+            w *= (double)static_cast<const T*>(k.vec[m])[j - q * e];
+            j = q;
         }
         if (pre)
             static_cast<T*>(k.wP)[idx] = (T)w;
         else
-            static_cast<T*>(k.wS)[idx - k.P] = (T)w;
+            static_cast<T*>(k.wS)[idx - P] = (T)w;
     }
 }
 
@@ -180,10 +183,14 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
     if (!stage2) ka.S = 0;
     if (nk) {
         const int grid = (int)std::min<uint64_t>((uint64_t)sms * 8, (nk + 255) / 256);
-        if (tdt == F64)
-            kron_kernel<double><<<grid, 256, 0, st>>>(ka);
-        else
-            kron_kernel<float><<<grid, 256, 0, st>>>(ka);
+        const bool narrow = nk < (uint64_t(1) << 32);
+        if (tdt == F64) {
+            if (narrow) kron_kernel<double, uint32_t><<<grid, 256, 0, st>>>(ka);
+            else kron_kernel<double, uint64_t><<<grid, 256, 0, st>>>(ka);
+        } else {
+            if (narrow) kron_kernel<float, uint32_t><<<grid, 256, 0, st>>>(ka);
+            else kron_kernel<float, uint64_t><<<grid, 256, 0, st>>>(ka);
+        }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
         ++launches;

@@ -361,7 +361,12 @@ __device__ __forceinline__ bool stage_b(T* smem_b, const T* b, uint64_t ib, uint
     if (threadIdx.x == 0) {
         if (!mbar_wait_bounded(bar, phase, err)) {
             *abort_flag = 1;
-            // give an in-flight copy a second bounded chance to land before leaving
+            // give an in-flight copy a second bounded chance to land before leaving.
+            // No further copy is issued after an expiry: the caller returns.  If this
+            // wait expires too, the CTA leaves with at most this one copy outstanding
+            // (its destination is this CTA's shared memory); the device error word is
+            // set, the host reports TLIBG_ERR_TIMEOUT and the results (and any later
+            // work sharing that SM's shared memory) must be treated as invalid.
             mbar_wait_bounded(bar, phase, err);
         }
     }

@@ -92,14 +92,15 @@ bool stream_eligible(int dtype, uint64_t P, uint64_t nq);
 // Montgomery ("Division by invariant integers using multiplication", PLDI
 // 1994, section 4) with l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
 // t = hi32(m n), n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0).
-// Otherwise the plain 64-bit division.  Built on the host per launch.
+// Otherwise the plain 64-bit division.  Built on the host per launch (and on
+// the device per problem by the batched executor's planning kernel).
 struct IdxDiv {
     uint64_t d;
     uint32_t m;
     uint8_t s1, s2, fast;
 };
 
-inline IdxDiv make_idx_div(uint64_t d, uint64_t max_dividend)
+__host__ __device__ inline IdxDiv make_idx_div(uint64_t d, uint64_t max_dividend)
 {
     IdxDiv v{d == 0 ? 1 : d, 0, 0, 0, 0};
     if (v.d < (uint64_t(1) << 32) && max_dividend < (uint64_t(1) << 32)) {

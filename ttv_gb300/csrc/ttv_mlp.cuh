@@ -12,7 +12,7 @@
 namespace tlibg {
 
 constexpr int NFEAT = 8;      // shape features of a problem (see batch_features)
-constexpr int NVARIANT = 8;   // kernel variants a batched problem can run with
+constexpr int NVARIANT = 9;   // kernel variants a batched problem can run with
 constexpr int MLP_IN = NFEAT + NVARIANT;
 constexpr int MLP_H = 64;
 constexpr int OFF_W1 = 0;

@@ -22,7 +22,10 @@
 //                segments of each row in fixed order (deterministic)
 //
 // Rows must allow 16-byte loads (n_q a multiple of V, A and b 16-byte
-// aligned); the planner keeps the row kernel otherwise.
+// aligned).  On request (TLIBG_KIND_ROW_PANEL) and as an autotuner candidate:
+// measured on GB300 the row kernel's segment-major walk (the S rows of one b
+// segment taken up by neighbouring warps, so b comes from HBM about once) is
+// as fast or faster on the asymmetric sweep's rows, so the planner keeps it.
 #pragma once
 
 namespace tlibg {

@@ -18,11 +18,10 @@
 // TLIBG_ROWT_NATIVE_EVERY native), fp32 / bf16 use the Kahan accumulator.
 #pragma once
 
+#include "ttv_rowwalk.cuh"
+
 namespace tlibg {
 
-#ifndef TLIBG_ROWT_NATIVE_EVERY
-#define TLIBG_ROWT_NATIVE_EVERY 2
-#endif
 
 // Shared memory of the kernel: mbarriers (128 bytes), b, b's split (fp64
 // with the double-float mix), then ROWT_WARPS * ROWT_NS stages.
@@ -37,114 +36,6 @@ __device__ __forceinline__ void rowt_issue(const TA* A, uint64_t S, uint64_t nq,
     const uint64_t r0 = t * 32 * R;
     const uint64_t r1 = min(S, r0 + 32 * R);
     stream_issue<TA>(A, r0 * nq, r1 * nq, slot, full, lane);
-}
-
-// One step of R rows at column c: element c of each row times b[c].
-template <int R, bool NATIVE, bool PRE, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void rowt_step(AccT (&acc)[R], const TA* (&rp)[R], const T* sb, const float2* bsp,
-                                          uint32_t c)
-{
-    const T bb = sb[c];
-    if constexpr (std::is_same<AccT, AccDF>::value) {
-        if constexpr (NATIVE) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) acc[r].d = fma((double)rp[r][c], bb, acc[r].d);
-        } else {
-            DSplit bs;
-            if constexpr (PRE) {
-                const float2 t = bsp[c];
-                bs.hi = t.x;
-                bs.lo = t.y;
-                bs.ok = true;
-            } else {
-                bs = split_double(bb);
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const double a = rp[r][c];
-                acc[r].add_split(split_double(a), bs, a, bb);
-            }
-        }
-    } else {
-#pragma unroll
-        for (int r = 0; r < R; ++r) acc[r].fma_add(Cvt<TA, T>::f(rp[r][c]), bb);
-    }
-}
-
-// Next column of the walk: wrapping at n_q (rotated walks of even n_q), or
-// straight (odd n_q, which starts at column 0).
-template <bool WRAP> __device__ __forceinline__ uint32_t rowt_next(uint32_t c, uint32_t nq)
-{
-    if constexpr (WRAP) return (c + 1 == nq) ? 0u : c + 1;
-    return c + 1;
-}
-
-// The lane's R rows (rp[r]) over all n_q columns, walking from column c.
-// fp64 with the double-float mix: the first step of every
-// TLIBG_ROWT_NATIVE_EVERY on the DFMA pipe, the rest emulated, in blocks of
-// RT_G such groups with one renormalisation each (at most 8 emulated
-// products between two); the last n_q mod E steps native.
-constexpr int RT_G = 4;
-template <int R, bool PRE, bool WRAP, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void rowt_dot(AccT (&acc)[R], const TA* (&rp)[R], const T* sb, const float2* bsp,
-                                         uint32_t nq, uint32_t c)
-{
-    if constexpr (std::is_same<AccT, AccDF>::value) {
-        constexpr int E = TLIBG_ROWT_NATIVE_EVERY;
-        static_assert(RT_G * (E - 1) <= 8, "renormalise at least every 8 emulated products");
-        uint32_t j = 0;
-        for (; j + RT_G * E <= nq; j += RT_G * E) {
-#pragma unroll
-            for (int gq = 0; gq < RT_G; ++gq) {
-                rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-                c = rowt_next<WRAP>(c, nq);
-#pragma unroll
-                for (int u = 1; u < E; ++u) {
-                    rowt_step<R, false, PRE>(acc, rp, sb, bsp, c);
-                    c = rowt_next<WRAP>(c, nq);
-                }
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) acc[r].renorm();
-        }
-        for (; j + E <= nq; j += E) {   // fewer than RT_G groups left: fold() renormalises
-            rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-            c = rowt_next<WRAP>(c, nq);
-#pragma unroll
-            for (int u = 1; u < E; ++u) {
-                rowt_step<R, false, PRE>(acc, rp, sb, bsp, c);
-                c = rowt_next<WRAP>(c, nq);
-            }
-        }
-        for (; j < nq; ++j) {
-            rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-            c = rowt_next<WRAP>(c, nq);
-        }
-    } else {
-        uint32_t j = 0;
-        for (; j + 8 <= nq; j += 8) {
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-                c = rowt_next<WRAP>(c, nq);
-            }
-        }
-        for (; j < nq; ++j) {
-            rowt_step<R, true, PRE>(acc, rp, sb, bsp, c);
-            c = rowt_next<WRAP>(c, nq);
-        }
-    }
-}
-
-// Even n_q walks rotated (wrapping), odd n_q straight.
-template <int R, bool PRE, typename TA, typename T, typename AccT>
-__device__ __forceinline__ void rowt_dot_any(AccT (&acc)[R], const TA* (&rp)[R], const T* sb, const float2* bsp,
-                                             uint32_t nq, uint32_t c)
-{
-    if (nq & 1u)
-        rowt_dot<R, PRE, false>(acc, rp, sb, bsp, nq, 0u);
-    else
-        rowt_dot<R, PRE, true>(acc, rp, sb, bsp, nq, c);
 }
 
 template <typename TA, typename T, bool KAHAN, int R>

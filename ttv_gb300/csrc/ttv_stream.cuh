@@ -15,6 +15,8 @@
 // CTA leaves.
 #pragma once
 
+#include "ttv_rowwalk.cuh"
+
 namespace tlibg {
 
 constexpr int STREAM_STAGE = STREAM_STAGE_BYTES;   // bytes of A per chunk
@@ -93,36 +95,6 @@ struct ChunkWalk {
         return true;
     }
 };
-
-template <typename TA>
-__device__ __forceinline__ void stream_issue(const TA* A, uint64_t e0, uint64_t e1, unsigned char* slot,
-                                             uint64_t* full, uint32_t lane)
-{
-    const uintptr_t g0 = reinterpret_cast<uintptr_t>(A + e0);
-    const uintptr_t g1 = reinterpret_cast<uintptr_t>(A + e1);
-    const uintptr_t base = g0 & ~uintptr_t(15);
-    uintptr_t body0 = (g0 + 15) & ~uintptr_t(15);
-    uintptr_t body1 = g1 & ~uintptr_t(15);
-    if (body0 > g1) body0 = g1;
-    if (body1 < body0) body1 = body0;
-    // ragged head [g0, body0) and tail [body1, g1): element-wise plain loads
-    const uint32_t head = (uint32_t)((body0 - g0) / sizeof(TA));
-    const uint32_t tail = (uint32_t)((g1 - body1) / sizeof(TA));
-    if (lane < head) {
-        const TA* src = reinterpret_cast<const TA*>(g0) + lane;
-        *reinterpret_cast<TA*>(slot + (reinterpret_cast<uintptr_t>(src) - base)) = *src;
-    } else if (lane >= 16 && lane - 16 < tail) {
-        const TA* src = reinterpret_cast<const TA*>(body1) + (lane - 16);
-        *reinterpret_cast<TA*>(slot + (reinterpret_cast<uintptr_t>(src) - base)) = *src;
-    }
-    __syncwarp();
-    if (lane == 0) {
-        const uint32_t bytes = (uint32_t)(body1 - body0);
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(full, bytes);
-        if (bytes) bulk_g2s(slot + (body0 - base), reinterpret_cast<const void*>(body0), bytes, full);
-    }
-}
 
 __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(STREAM_NT) : "memory"); }
 
