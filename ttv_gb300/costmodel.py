@@ -136,6 +136,7 @@ def tune_mixed(shapes, seed=0, reps=2, lo=64, hi=4096, log_every=5000,
     times = np.zeros((len(shapes), B.NVARIANT), np.float32)
     heur = np.zeros(len(shapes), np.int32)
     batch_of = np.zeros(len(shapes), np.int32)
+    valid = variant_mask(shapes)
     t0 = time.time()
     i = nb = 0
     while i < len(shapes):
@@ -165,7 +166,7 @@ def tune_mixed(shapes, seed=0, reps=2, lo=64, hi=4096, log_every=5000,
                     bt.launch()
                     c = bt.costs().astype(np.float64)
                     best = c if best is None else np.minimum(best, c)
-                times[idx, v] = best / 2070.0
+                times[idx, v] = np.where(valid[idx, v], best / 2070.0, np.inf)
         i += len(chunk)
         nb += 1
         if log_every and i // log_every != (i - len(chunk)) // log_every:
@@ -174,10 +175,43 @@ def tune_mixed(shapes, seed=0, reps=2, lo=64, hi=4096, log_every=5000,
     return feats, times, heur
 
 
+def variant_mask(shapes):
+    """Variants each shape can run: all but the staged rows, which need q to be the
+    fastest layout mode (prefix P == 1) and n_q <= 64."""
+    valid = np.ones((len(shapes), B.NVARIANT), bool)
+    for i, (na, pia, q) in enumerate(shapes):
+        valid[i, B.VARIANT_STAGED] = pia[0] == q and na[q - 1] <= 64
+    return valid
+
+
 def training_set(feats, times):
+    """(inputs, log2 cost) of every runnable (problem, variant) pair."""
     x = B.mlp_inputs(feats)
-    y = np.log2(np.maximum(times, 1e-3)).ravel().astype(np.float32)
-    return x, y
+    t = times.ravel()
+    ok = np.isfinite(t)
+    y = np.log2(np.maximum(t[ok], 1e-3)).astype(np.float32)
+    return x[ok], y
+
+
+def derive_fixed_rule(feats, times):
+    """The best single variant per (kernel family, widest load) over tuned shapes:
+    the variant with the least total time in each class ({(kind, vec): v})."""
+    kind = np.where(feats[:, 2] > 0, 1, 0)          # log2 P > 0: column form
+    vec = np.rint(feats[:, 7] * 4).astype(int)
+    rule = {}
+    for k in (0, 1):
+        for v in (1, 2, 4):
+            m = (kind == k) & (vec == v)
+            if m.any():
+                tot = np.where(np.isfinite(times[m]), times[m], np.inf).sum(axis=0)
+                rule[(k, v)] = int(np.argmin(tot))
+    return rule
+
+
+def apply_fixed_rule(rule, feats):
+    kind = np.where(feats[:, 2] > 0, 1, 0)
+    vec = np.rint(feats[:, 7] * 4).astype(int)
+    return np.array([rule.get((k, v), 0) for k, v in zip(kind, vec)], np.int32)
 
 
 def train(feats, times, epochs=60, batch=512, lr=2e-3, seed=0):
@@ -190,12 +224,16 @@ def train(feats, times, epochs=60, batch=512, lr=2e-3, seed=0):
     return params.cpu().numpy(), losses
 
 
-def predict_scores(params, feats):
-    """Predicted log2 cost of every variant of every shape (the engine's inference kernel)."""
+def predict_scores(params, feats, valid=None):
+    """Predicted log2 cost of every variant of every shape (the engine's inference
+    kernel); variants a shape cannot run score +inf."""
     import torch
     x = torch.from_numpy(B.mlp_inputs(feats)).cuda()
     pred = B.mlp_predict(torch.from_numpy(np.asarray(params, np.float32)).cuda(), x)
-    return pred.cpu().numpy().reshape(len(feats), B.NVARIANT)
+    scores = pred.cpu().numpy().reshape(len(feats), B.NVARIANT)
+    if valid is not None:
+        scores = np.where(valid, scores, np.inf)
+    return scores
 
 
 def choose(scores, heuristic, margin):
@@ -207,8 +245,8 @@ def choose(scores, heuristic, margin):
     return np.where(keep, heuristic, best)
 
 
-def predict_variants(params, feats, heuristic=None, margin=0.0):
-    scores = predict_scores(params, feats)
+def predict_variants(params, feats, heuristic=None, margin=0.0, valid=None):
+    scores = predict_scores(params, feats, valid)
     if heuristic is None:
         return scores.argmin(axis=1)
     return choose(scores, heuristic, margin)
@@ -240,6 +278,7 @@ def main():
     if args.reuse_db and os.path.exists(db_path):
         d = np.load(db_path)
         feats, times, heur, split = d["features"], d["times"], d["heuristic"], d["is_test"]
+        valid = d["valid"] if "valid" in d else np.isfinite(times)
     else:
         shapes = random_shapes(args.train + args.test, args.seed)
         t0 = time.time()
@@ -247,35 +286,44 @@ def main():
             feats, times, heur = tune_mixed(shapes, seed=args.seed)
         else:
             feats, times, heur = tune(shapes)
+        valid = variant_mask(shapes)
         print(f"tuning: {time.time() - t0:.1f} s for {len(shapes)} shapes x {B.NVARIANT} variants")
         split = np.zeros(len(shapes), bool)
         split[args.train:] = True
         np.savez_compressed(db_path, features=feats, times=times, heuristic=heur, is_test=split,
-                            shapes=np.frombuffer(json.dumps(shapes).encode(), np.uint8))
+                            valid=valid, shapes=np.frombuffer(json.dumps(shapes).encode(), np.uint8))
     tr, te = ~split, split
+    # the fixed rule, re-derived from the training shapes: the best single variant of
+    # each (kernel family, widest load) class
+    rule = derive_fixed_rule(feats[tr], times[tr])
+    fixed = apply_fixed_rule(rule, feats)
     # the last tenth of the training shapes picks the selection margin
     tr_idx = np.where(tr)[0]
     fit, val = tr_idx[: len(tr_idx) * 9 // 10], tr_idx[len(tr_idx) * 9 // 10:]
     t0 = time.time()
     params, losses = train(feats[fit], times[fit], epochs=args.epochs, seed=args.seed)
     t_train = time.time() - t0
-    val_scores = predict_scores(params, feats[val])
-    margins = [0.0, 0.05, 0.1, 0.15, 0.2, 0.3, 0.5]
-    val_regret = {m: regret(times[val], choose(val_scores, heur[val], m))[0] for m in margins}
+    val_scores = predict_scores(params, feats[val], valid[val])
+    margins = [0.0, 0.02, 0.05, 0.1, 0.15, 0.2, 0.3, 0.5]
+    val_regret = {m: regret(times[val], choose(val_scores, fixed[val], m))[0] for m in margins}
     margin = min(margins, key=lambda m: val_regret[m])
-    learned = predict_variants(params, feats[te], heur[te], margin)
+    learned = predict_variants(params, feats[te], fixed[te], margin, valid[te])
     r_learn = regret(times[te], learned)
-    r_argmin = regret(times[te], predict_variants(params, feats[te]))
-    r_heur = regret(times[te], heur[te])
-    r_fixed = {v: regret(times[te], np.full(te.sum(), v))[0] for v in range(B.NVARIANT)}
+    r_argmin = regret(times[te], predict_variants(params, feats[te], valid=valid[te]))
+    r_fixed_rule = regret(times[te], fixed[te])
+    r_engine_rule = regret(times[te], heur[te])
+    r_single = {v: regret(times[te], np.where(valid[te][:, v], v, fixed[te]))[0] for v in range(B.NVARIANT)}
+    best = np.where(valid[te], times[te], np.inf).argmin(axis=1)
     summary = {"train_shapes": int(len(fit)), "validation_shapes": int(len(val)),
                "test_shapes": int(te.sum()),
                "train_seconds": round(t_train, 2), "final_loss": float(losses[-1]),
+               "fixed_rule": {f"{'col' if k else 'row'}_vec{v}": r for (k, v), r in sorted(rule.items())},
                "margin": margin, "validation_regret_by_margin": val_regret,
                "regret_learned": r_learn, "regret_learned_plain_argmin": r_argmin,
-               "regret_fixed_rule": r_heur, "regret_single_variant": r_fixed,
-               "learned_picks_best": float(np.mean(learned == times[te].argmin(axis=1))),
-               "learned_leaves_fixed_rule": float(np.mean(learned != heur[te]))}
+               "regret_fixed_rule": r_fixed_rule, "regret_engine_rule": r_engine_rule,
+               "regret_single_variant": r_single,
+               "learned_picks_best": float(np.mean(learned == best)),
+               "learned_leaves_fixed_rule": float(np.mean(learned != fixed[te]))}
     np.savez_compressed(os.path.join(args.out, "cost_model.npz"), params=params, losses=losses,
                         margin=np.float32(margin),
                         summary=np.frombuffer(json.dumps(summary).encode(), np.uint8))

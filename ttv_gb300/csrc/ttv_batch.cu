@@ -54,9 +54,6 @@ struct BProb {
     uint64_t unit_begin;   // first unit of the problem in its executor's unit space
     uint64_t part_off;     // in BPair elements
     uint64_t tiles;        // column units: tiles per segment
-    uint64_t wbegin[2];    // weight (bytes of A) of the units before the problem's: [0] batch_exec,
-                           // [1] batch_rowtile (both prefixes for every problem)
-    uint64_t wunit;        // weight of one of the problem's units
     IdxDiv pdiv;           // column units: output -> slice (division by P)
     IdxDiv tdiv;           // column units: unit -> segment (division by tiles)
     IdxDiv sdiv;           // row units: item -> row (division by the segment count)
@@ -75,22 +72,12 @@ struct BProb {
 };
 
 struct BCtl {
-    unsigned long long head;     // batch_exec's dynamic tail: next unit to hand out
+    unsigned long long head;     // batch_exec's queue: next unit to hand out
     unsigned long long total;    // batch_exec's units
     unsigned long long head_r;   // the same for batch_rowtile
     unsigned long long total_r;
-    unsigned long long wtot;     // batch_exec's total weight (bytes of A)
-    unsigned long long wtot_r;
     int record;                  // nonzero: accumulate per-problem unit cycles
 };
-
-// Share of each executor's weight handed out statically (contiguous unit
-// ranges of equal weight per CTA, or per warp for batch_rowtile, with no
-// atomics or queue latency); the rest goes through the atomic queue so that
-// the launch ends level.
-#ifndef TLIBG_BATCH_STATIC_PCT
-#define TLIBG_BATCH_STATIC_PCT 90
-#endif
 
 // Staged row units (variant 8, batch_rowtile): tiles of 32 R rows of at most
 // BRT_TILE_BYTES, BRT_TPU tiles per work unit, one two-stage ring per warp.
@@ -219,7 +206,7 @@ __global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
 // --------------------------------------------------------------------------
 // plan: units, prefix sums, unit -> problem map, queue reset (one CTA)
 // --------------------------------------------------------------------------
-constexpr int PLAN_SUMS = 5;   // batch_exec units, split partials, batch_rowtile units, their weights
+constexpr int PLAN_SUMS = 3;   // batch_exec units, split partials, batch_rowtile units
 
 __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl,
                                                    uint32_t* __restrict__ unit_map, uint32_t* __restrict__ unit_map_r)
@@ -231,7 +218,7 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int base = 0; base < n; base += blockDim.x) {
         const int i = base + threadIdx.x;
-        unsigned long long x[PLAN_SUMS] = {0, 0, 0, 0, 0};
+        unsigned long long x[PLAN_SUMS] = {0, 0, 0};
         if (i < n) {
             BProb& P = pr[i];
             if (!((P.valid_mask >> P.variant) & 1u)) P.variant = P.heuristic;   // not runnable: the fixed rule
@@ -248,7 +235,6 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
             P.done = 0u;
             P.cycles = 0ull;
             const uint64_t outputs = P.S * P.P;
-            const uint64_t abytes = 4 * outputs * P.nq;
             if (P.kind == KIND_COL) {
                 const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * P.vec;
                 P.tiles = (outputs + TO - 1) / TO;
@@ -266,8 +252,6 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
                 x[0] = u;
                 x[1] = nseg > 1 ? (unsigned long long)nseg * outputs : 0ull;
             }
-            P.wunit = (abytes + P.units - 1) / (P.units ? P.units : 1);
-            x[P.staged ? 4 : 3] = P.wunit * P.units;
         }
         // inclusive warp scans, then across warps
         unsigned long long y[PLAN_SUMS];
@@ -305,8 +289,6 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
         if (i < n) {
             BProb& P = pr[i];
             P.part_off = before[1];
-            P.wbegin[0] = before[3];
-            P.wbegin[1] = before[4];
             if (P.staged) {
                 P.unit_begin = before[2];
                 for (unsigned long long k = 0; k < x[2]; ++k) unit_map_r[before[2] + k] = (uint32_t)i;
@@ -321,53 +303,9 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
     }
     if (threadIdx.x == 0) {
         ctl->total = carry[0];
+        ctl->head = 0ull;
         ctl->total_r = carry[2];
-        ctl->wtot = carry[3];
-        ctl->wtot_r = carry[4];
-    }
-}
-
-// Static share of the work: boundary b of `parts` equal-weight ranges of an
-// executor's units (the first TLIBG_BATCH_STATIC_PCT percent of its weight);
-// boundary `parts` also starts the atomic queue of the rest.  One thread per
-// boundary, a binary search over the problems' weight prefix.
-__device__ __forceinline__ unsigned long long partition_boundary(const BProb* __restrict__ pr, int n, bool staged,
-                                                                 unsigned long long wstatic, unsigned long long total,
-                                                                 int parts, int b)
-{
-    const unsigned long long t = (unsigned long long)((double)wstatic * (double)b / (double)parts);
-    // first problem whose units of this executor end beyond weight t
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        const BProb& P = pr[mid];
-        const bool mine = (P.staged != 0) == staged;
-        const unsigned long long end = P.wbegin[staged ? 1 : 0] + (mine ? (unsigned long long)P.wunit * P.units : 0ull);
-        if (end > t) hi = mid;
-        else lo = mid + 1;
-    }
-    if (lo >= n) return total;
-    // the first problem whose units end beyond t carries weight, so it is one of this executor's
-    const BProb& P = pr[lo];
-    const unsigned long long k = (t - P.wbegin[staged ? 1 : 0] + P.wunit - 1) / P.wunit;
-    return P.unit_begin + (k < P.units ? k : P.units);
-}
-
-__global__ void batch_partition(const BProb* __restrict__ pr, int n, BCtl* ctl, unsigned long long* __restrict__ cta_begin,
-                                int parts, unsigned long long* __restrict__ warp_begin, int parts_r)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t <= parts) {
-        const unsigned long long ws = ctl->wtot * TLIBG_BATCH_STATIC_PCT / 100;
-        const unsigned long long u = partition_boundary(pr, n, false, ws, ctl->total, parts, t);
-        cta_begin[t] = u;
-        if (t == parts) ctl->head = u;
-    } else if (t <= parts + 1 + parts_r) {
-        const int b = t - parts - 1;
-        const unsigned long long ws = ctl->wtot_r * TLIBG_BATCH_STATIC_PCT / 100;
-        const unsigned long long u = partition_boundary(pr, n, true, ws, ctl->total_r, parts_r, b);
-        warp_begin[b] = u;
-        if (b == parts_r) ctl->head_r = u;
+        ctl->head_r = 0ull;
     }
 }
 
@@ -628,15 +566,17 @@ __device__ __forceinline__ void fetch_desc(BProb* dst, const BProb* __restrict__
     for (uint32_t w = lane; w < sizeof(BProb) / 4; w += 32) d[w] = __ldcg(src + w);
 }
 
-// CTA loop: its static range of units [cta_begin[b], cta_begin[b + 1]) in
-// order, then units from the atomic queue.  Warp 0 fetches the next unit's
-// problem descriptor into the other of two shared-memory slots while the CTA
-// works on the current unit, so no unit waits on a descriptor load; one CTA
-// barrier per unit (two more for a split problem's completion count).
+// CTA loop over units from the atomic queue.  Warp 0 keeps the queue two
+// units ahead: during unit k it claims unit k + 2 (the atomic's latency is
+// hidden by a whole unit) and reads unit k + 1's problem index (issued before
+// its share of unit k, used after it); the next descriptor goes into the other
+// of two shared-memory slots after warp 0's share of the work, copied within
+// shared memory when the problem is the same, read from L2 only when it
+// changes.  One CTA barrier per unit (two more for a split problem's
+// completion count).
 template <bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
-    batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map, BCtl* ctl, BPair* __restrict__ part,
-               const unsigned long long* __restrict__ cta_begin)
+    batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map, BCtl* ctl, BPair* __restrict__ part)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* red = reinterpret_cast<float*>(smem_raw);
@@ -647,27 +587,24 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total);
     const int record = *reinterpret_cast<volatile int*>(&ctl->record);
-    unsigned long long u_next = cta_begin[blockIdx.x];
-    const unsigned long long u_static_end = cta_begin[blockIdx.x + 1];
+    constexpr unsigned FULL = 0xffffffffu;
 
-    // warp 0: the unit after the current one and its descriptor, into `slot`
-    auto prepare = [&](int slot) {
-        unsigned long long u;
-        if (u_next < u_static_end) {
-            u = u_next++;
-        } else {
-            unsigned long long v = 0;
-            if (lane == 0) v = atomicAdd(&ctl->head, 1ull);
-            u = __shfl_sync(0xffffffffu, v, 0);
-        }
-        const int pi = u < total ? (int)__ldg(unit_map + u) : -1;
+    unsigned long long u_claim = 0;   // warp 0: the unit claimed for two iterations ahead
+    if (warp == 0) {
+        unsigned long long u0 = 0, u1 = 0;
         if (lane == 0) {
-            s_u[slot] = u;
-            s_p[slot] = pi;
+            u0 = atomicAdd(&ctl->head, 1ull);
+            u1 = atomicAdd(&ctl->head, 1ull);
         }
-        if (pi >= 0) fetch_desc(&s_desc[slot], pr, pi, lane);
-    };
-    if (warp == 0) prepare(0);
+        u0 = __shfl_sync(FULL, u0, 0);
+        u_claim = __shfl_sync(FULL, u1, 0);
+        const int p0 = u0 < total ? (int)__ldg(unit_map + u0) : -1;
+        if (lane == 0) {
+            s_u[0] = u0;
+            s_p[0] = p0;
+        }
+        if (p0 >= 0) fetch_desc(&s_desc[0], pr, p0, lane);
+    }
     __syncthreads();
     long long t_unit = 0;
     for (int k = 0;; ++k) {
@@ -675,9 +612,22 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
         const unsigned long long u = s_u[slot];
         if (u >= total) break;
         if (record && threadIdx.x == 0) t_unit = clock64();
-        if (warp == 0) prepare(slot ^ 1);
         const BProb& P = s_desc[slot];
         const int pi = s_p[slot];
+        // warp 0, before its share: the next unit (claimed last iteration), its
+        // problem index (load in flight during the work), the claim after it
+        unsigned long long u_nx = 0;
+        int p_nx = -1;
+        if (warp == 0) {
+            u_nx = u_claim;
+            if (u_nx < total) {
+                if (u_nx >= P.unit_begin && u_nx < P.unit_begin + P.units) p_nx = pi;
+                else p_nx = (int)__ldg(unit_map + u_nx);
+            }
+            unsigned long long c = 0;
+            if (lane == 0 && u_nx < total) c = atomicAdd(&ctl->head, 1ull);
+            u_claim = u_nx < total ? __shfl_sync(FULL, c, 0) : total;
+        }
         const uint64_t lu = u - P.unit_begin;
         if (P.kind == KIND_ROW) {
             switch (P.vec) {
@@ -690,6 +640,22 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
             case 4: col_unit<4, KAHAN>(P, lu, P.group, red, part); break;
             case 2: col_unit<2, KAHAN>(P, lu, P.group, red, part); break;
             default: col_unit<1, KAHAN>(P, lu, P.group, red, part); break;
+            }
+        }
+        if (warp == 0) {
+            // the next unit's descriptor into the other slot
+            if (lane == 0) {
+                s_u[slot ^ 1] = u_nx;
+                s_p[slot ^ 1] = p_nx;
+            }
+            if (p_nx >= 0) {
+                if (p_nx == pi) {
+                    const uint32_t* src = reinterpret_cast<const uint32_t*>(&s_desc[slot]);
+                    uint32_t* d = reinterpret_cast<uint32_t*>(&s_desc[slot ^ 1]);
+                    for (uint32_t w = lane; w < sizeof(BProb) / 4; w += 32) d[w] = src[w];
+                } else {
+                    fetch_desc(&s_desc[slot ^ 1], pr, p_nx, lane);
+                }
             }
         }
         if (P.nseg > 1) {
@@ -713,8 +679,7 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
 // --------------------------------------------------------------------------
 // staged row units: one lane per row from shared memory (variant 8)
 // --------------------------------------------------------------------------
-// Every warp works alone: its static range of units [warp_begin[w],
-// warp_begin[w + 1]), then units from the atomic queue; a unit is BRT_TPU
+// Every warp works alone, on units from the atomic queue; a unit is BRT_TPU
 // tiles of 32 R consecutive rows of one problem (contiguous in HBM).  Each
 // tile moves into the warp's two-stage ring with one TMA bulk copy (ragged
 // head and tail by plain loads), the problem's b beside it; the warp then
@@ -724,11 +689,10 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
 // the warp leaves once its copies in flight have landed (bounded).
 template <bool KAHAN>
 __global__ void __launch_bounds__(BRT_THREADS) batch_rowtile(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map_r,
-                                                             BCtl* ctl, const unsigned long long* __restrict__ warp_begin)
+                                                             BCtl* ctl)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint64_t gw = (uint64_t)blockIdx.x * BRT_WARPS + warp;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw) + warp * BRT_NS;
     unsigned char* wbase = smem_raw + 128 + (size_t)warp * BRT_WARP_BYTES;
     float* barea = reinterpret_cast<float*>(wbase);                        // [BRT_NS][BRT_MAX_NQ]
@@ -740,22 +704,15 @@ __global__ void __launch_bounds__(BRT_THREADS) batch_rowtile(BProb* __restrict__
     __syncwarp();
     const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total_r);
     const int record = *reinterpret_cast<volatile int*>(&ctl->record);
-    unsigned long long u_next = warp_begin[gw];
-    const unsigned long long u_static_end = warp_begin[gw + 1];
 
     // issue side: the problem and tile range of the unit being issued
     int iprob = -1;
     uint64_t it = 0, it_end = 0;
     auto advance = [&]() -> bool {
         while (it >= it_end) {
-            unsigned long long u;
-            if (u_next < u_static_end) {
-                u = u_next++;
-            } else {
-                unsigned long long v = 0;
-                if (lane == 0) v = atomicAdd(&ctl->head_r, 1ull);
-                u = __shfl_sync(0xffffffffu, v, 0);
-            }
+            unsigned long long v = 0;
+            if (lane == 0) v = atomicAdd(&ctl->head_r, 1ull);
+            const unsigned long long u = __shfl_sync(0xffffffffu, v, 0);
             if (u >= total) return false;
             iprob = (int)__ldg(unit_map_r + u);
             const BProb& P = pr[iprob];
@@ -938,8 +895,6 @@ struct tlibg_batch {
     BCtl* d_ctl = nullptr;
     uint32_t* d_map = nullptr;
     uint32_t* d_map_r = nullptr;
-    unsigned long long* d_cta_begin = nullptr;    // grid + 1 boundaries of batch_exec's static ranges
-    unsigned long long* d_warp_begin = nullptr;   // grid_r * BRT_WARPS + 1 of batch_rowtile's
     BPair* d_part = nullptr;
     float* d_model = nullptr;
     float log2_count = 0.f;
@@ -958,21 +913,15 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
         ++n;
     }
     batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map, bt->d_map_r);
-    const int wr = bt->grid_r * BRT_WARPS;
-    const int nb = bt->grid + 1 + wr + 1;
-    batch_partition<<<(nb + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_cta_begin, bt->grid,
-                                                      bt->d_warp_begin, wr);
     const size_t smem = exec_smem_bytes();
     if (bt->kahan) {
-        batch_exec<true><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part, bt->d_cta_begin);
-        batch_rowtile<true><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl,
-                                                                       bt->d_warp_begin);
+        batch_exec<true><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
+        batch_rowtile<true><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl);
     } else {
-        batch_exec<false><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part, bt->d_cta_begin);
-        batch_rowtile<false><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl,
-                                                                        bt->d_warp_begin);
+        batch_exec<false><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
+        batch_rowtile<false><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl);
     }
-    n += 4;
+    n += 3;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
     internal_count_launches(n);
@@ -981,7 +930,7 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
 
 int launches_per_run(const tlibg_batch* bt)
 {
-    return bt->select == TLIBG_SELECT_FIXED ? 5 : 4;
+    return bt->select == TLIBG_SELECT_FIXED ? 4 : 3;
 }
 
 void release(tlibg_batch* bt)
@@ -993,8 +942,6 @@ void release(tlibg_batch* bt)
     if (bt->d_ctl) cudaFree(bt->d_ctl);
     if (bt->d_map) cudaFree(bt->d_map);
     if (bt->d_map_r) cudaFree(bt->d_map_r);
-    if (bt->d_cta_begin) cudaFree(bt->d_cta_begin);
-    if (bt->d_warp_begin) cudaFree(bt->d_warp_begin);
     if (bt->d_part) cudaFree(bt->d_part);
     if (bt->d_model) cudaFree(bt->d_model);
     delete bt;
@@ -1163,8 +1110,6 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         (e = internal_malloc((void**)&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_map, std::max<uint64_t>(total_units, 1) * sizeof(uint32_t))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_map_r, std::max<uint64_t>(total_units_r, 1) * sizeof(uint32_t))) != cudaSuccess ||
-        (e = internal_malloc((void**)&bt->d_cta_begin, (size_t)(bt->grid + 1) * sizeof(unsigned long long))) != cudaSuccess ||
-        (e = internal_malloc((void**)&bt->d_warp_begin, (size_t)(bt->grid_r * BRT_WARPS + 1) * sizeof(unsigned long long))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
         (!model.empty() && (e = internal_malloc((void**)&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
         cudaGetLastError();
