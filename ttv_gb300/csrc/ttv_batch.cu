@@ -54,8 +54,10 @@ struct BProb {
     uint64_t unit_begin;   // first unit of the problem in its executor's unit space
     uint64_t part_off;     // in BPair elements
     uint64_t tiles;        // column units: tiles per segment
+    uint64_t tpu;          // column units: tiles per unit
+    uint64_t upseg;        // column units: units per segment
     IdxDiv pdiv;           // column units: output -> slice (division by P)
-    IdxDiv tdiv;           // column units: unit -> segment (division by tiles)
+    IdxDiv tdiv;           // column units: unit -> segment (division by the units per segment)
     IdxDiv sdiv;           // row units: item -> row (division by the segment count)
     float feat[NFEAT];
     int kind;
@@ -127,14 +129,28 @@ __host__ __device__ inline void decode_variant(int kind, int v, uint64_t nq, int
     *nseg = (uint32_t)ns;
 }
 
-// Row form: rounds of one row segment per lane group that make up a work unit,
-// so that a unit covers about 64 KB of A (per-unit queue overhead amortised).
+// Bytes of A a work unit covers: enough that the per-unit latency (claiming it,
+// its problem's descriptor, the first loads' round trip) is small next to the
+// unit's streaming time, few enough that the launch still ends level.
+#ifndef TLIBG_BATCH_UNIT_BYTES
+#define TLIBG_BATCH_UNIT_BYTES 131072
+#endif
+
+// Row form: rounds of one row segment per lane group that make up a work unit.
 __host__ __device__ inline uint64_t rows_per_group(uint64_t seg_len, int group)
 {
     const uint64_t gpc = BLOCK / group;
     const uint64_t per_round = gpc * seg_len * 4;
-    uint64_t r = (65536 + per_round - 1) / per_round;
-    return r < 1 ? 1 : (r > 64 ? 64 : r);
+    uint64_t r = (TLIBG_BATCH_UNIT_BYTES + per_round - 1) / per_round;
+    return r < 1 ? 1 : (r > 256 ? 256 : r);
+}
+
+// Column form: a unit is `tpu` consecutive tiles of one segment.
+__host__ __device__ inline uint64_t tiles_per_unit(uint64_t TO, uint64_t seg_len, uint64_t tiles)
+{
+    uint64_t t = TLIBG_BATCH_UNIT_BYTES / (TO * seg_len * 4);
+    if (t < 1) t = 1;
+    return t > tiles ? tiles : t;
 }
 
 __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uint64_t P, uint64_t nq,
@@ -149,7 +165,9 @@ __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uin
         return (S * ns + per_unit - 1) / per_unit;
     }
     const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * vec;
-    return (S * P + TO - 1) / TO * ns;
+    const uint64_t tiles = (S * P + TO - 1) / TO;
+    const uint64_t tpu = tiles_per_unit(TO, sl, tiles);
+    return (tiles + tpu - 1) / tpu * ns;
 }
 
 // --------------------------------------------------------------------------
@@ -238,8 +256,10 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
             if (P.kind == KIND_COL) {
                 const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * P.vec;
                 P.tiles = (outputs + TO - 1) / TO;
+                P.tpu = tiles_per_unit(TO, seg_len, P.tiles);
+                P.upseg = (P.tiles + P.tpu - 1) / P.tpu;
                 P.pdiv = make_idx_div(P.P, outputs);
-                P.tdiv = make_idx_div(P.tiles, P.tiles * nseg);
+                P.tdiv = make_idx_div(P.upseg, P.upseg * nseg);
             } else {
                 P.tiles = 0;
                 P.sdiv = make_idx_div(nseg, P.S * nseg);
@@ -446,7 +466,10 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
     }
 }
 
-// column unit: tile of TO outputs over one segment
+// column unit: `tpu` consecutive tiles of TO outputs over one segment; each
+// warp row walks its 32 V outputs of every tile in turn (its loads of the next
+// tile follow its last products of this one without a CTA barrier unless the
+// warps along q reduce through shared memory)
 template <int V, bool KAHAN>
 __device__ __forceinline__ void col_unit(const BProb& P, uint64_t lu, int WI, float* red, BPair* __restrict__ part)
 {
@@ -455,75 +478,80 @@ __device__ __forceinline__ void col_unit(const BProb& P, uint64_t lu, int WI, fl
     const uint32_t wi = warp % WI, wo = warp / WI;
     const uint64_t TO = (uint64_t)WO * 32u * V;
     const uint64_t outputs = P.S * P.P;
-    const uint64_t tiles = P.tiles;
-    const uint64_t seg = P.nseg == 1 ? 0 : idx_div(lu, P.tdiv), tile = lu - seg * tiles;
+    const uint64_t seg = P.nseg == 1 ? 0 : idx_div(lu, P.tdiv);
+    const uint64_t tile0 = (lu - seg * P.upseg) * P.tpu;
+    const uint64_t tile1 = min(P.tiles, tile0 + P.tpu);
     const uint64_t ib = seg * P.seg_len;
     const uint64_t ie = min(P.nq, ib + P.seg_len);
+    const uint64_t Pp = P.P, nq = P.nq;
+    const float* __restrict__ A = P.a;
     // b is read through L1 (warp-uniform per row)
     const float* __restrict__ bs = P.b;
     constexpr int U = (int)sizeof(float) * V >= 16 ? 4 : 64 / ((int)sizeof(float) * V);
 
-    const uint64_t o0 = tile * TO + ((uint64_t)wo * 32u + lane) * V;
-    const bool valid = o0 < outputs;
-    Acc<float, KAHAN> acc[V];
+    for (uint64_t tile = tile0; tile < tile1; ++tile) {
+        const uint64_t o0 = tile * TO + ((uint64_t)wo * 32u + lane) * V;
+        const bool valid = o0 < outputs;
+        Acc<float, KAHAN> acc[V];
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc[v].init();
-    if (valid) {
-        const uint64_t s = idx_div(o0, P.pdiv);
-        const uint64_t j = o0 - s * P.P;
-        const float* ap = P.a + (s * P.nq) * P.P + j;
-        uint64_t i = ib + wi;
-        for (; i + (U - 1) * WI < ie; i += U * WI) {
-            float av[U][V];
+        for (int v = 0; v < V; ++v) acc[v].init();
+        if (valid) {
+            const uint64_t s = idx_div(o0, P.pdiv);
+            const uint64_t j = o0 - s * Pp;
+            const float* ap = A + (s * nq) * Pp + j;
+            uint64_t i = ib + wi;
+            for (; i + (U - 1) * WI < ie; i += U * WI) {
+                float av[U][V];
 #pragma unroll
-            for (int u = 0; u < U; ++u) load_a<float, float, V>(ap + (i + u * WI) * P.P, av[u]);
+                for (int u = 0; u < U; ++u) load_a<float, float, V>(ap + (i + u * WI) * Pp, av[u]);
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const float bb = __ldg(bs + i + u * WI);
+                for (int u = 0; u < U; ++u) {
+                    const float bb = __ldg(bs + i + u * WI);
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
+                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
+                }
             }
-        }
 #pragma unroll 4
-        for (; i < ie; i += WI) {
-            float av[V];
-            load_a<float, float, V>(ap + i * P.P, av);
-            const float bb = __ldg(bs + i);
+            for (; i < ie; i += WI) {
+                float av[V];
+                load_a<float, float, V>(ap + i * Pp, av);
+                const float bb = __ldg(bs + i);
 #pragma unroll
-            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
-        }
-    }
-    if (WI > 1) {
-        const uint32_t slot = wo * 32u + lane;
-        if (wi > 0) {
-            float* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * V);
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                r[2 * v] = acc[v].s;
-                r[2 * v + 1] = acc[v].c;
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
             }
         }
-        __syncthreads();
-        if (wi == 0) {
-            for (uint32_t w = 1; w < (uint32_t)WI; ++w) {
-                const float* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * V);
+        if (WI > 1) {
+            const uint32_t slot = wo * 32u + lane;
+            if (wi > 0) {
+                float* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * V);
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].merge(r[2 * v], r[2 * v + 1]);
+                for (int v = 0; v < V; ++v) {
+                    r[2 * v] = acc[v].s;
+                    r[2 * v + 1] = acc[v].c;
+                }
             }
+            __syncthreads();
+            if (wi == 0) {
+                for (uint32_t w = 1; w < (uint32_t)WI; ++w) {
+                    const float* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].merge(r[2 * v], r[2 * v + 1]);
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
-    }
-    if (wi == 0 && valid) {
-        if (P.nseg == 1) {
+        if (wi == 0 && valid) {
+            if (P.nseg == 1) {
 #pragma unroll
-            for (int v = 0; v < V; ++v) P.c[o0 + v] = acc[v].value();
-        } else {
+                for (int v = 0; v < V; ++v) P.c[o0 + v] = acc[v].value();
+            } else {
 #pragma unroll
-            for (int v = 0; v < V; ++v) {
-                BPair pr;
-                pr.s = acc[v].s;
-                pr.c = KAHAN ? acc[v].c : 0.f;
-                part[P.part_off + seg * outputs + o0 + v] = pr;
+                for (int v = 0; v < V; ++v) {
+                    BPair pr;
+                    pr.s = acc[v].s;
+                    pr.c = KAHAN ? acc[v].c : 0.f;
+                    part[P.part_off + seg * outputs + o0 + v] = pr;
+                }
             }
         }
     }
@@ -557,77 +585,40 @@ __device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __r
 #define TLIBG_BATCH_MIN_CTAS 6
 #endif
 
-// Copy problem descriptor `pi` into shared memory (one warp, word by word).
-__device__ __forceinline__ void fetch_desc(BProb* dst, const BProb* __restrict__ pr, int pi, uint32_t lane)
-{
-    static_assert(sizeof(BProb) % 4 == 0, "descriptor copied in words");
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(pr + pi);
-    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-    for (uint32_t w = lane; w < sizeof(BProb) / 4; w += 32) d[w] = __ldcg(src + w);
-}
-
-// CTA loop over units from the atomic queue.  Warp 0 keeps the queue two
-// units ahead: during unit k it claims unit k + 2 (the atomic's latency is
-// hidden by a whole unit) and reads unit k + 1's problem index (issued before
-// its share of unit k, used after it); the next descriptor goes into the other
-// of two shared-memory slots after warp 0's share of the work, copied within
-// shared memory when the problem is the same, read from L2 only when it
-// changes.  One CTA barrier per unit (two more for a split problem's
-// completion count).
+// CTA loop over units from the atomic queue: thread 0 claims the next unit one
+// iteration ahead (the atomic's latency hidden by a whole unit) and reads its
+// problem index; one CTA barrier per unit (two more for a split problem's
+// completion count).  Units are large (TLIBG_BATCH_UNIT_BYTES of A) so the
+// per-unit latency -- the claim, the problem's descriptor, the first loads'
+// round trip -- is small next to a unit's streaming time.
 template <bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
     batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map, BCtl* ctl, BPair* __restrict__ part)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* red = reinterpret_cast<float*>(smem_raw);
-    __shared__ __align__(16) BProb s_desc[2];
-    __shared__ unsigned long long s_u[2];
-    __shared__ int s_p[2];
-    __shared__ int s_last;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    __shared__ unsigned long long s_unit;
+    __shared__ int s_prob, s_last;
     const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total);
     const int record = *reinterpret_cast<volatile int*>(&ctl->record);
-    constexpr unsigned FULL = 0xffffffffu;
-
-    unsigned long long u_claim = 0;   // warp 0: the unit claimed for two iterations ahead
-    if (warp == 0) {
-        unsigned long long u0 = 0, u1 = 0;
-        if (lane == 0) {
-            u0 = atomicAdd(&ctl->head, 1ull);
-            u1 = atomicAdd(&ctl->head, 1ull);
-        }
-        u0 = __shfl_sync(FULL, u0, 0);
-        u_claim = __shfl_sync(FULL, u1, 0);
-        const int p0 = u0 < total ? (int)__ldg(unit_map + u0) : -1;
-        if (lane == 0) {
-            s_u[0] = u0;
-            s_p[0] = p0;
-        }
-        if (p0 >= 0) fetch_desc(&s_desc[0], pr, p0, lane);
-    }
-    __syncthreads();
     long long t_unit = 0;
-    for (int k = 0;; ++k) {
-        const int slot = k & 1;
-        const unsigned long long u = s_u[slot];
+    unsigned long long next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(&ctl->head, 1ull);
+
+    while (true) {
+        if (threadIdx.x == 0) {
+            s_unit = next;
+            if (next < total) {
+                s_prob = (int)unit_map[next];
+                next = atomicAdd(&ctl->head, 1ull);   // consumed on the next iteration
+            }
+        }
+        __syncthreads();
+        const unsigned long long u = s_unit;
         if (u >= total) break;
         if (record && threadIdx.x == 0) t_unit = clock64();
-        const BProb& P = s_desc[slot];
-        const int pi = s_p[slot];
-        // warp 0, before its share: the next unit (claimed last iteration), its
-        // problem index (load in flight during the work), the claim after it
-        unsigned long long u_nx = 0;
-        int p_nx = -1;
-        if (warp == 0) {
-            u_nx = u_claim;
-            if (u_nx < total) {
-                if (u_nx >= P.unit_begin && u_nx < P.unit_begin + P.units) p_nx = pi;
-                else p_nx = (int)__ldg(unit_map + u_nx);
-            }
-            unsigned long long c = 0;
-            if (lane == 0 && u_nx < total) c = atomicAdd(&ctl->head, 1ull);
-            u_claim = u_nx < total ? __shfl_sync(FULL, c, 0) : total;
-        }
+        const int pi = s_prob;
+        const BProb& P = pr[pi];
         const uint64_t lu = u - P.unit_begin;
         if (P.kind == KIND_ROW) {
             switch (P.vec) {
@@ -640,22 +631,6 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
             case 4: col_unit<4, KAHAN>(P, lu, P.group, red, part); break;
             case 2: col_unit<2, KAHAN>(P, lu, P.group, red, part); break;
             default: col_unit<1, KAHAN>(P, lu, P.group, red, part); break;
-            }
-        }
-        if (warp == 0) {
-            // the next unit's descriptor into the other slot
-            if (lane == 0) {
-                s_u[slot ^ 1] = u_nx;
-                s_p[slot ^ 1] = p_nx;
-            }
-            if (p_nx >= 0) {
-                if (p_nx == pi) {
-                    const uint32_t* src = reinterpret_cast<const uint32_t*>(&s_desc[slot]);
-                    uint32_t* d = reinterpret_cast<uint32_t*>(&s_desc[slot ^ 1]);
-                    for (uint32_t w = lane; w < sizeof(BProb) / 4; w += 32) d[w] = src[w];
-                } else {
-                    fetch_desc(&s_desc[slot ^ 1], pr, p_nx, lane);
-                }
             }
         }
         if (P.nseg > 1) {
