@@ -69,16 +69,22 @@ struct BProb {
     uint32_t valid_mask;
     int heuristic;               // the fixed rule's variant (kept unless the model beats it by the margin)
     int staged;                  // this launch runs the problem in batch_rowtile (variant 8)
+    int cls;                     // executor class of this launch (CLS_*)
     unsigned int done;
     unsigned long long cycles;   // SM clock cycles spent on this problem's units (recording launches)
 };
 
+// Executor classes, one persistent kernel each (launched in turn):
+//   CLS_GENERIC  row units (lane groups) and column units with 8- or 16-byte loads
+//   CLS_COL1     column units with scalar loads (odd prefixes): two outputs per
+//                thread 32 apart, running row pointers, more loads in flight
+//   CLS_STAGED   staged short rows (variant 8)
+constexpr int CLS_GENERIC = 0, CLS_COL1 = 1, CLS_STAGED = 2, NCLS = 3;
+
 struct BCtl {
-    unsigned long long head;     // batch_exec's queue: next unit to hand out
-    unsigned long long total;    // batch_exec's units
-    unsigned long long head_r;   // the same for batch_rowtile
-    unsigned long long total_r;
-    int record;                  // nonzero: accumulate per-problem unit cycles
+    unsigned long long head[NCLS];    // each class's queue: next unit to hand out
+    unsigned long long total[NCLS];   // each class's units
+    int record;                       // nonzero: accumulate per-problem unit cycles
 };
 
 // Staged row units (variant 8, batch_rowtile): tiles of 32 R rows of at most
@@ -145,6 +151,14 @@ __host__ __device__ inline uint64_t rows_per_group(uint64_t seg_len, int group)
     return r < 1 ? 1 : (r > 256 ? 256 : r);
 }
 
+// Column form: outputs per thread (two, 32 apart, for scalar loads) and per
+// tile (the CTA's warp rows of 32 lanes).
+constexpr int COL1_MO = 2;
+__host__ __device__ inline uint64_t col_tile_outputs(int group, int vec)
+{
+    return (uint64_t)((BLOCK / 32) / group) * 32 * vec * (vec == 1 ? COL1_MO : 1);
+}
+
 // Column form: a unit is `tpu` consecutive tiles of one segment.
 __host__ __device__ inline uint64_t tiles_per_unit(uint64_t TO, uint64_t seg_len, uint64_t tiles)
 {
@@ -164,7 +178,7 @@ __host__ __device__ inline uint64_t unit_count(int kind, int group, int vec, uin
         const uint64_t per_unit = (BLOCK / group) * rows_per_group(sl, group);
         return (S * ns + per_unit - 1) / per_unit;
     }
-    const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * vec;
+    const uint64_t TO = col_tile_outputs(group, vec);
     const uint64_t tiles = (S * P + TO - 1) / TO;
     const uint64_t tpu = tiles_per_unit(TO, sl, tiles);
     return (tiles + tpu - 1) / tpu * ns;
@@ -224,10 +238,11 @@ __global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
 // --------------------------------------------------------------------------
 // plan: units, prefix sums, unit -> problem map, queue reset (one CTA)
 // --------------------------------------------------------------------------
-constexpr int PLAN_SUMS = 3;   // batch_exec units, split partials, batch_rowtile units
+constexpr int PLAN_SUMS = 4;   // units of the three executor classes, split partials
 
 __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl,
-                                                   uint32_t* __restrict__ unit_map, uint32_t* __restrict__ unit_map_r)
+                                                   uint32_t* __restrict__ map0, uint32_t* __restrict__ map1,
+                                                   uint32_t* __restrict__ map2)
 {
     __shared__ unsigned long long s_sum[PLAN_SUMS][32];
     __shared__ unsigned long long carry[PLAN_SUMS];
@@ -236,7 +251,7 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int base = 0; base < n; base += blockDim.x) {
         const int i = base + threadIdx.x;
-        unsigned long long x[PLAN_SUMS] = {0, 0, 0};
+        unsigned long long x[PLAN_SUMS] = {0, 0, 0, 0};
         if (i < n) {
             BProb& P = pr[i];
             if (!((P.valid_mask >> P.variant) & 1u)) P.variant = P.heuristic;   // not runnable: the fixed rule
@@ -254,7 +269,7 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
             P.cycles = 0ull;
             const uint64_t outputs = P.S * P.P;
             if (P.kind == KIND_COL) {
-                const uint64_t TO = (uint64_t)((BLOCK / 32) / group) * 32 * P.vec;
+                const uint64_t TO = col_tile_outputs(group, P.vec);
                 P.tiles = (outputs + TO - 1) / TO;
                 P.tpu = tiles_per_unit(TO, seg_len, P.tiles);
                 P.upseg = (P.tiles + P.tpu - 1) / P.tpu;
@@ -264,14 +279,14 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
                 P.tiles = 0;
                 P.sdiv = make_idx_div(nseg, P.S * nseg);
             }
+            P.cls = P.staged ? CLS_STAGED : (P.kind == KIND_COL && P.vec == 1 ? CLS_COL1 : CLS_GENERIC);
             if (P.staged) {
                 P.units = (uint32_t)brt_units(P.nq, P.S);
-                x[2] = P.units;
             } else {
                 P.units = (uint32_t)u;
-                x[0] = u;
-                x[1] = nseg > 1 ? (unsigned long long)nseg * outputs : 0ull;
+                x[3] = nseg > 1 ? (unsigned long long)nseg * outputs : 0ull;
             }
+            x[P.cls] = P.units;
         }
         // inclusive warp scans, then across warps
         unsigned long long y[PLAN_SUMS];
@@ -308,24 +323,18 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
         for (int c = 0; c < PLAN_SUMS; ++c) before[c] = carry[c] + (warp ? s_sum[c][warp - 1] : 0ull) + y[c] - x[c];
         if (i < n) {
             BProb& P = pr[i];
-            P.part_off = before[1];
-            if (P.staged) {
-                P.unit_begin = before[2];
-                for (unsigned long long k = 0; k < x[2]; ++k) unit_map_r[before[2] + k] = (uint32_t)i;
-            } else {
-                P.unit_begin = before[0];
-                for (unsigned long long k = 0; k < x[0]; ++k) unit_map[before[0] + k] = (uint32_t)i;
-            }
+            P.part_off = before[3];
+            P.unit_begin = before[P.cls];
+            uint32_t* map = P.cls == CLS_GENERIC ? map0 : (P.cls == CLS_COL1 ? map1 : map2);
+            for (unsigned long long k = 0; k < x[P.cls]; ++k) map[before[P.cls] + k] = (uint32_t)i;
         }
         __syncthreads();
         if (threadIdx.x < PLAN_SUMS) carry[threadIdx.x] += s_sum[threadIdx.x][(blockDim.x >> 5) - 1];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        ctl->total = carry[0];
-        ctl->head = 0ull;
-        ctl->total_r = carry[2];
-        ctl->head_r = 0ull;
+    if (threadIdx.x < NCLS) {
+        ctl->total[threadIdx.x] = carry[threadIdx.x];
+        ctl->head[threadIdx.x] = 0ull;
     }
 }
 
@@ -557,6 +566,122 @@ __device__ __forceinline__ void col_unit(const BProb& P, uint64_t lu, int WI, fl
     }
 }
 
+// Column unit with scalar loads (odd prefixes, or A at an odd offset): each
+// thread owns COL1_MO outputs 32 apart, so each row puts COL1_MO independent
+// coalesced warp loads in flight per thread, every output walks its column
+// with one running pointer (one 64-bit add per load), and blocks of
+// TLIBG_BATCH_COL1_LOADS loads (then halves, quarters, single rows) are issued
+// before their products.  An output past the end re-reads output o0's column
+// (its sum is never stored) instead of predicating every load.
+#ifndef TLIBG_BATCH_COL1_LOADS
+#define TLIBG_BATCH_COL1_LOADS 24
+#endif
+template <int UB, bool KAHAN>
+__device__ __forceinline__ void col1_rows(Acc<float, KAHAN> (&acc)[COL1_MO], const float* (&rp)[COL1_MO], uint64_t step,
+                                          const float* __restrict__ bs, uint64_t i, uint32_t WI)
+{
+    float av[UB][COL1_MO];
+#pragma unroll
+    for (int u = 0; u < UB; ++u)
+#pragma unroll
+        for (int m = 0; m < COL1_MO; ++m) {
+            av[u][m] = __ldcs(rp[m]);
+            rp[m] += step;
+        }
+#pragma unroll
+    for (int u = 0; u < UB; ++u) {
+        const float bb = __ldg(bs + i + u * WI);
+#pragma unroll
+        for (int m = 0; m < COL1_MO; ++m) acc[m].fma_add(av[u][m], bb);
+    }
+}
+
+template <bool KAHAN>
+__device__ __forceinline__ void col1_unit(const BProb& P, uint64_t lu, int WI, float* red, BPair* __restrict__ part)
+{
+    constexpr int MO = COL1_MO;
+    constexpr int U = TLIBG_BATCH_COL1_LOADS / MO;
+    const uint32_t WO = (BLOCK / 32) / WI;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t wi = warp % WI, wo = warp / WI;
+    const uint64_t TO = (uint64_t)WO * 32u * MO;
+    const uint64_t outputs = P.S * P.P;
+    const uint64_t seg = P.nseg == 1 ? 0 : idx_div(lu, P.tdiv);
+    const uint64_t tile0 = (lu - seg * P.upseg) * P.tpu;
+    const uint64_t tile1 = min(P.tiles, tile0 + P.tpu);
+    const uint64_t ib = seg * P.seg_len;
+    const uint64_t ie = min(P.nq, ib + P.seg_len);
+    const uint64_t Pp = P.P, nq = P.nq;
+    const float* __restrict__ A = P.a;
+    const float* __restrict__ bs = P.b;
+    const uint64_t step = (uint64_t)WI * Pp;
+
+    for (uint64_t tile = tile0; tile < tile1; ++tile) {
+        const uint64_t o0 = tile * TO + (uint64_t)wo * 32u * MO + lane;   // outputs o0 + 32 m
+        bool ok[MO];
+#pragma unroll
+        for (int m = 0; m < MO; ++m) ok[m] = o0 + 32u * m < outputs;
+        Acc<float, KAHAN> acc[MO];
+#pragma unroll
+        for (int m = 0; m < MO; ++m) acc[m].init();
+        if (ok[0]) {
+            const float* rp[MO];
+#pragma unroll
+            for (int m = 0; m < MO; ++m) {
+                const uint64_t o = ok[m] ? o0 + 32u * m : o0;
+                const uint64_t sl = idx_div(o, P.pdiv);
+                rp[m] = A + (sl * nq + ib + wi) * Pp + (o - sl * Pp);
+            }
+            uint64_t i = ib + wi;
+            for (; i + (U - 1) * WI < ie; i += U * WI) col1_rows<U>(acc, rp, step, bs, i, WI);
+            if (i + (U / 2 - 1) * WI < ie) {
+                col1_rows<U / 2>(acc, rp, step, bs, i, WI);
+                i += (U / 2) * WI;
+            }
+            if (i + (U / 4 - 1) * WI < ie) {
+                col1_rows<U / 4>(acc, rp, step, bs, i, WI);
+                i += (U / 4) * WI;
+            }
+            for (; i < ie; i += WI) col1_rows<1>(acc, rp, step, bs, i, WI);
+        }
+        if (WI > 1) {
+            const uint32_t slot = wo * 32u + lane;
+            if (wi > 0) {
+                float* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * MO);
+#pragma unroll
+                for (int m = 0; m < MO; ++m) {
+                    r[2 * m] = acc[m].s;
+                    r[2 * m + 1] = acc[m].c;
+                }
+            }
+            __syncthreads();
+            if (wi == 0) {
+                for (uint32_t w = 1; w < (uint32_t)WI; ++w) {
+                    const float* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * MO);
+#pragma unroll
+                    for (int m = 0; m < MO; ++m) acc[m].merge(r[2 * m], r[2 * m + 1]);
+                }
+            }
+            __syncthreads();
+        }
+        if (wi == 0) {
+#pragma unroll
+            for (int m = 0; m < MO; ++m) {
+                if (!ok[m]) continue;
+                const uint64_t o = o0 + 32u * m;
+                if (P.nseg == 1) {
+                    P.c[o] = acc[m].value();
+                } else {
+                    BPair pr;
+                    pr.s = acc[m].s;
+                    pr.c = KAHAN ? acc[m].c : 0.f;
+                    part[P.part_off + seg * outputs + o] = pr;
+                }
+            }
+        }
+    }
+}
+
 template <bool KAHAN>
 __device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __restrict__ part)
 {
@@ -585,32 +710,42 @@ __device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __r
 #define TLIBG_BATCH_MIN_CTAS 6
 #endif
 
-// CTA loop over units from the atomic queue: thread 0 claims the next unit one
-// iteration ahead (the atomic's latency hidden by a whole unit) and reads its
-// problem index; one CTA barrier per unit (two more for a split problem's
-// completion count).  Units are large (TLIBG_BATCH_UNIT_BYTES of A) so the
-// per-unit latency -- the claim, the problem's descriptor, the first loads'
-// round trip -- is small next to a unit's streaming time.
-template <bool KAHAN>
-__global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
+// Resident CTAs per SM the scalar-column executor is compiled for (more
+// registers per thread than the generic one: its loads in flight).
+#ifndef TLIBG_BATCH_COL1_MIN_CTAS
+#define TLIBG_BATCH_COL1_MIN_CTAS 4
+#endif
+template <int CLS> __host__ __device__ constexpr int exec_min_ctas()
+{
+    return CLS == CLS_COL1 ? TLIBG_BATCH_COL1_MIN_CTAS : TLIBG_BATCH_MIN_CTAS;
+}
+
+// CTA loop over the class's units from its atomic queue: thread 0 claims the
+// next unit one iteration ahead (the atomic's latency hidden by a whole unit)
+// and reads its problem index; one CTA barrier per unit (two more for a split
+// problem's completion count).  Units are large (TLIBG_BATCH_UNIT_BYTES of A)
+// so the per-unit latency -- the claim, the problem's descriptor, the first
+// loads' round trip -- is small next to a unit's streaming time.
+template <bool KAHAN, int CLS>
+__global__ void __launch_bounds__(BLOCK, exec_min_ctas<CLS>())
     batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map, BCtl* ctl, BPair* __restrict__ part)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* red = reinterpret_cast<float*>(smem_raw);
     __shared__ unsigned long long s_unit;
     __shared__ int s_prob, s_last;
-    const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total);
+    const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total[CLS]);
     const int record = *reinterpret_cast<volatile int*>(&ctl->record);
     long long t_unit = 0;
     unsigned long long next = 0;
-    if (threadIdx.x == 0) next = atomicAdd(&ctl->head, 1ull);
+    if (threadIdx.x == 0) next = atomicAdd(&ctl->head[CLS], 1ull);
 
     while (true) {
         if (threadIdx.x == 0) {
             s_unit = next;
             if (next < total) {
                 s_prob = (int)unit_map[next];
-                next = atomicAdd(&ctl->head, 1ull);   // consumed on the next iteration
+                next = atomicAdd(&ctl->head[CLS], 1ull);   // consumed on the next iteration
             }
         }
         __syncthreads();
@@ -620,7 +755,9 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
         const int pi = s_prob;
         const BProb& P = pr[pi];
         const uint64_t lu = u - P.unit_begin;
-        if (P.kind == KIND_ROW) {
+        if constexpr (CLS == CLS_COL1) {
+            col1_unit<KAHAN>(P, lu, P.group, red, part);
+        } else if (P.kind == KIND_ROW) {
             switch (P.vec) {
             case 4: row_unit<4, KAHAN>(P, lu, P.group, part); break;
             case 2: row_unit<2, KAHAN>(P, lu, P.group, part); break;
@@ -629,8 +766,7 @@ __global__ void __launch_bounds__(BLOCK, TLIBG_BATCH_MIN_CTAS)
         } else {
             switch (P.vec) {
             case 4: col_unit<4, KAHAN>(P, lu, P.group, red, part); break;
-            case 2: col_unit<2, KAHAN>(P, lu, P.group, red, part); break;
-            default: col_unit<1, KAHAN>(P, lu, P.group, red, part); break;
+            default: col_unit<2, KAHAN>(P, lu, P.group, red, part); break;
             }
         }
         if (P.nseg > 1) {
@@ -677,7 +813,7 @@ __global__ void __launch_bounds__(BRT_THREADS) batch_rowtile(BProb* __restrict__
         fence_mbar_init();
     }
     __syncwarp();
-    const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total_r);
+    const unsigned long long total = *reinterpret_cast<volatile unsigned long long*>(&ctl->total[CLS_STAGED]);
     const int record = *reinterpret_cast<volatile int*>(&ctl->record);
 
     // issue side: the problem and tile range of the unit being issued
@@ -686,7 +822,7 @@ __global__ void __launch_bounds__(BRT_THREADS) batch_rowtile(BProb* __restrict__
     auto advance = [&]() -> bool {
         while (it >= it_end) {
             unsigned long long v = 0;
-            if (lane == 0) v = atomicAdd(&ctl->head_r, 1ull);
+            if (lane == 0) v = atomicAdd(&ctl->head[CLS_STAGED], 1ull);
             const unsigned long long u = __shfl_sync(0xffffffffu, v, 0);
             if (u >= total) return false;
             iprob = (int)__ldg(unit_map_r + u);
@@ -790,17 +926,25 @@ size_t exec_smem_bytes()
     return red_floats * 4;
 }
 
-int exec_ctas_per_sm(bool kahan)
+// Resident CTAs per SM of a class's executor kernel (its launch grid is SMs x this).
+const void* exec_fn(bool kahan, int cls)
 {
-    static int cache[2] = {-1, -1};
+    if (cls == CLS_COL1)
+        return kahan ? reinterpret_cast<const void*>(batch_exec<true, CLS_COL1>)
+                     : reinterpret_cast<const void*>(batch_exec<false, CLS_COL1>);
+    return kahan ? reinterpret_cast<const void*>(batch_exec<true, CLS_GENERIC>)
+                 : reinterpret_cast<const void*>(batch_exec<false, CLS_GENERIC>);
+}
+
+int exec_ctas_per_sm(bool kahan, int cls)
+{
+    static int cache[2][2] = {{-1, -1}, {-1, -1}};
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
-    int& c = cache[kahan ? 1 : 0];
+    int& c = cache[kahan ? 1 : 0][cls == CLS_COL1 ? 1 : 0];
     if (c >= 0) return c;
-    const void* fn = kahan ? reinterpret_cast<const void*>(batch_exec<true>)
-                           : reinterpret_cast<const void*>(batch_exec<false>);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, exec_smem_bytes()) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, exec_fn(kahan, cls), BLOCK, exec_smem_bytes()) != cudaSuccess) {
         cudaGetLastError();
         n = 1;
     }
@@ -863,13 +1007,11 @@ struct tlibg_batch {
     int select = TLIBG_SELECT_HEURISTIC;
     int fixed_variant = 0;
     bool kahan = true;
-    int grid = 0;                 // batch_exec CTAs
-    int grid_r = 0;               // batch_rowtile CTAs
-    int slots = 1, slots_r = 1;   // resident CTAs (batch_exec) / warps (batch_rowtile) per SM
+    int grid[NCLS] = {0, 0, 0};    // CTAs of each class's kernel
+    int slots[NCLS] = {1, 1, 1};   // resident CTAs (staged rows: warps) per SM of each class
     BProb* d_prob = nullptr;
     BCtl* d_ctl = nullptr;
-    uint32_t* d_map = nullptr;
-    uint32_t* d_map_r = nullptr;
+    uint32_t* d_map[NCLS] = {nullptr, nullptr, nullptr};   // unit -> problem of each class
     BPair* d_part = nullptr;
     float* d_model = nullptr;
     float log2_count = 0.f;
@@ -887,16 +1029,18 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
         batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
         ++n;
     }
-    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map, bt->d_map_r);
+    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map[0], bt->d_map[1], bt->d_map[2]);
     const size_t smem = exec_smem_bytes();
     if (bt->kahan) {
-        batch_exec<true><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
-        batch_rowtile<true><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl);
+        batch_exec<true, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
+        batch_exec<true, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
+        batch_rowtile<true><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     } else {
-        batch_exec<false><<<bt->grid, BLOCK, smem, st>>>(bt->d_prob, bt->d_map, bt->d_ctl, bt->d_part);
-        batch_rowtile<false><<<bt->grid_r, BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map_r, bt->d_ctl);
+        batch_exec<false, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
+        batch_exec<false, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
+        batch_rowtile<false><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     }
-    n += 3;
+    n += 4;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
     internal_count_launches(n);
@@ -905,7 +1049,7 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
 
 int launches_per_run(const tlibg_batch* bt)
 {
-    return bt->select == TLIBG_SELECT_FIXED ? 4 : 3;
+    return bt->select == TLIBG_SELECT_FIXED ? 5 : 4;
 }
 
 void release(tlibg_batch* bt)
@@ -915,8 +1059,8 @@ void release(tlibg_batch* bt)
     if (bt->graph) cudaGraphDestroy(bt->graph);
     if (bt->d_prob) cudaFree(bt->d_prob);
     if (bt->d_ctl) cudaFree(bt->d_ctl);
-    if (bt->d_map) cudaFree(bt->d_map);
-    if (bt->d_map_r) cudaFree(bt->d_map_r);
+    for (int c = 0; c < NCLS; ++c)
+        if (bt->d_map[c]) cudaFree(bt->d_map[c]);
     if (bt->d_part) cudaFree(bt->d_part);
     if (bt->d_model) cudaFree(bt->d_model);
     delete bt;
@@ -1025,7 +1169,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
 
     // descriptors; unit map and partial scratch sized for the worst variant of each problem
     std::vector<BProb> hp(count);
-    uint64_t total_units = 0, max_part = 0, total_units_r = 0;
+    uint64_t total_units[NCLS] = {0, 0, 0}, max_part = 0;
     for (size_t i = 0; i < count; ++i) {
         const tlibg_problem& x = probs[i];
         s = internal_check_device_pointers(x.a, x.b, x.c);
@@ -1069,22 +1213,28 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
             const uint64_t nsr = (b.nq + sl - 1) / sl;
             if (nsr > 1) mp = std::max(mp, nsr * b.S * b.P);
         }
-        total_units += mu;
+        // units in the class the problem runs in unless staged (its kind and load width
+        // decide), and in the staged class where that variant applies
+        total_units[(b.kind == KIND_COL && b.vec == 1) ? CLS_COL1 : CLS_GENERIC] += mu;
         max_part += mp;
-        if ((b.valid_mask >> VARIANT_STAGED) & 1u) total_units_r += brt_units(b.nq, b.S);
+        if ((b.valid_mask >> VARIANT_STAGED) & 1u) total_units[CLS_STAGED] += brt_units(b.nq, b.S);
     }
-    bt->slots = exec_ctas_per_sm(bt->kahan);
-    bt->slots_r = rowtile_ctas_per_sm(bt->kahan) * BRT_WARPS;
-    bt->grid = sms * bt->slots;
-    bt->grid_r = sms * (bt->slots_r / BRT_WARPS);
-    if (total_units >= ((uint64_t)1 << 32) || total_units_r >= ((uint64_t)1 << 32))
-        return create_fail(bt, TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: more than 2^32 work units");
+    bt->slots[CLS_GENERIC] = exec_ctas_per_sm(bt->kahan, CLS_GENERIC);
+    bt->slots[CLS_COL1] = exec_ctas_per_sm(bt->kahan, CLS_COL1);
+    bt->slots[CLS_STAGED] = rowtile_ctas_per_sm(bt->kahan) * BRT_WARPS;
+    bt->grid[CLS_GENERIC] = sms * bt->slots[CLS_GENERIC];
+    bt->grid[CLS_COL1] = sms * bt->slots[CLS_COL1];
+    bt->grid[CLS_STAGED] = sms * (bt->slots[CLS_STAGED] / BRT_WARPS);
+    for (int c = 0; c < NCLS; ++c)
+        if (total_units[c] >= ((uint64_t)1 << 32))
+            return create_fail(bt, TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: more than 2^32 work units");
 
     cudaError_t e = cudaSuccess;
     if ((e = internal_malloc((void**)&bt->d_prob, count * sizeof(BProb))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
-        (e = internal_malloc((void**)&bt->d_map, std::max<uint64_t>(total_units, 1) * sizeof(uint32_t))) != cudaSuccess ||
-        (e = internal_malloc((void**)&bt->d_map_r, std::max<uint64_t>(total_units_r, 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_map[0], std::max<uint64_t>(total_units[0], 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_map[1], std::max<uint64_t>(total_units[1], 1) * sizeof(uint32_t))) != cudaSuccess ||
+        (e = internal_malloc((void**)&bt->d_map[2], std::max<uint64_t>(total_units[2], 1) * sizeof(uint32_t))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
         (!model.empty() && (e = internal_malloc((void**)&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
         cudaGetLastError();
@@ -1194,9 +1344,10 @@ int tlibg_batch_costs(tlibg_batch* bt, uint64_t* cycles, void* stream)
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return internal_cuda_fail(e, "tlibg_batch_costs");
     // SM cycles: a unit's CTA (or, staged, warp) cycles over the CTAs (warps) resident per SM
-    for (int i = 0; i < bt->count; ++i)
-        cycles[i] = (hp[i].cycles + (uint64_t)(hp[i].staged ? bt->slots_r : bt->slots) / 2) /
-                    (uint64_t)(hp[i].staged ? bt->slots_r : bt->slots);
+    for (int i = 0; i < bt->count; ++i) {
+        const uint64_t sl = (uint64_t)bt->slots[hp[i].cls];
+        cycles[i] = (hp[i].cycles + sl / 2) / sl;
+    }
     return internal_ok();
 }
 
