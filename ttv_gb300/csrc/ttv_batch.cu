@@ -75,20 +75,11 @@ struct BProb {
 };
 
 // Executor classes, one persistent kernel each (launched in turn):
-//   CLS_COLV     column units with 8- or 16-byte loads
+//   CLS_GENERIC  row units (lane groups) and column units with 8- or 16-byte loads
 //   CLS_COL1     column units with scalar loads (odd prefixes): two outputs per
 //                thread 32 apart, running row pointers, more loads in flight
 //   CLS_STAGED   staged short rows (variant 8)
-//   CLS_ROW      row units (lane groups per row)
-// Each kernel carries only its units' code, so each gets its own register
-// budget and occupancy target.
-constexpr int CLS_COLV = 0, CLS_COL1 = 1, CLS_STAGED = 2, CLS_ROW = 3, NCLS = 4;
-
-// class of a problem that is not staged: by kernel family and load width
-__host__ __device__ inline int exec_class(int kind, int vec)
-{
-    return kind == KIND_ROW ? CLS_ROW : (vec == 1 ? CLS_COL1 : CLS_COLV);
-}
+constexpr int CLS_GENERIC = 0, CLS_COL1 = 1, CLS_STAGED = 2, NCLS = 3;
 
 struct BCtl {
     unsigned long long head[NCLS];    // each class's queue: next unit to hand out
@@ -247,11 +238,11 @@ __global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
 // --------------------------------------------------------------------------
 // plan: units, prefix sums, unit -> problem map, queue reset (one CTA)
 // --------------------------------------------------------------------------
-constexpr int PLAN_SUMS = NCLS + 1;   // units of each executor class, split partials
+constexpr int PLAN_SUMS = 4;   // units of the three executor classes, split partials
 
 __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl,
                                                    uint32_t* __restrict__ map0, uint32_t* __restrict__ map1,
-                                                   uint32_t* __restrict__ map2, uint32_t* __restrict__ map3)
+                                                   uint32_t* __restrict__ map2)
 {
     __shared__ unsigned long long s_sum[PLAN_SUMS][32];
     __shared__ unsigned long long carry[PLAN_SUMS];
@@ -260,7 +251,7 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int base = 0; base < n; base += blockDim.x) {
         const int i = base + threadIdx.x;
-        unsigned long long x[PLAN_SUMS] = {0, 0, 0, 0, 0};
+        unsigned long long x[PLAN_SUMS] = {0, 0, 0, 0};
         if (i < n) {
             BProb& P = pr[i];
             if (!((P.valid_mask >> P.variant) & 1u)) P.variant = P.heuristic;   // not runnable: the fixed rule
@@ -288,12 +279,12 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
                 P.tiles = 0;
                 P.sdiv = make_idx_div(nseg, P.S * nseg);
             }
-            P.cls = P.staged ? CLS_STAGED : exec_class(P.kind, P.vec);
+            P.cls = P.staged ? CLS_STAGED : (P.kind == KIND_COL && P.vec == 1 ? CLS_COL1 : CLS_GENERIC);
             if (P.staged) {
                 P.units = (uint32_t)brt_units(P.nq, P.S);
             } else {
                 P.units = (uint32_t)u;
-                x[NCLS] = nseg > 1 ? (unsigned long long)nseg * outputs : 0ull;
+                x[3] = nseg > 1 ? (unsigned long long)nseg * outputs : 0ull;
             }
             x[P.cls] = P.units;
         }
@@ -332,9 +323,9 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
         for (int c = 0; c < PLAN_SUMS; ++c) before[c] = carry[c] + (warp ? s_sum[c][warp - 1] : 0ull) + y[c] - x[c];
         if (i < n) {
             BProb& P = pr[i];
-            P.part_off = before[NCLS];
+            P.part_off = before[3];
             P.unit_begin = before[P.cls];
-            uint32_t* map = P.cls == CLS_COLV ? map0 : (P.cls == CLS_COL1 ? map1 : (P.cls == CLS_STAGED ? map2 : map3));
+            uint32_t* map = P.cls == CLS_GENERIC ? map0 : (P.cls == CLS_COL1 ? map1 : map2);
             for (unsigned long long k = 0; k < x[P.cls]; ++k) map[before[P.cls] + k] = (uint32_t)i;
         }
         __syncthreads();
@@ -724,13 +715,9 @@ __device__ __forceinline__ void combine_problem(const BProb& P, const BPair* __r
 #ifndef TLIBG_BATCH_COL1_MIN_CTAS
 #define TLIBG_BATCH_COL1_MIN_CTAS 4
 #endif
-// ... and the row executor (lane groups per row)
-#ifndef TLIBG_BATCH_ROW_MIN_CTAS
-#define TLIBG_BATCH_ROW_MIN_CTAS 6
-#endif
 template <int CLS> __host__ __device__ constexpr int exec_min_ctas()
 {
-    return CLS == CLS_COL1 ? TLIBG_BATCH_COL1_MIN_CTAS : (CLS == CLS_ROW ? TLIBG_BATCH_ROW_MIN_CTAS : TLIBG_BATCH_MIN_CTAS);
+    return CLS == CLS_COL1 ? TLIBG_BATCH_COL1_MIN_CTAS : TLIBG_BATCH_MIN_CTAS;
 }
 
 // CTA loop over the class's units from its atomic queue: thread 0 claims the
@@ -770,7 +757,7 @@ __global__ void __launch_bounds__(BLOCK, exec_min_ctas<CLS>())
         const uint64_t lu = u - P.unit_begin;
         if constexpr (CLS == CLS_COL1) {
             col1_unit<KAHAN>(P, lu, P.group, red, part);
-        } else if constexpr (CLS == CLS_ROW) {
+        } else if (P.kind == KIND_ROW) {
             switch (P.vec) {
             case 4: row_unit<4, KAHAN>(P, lu, P.group, part); break;
             case 2: row_unit<2, KAHAN>(P, lu, P.group, part); break;
@@ -942,25 +929,19 @@ size_t exec_smem_bytes()
 // Resident CTAs per SM of a class's executor kernel (its launch grid is SMs x this).
 const void* exec_fn(bool kahan, int cls)
 {
-    switch (cls) {
-    case CLS_COL1:
+    if (cls == CLS_COL1)
         return kahan ? reinterpret_cast<const void*>(batch_exec<true, CLS_COL1>)
                      : reinterpret_cast<const void*>(batch_exec<false, CLS_COL1>);
-    case CLS_ROW:
-        return kahan ? reinterpret_cast<const void*>(batch_exec<true, CLS_ROW>)
-                     : reinterpret_cast<const void*>(batch_exec<false, CLS_ROW>);
-    default:
-        return kahan ? reinterpret_cast<const void*>(batch_exec<true, CLS_COLV>)
-                     : reinterpret_cast<const void*>(batch_exec<false, CLS_COLV>);
-    }
+    return kahan ? reinterpret_cast<const void*>(batch_exec<true, CLS_GENERIC>)
+                 : reinterpret_cast<const void*>(batch_exec<false, CLS_GENERIC>);
 }
 
 int exec_ctas_per_sm(bool kahan, int cls)
 {
-    static int cache[2][NCLS] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
+    static int cache[2][2] = {{-1, -1}, {-1, -1}};
     static std::mutex mu;
     std::lock_guard<std::mutex> lk(mu);
-    int& c = cache[kahan ? 1 : 0][cls];
+    int& c = cache[kahan ? 1 : 0][cls == CLS_COL1 ? 1 : 0];
     if (c >= 0) return c;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, exec_fn(kahan, cls), BLOCK, exec_smem_bytes()) != cudaSuccess) {
@@ -1026,11 +1007,11 @@ struct tlibg_batch {
     int select = TLIBG_SELECT_HEURISTIC;
     int fixed_variant = 0;
     bool kahan = true;
-    int grid[NCLS] = {0, 0, 0, 0};    // CTAs of each class's kernel
-    int slots[NCLS] = {1, 1, 1, 1};   // resident CTAs (staged rows: warps) per SM of each class
+    int grid[NCLS] = {0, 0, 0};    // CTAs of each class's kernel
+    int slots[NCLS] = {1, 1, 1};   // resident CTAs (staged rows: warps) per SM of each class
     BProb* d_prob = nullptr;
     BCtl* d_ctl = nullptr;
-    uint32_t* d_map[NCLS] = {nullptr, nullptr, nullptr, nullptr};   // unit -> problem of each class
+    uint32_t* d_map[NCLS] = {nullptr, nullptr, nullptr};   // unit -> problem of each class
     BPair* d_part = nullptr;
     float* d_model = nullptr;
     float log2_count = 0.f;
@@ -1048,21 +1029,18 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
         batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
         ++n;
     }
-    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map[0], bt->d_map[1], bt->d_map[2],
-                                   bt->d_map[3]);
+    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map[0], bt->d_map[1], bt->d_map[2]);
     const size_t smem = exec_smem_bytes();
     if (bt->kahan) {
-        batch_exec<true, CLS_COLV><<<bt->grid[CLS_COLV], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[CLS_COLV], bt->d_ctl, bt->d_part);
-        batch_exec<true, CLS_COL1><<<bt->grid[CLS_COL1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[CLS_COL1], bt->d_ctl, bt->d_part);
-        batch_exec<true, CLS_ROW><<<bt->grid[CLS_ROW], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[CLS_ROW], bt->d_ctl, bt->d_part);
-        batch_rowtile<true><<<bt->grid[CLS_STAGED], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[CLS_STAGED], bt->d_ctl);
+        batch_exec<true, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
+        batch_exec<true, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
+        batch_rowtile<true><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     } else {
-        batch_exec<false, CLS_COLV><<<bt->grid[CLS_COLV], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[CLS_COLV], bt->d_ctl, bt->d_part);
-        batch_exec<false, CLS_COL1><<<bt->grid[CLS_COL1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[CLS_COL1], bt->d_ctl, bt->d_part);
-        batch_exec<false, CLS_ROW><<<bt->grid[CLS_ROW], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[CLS_ROW], bt->d_ctl, bt->d_part);
-        batch_rowtile<false><<<bt->grid[CLS_STAGED], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[CLS_STAGED], bt->d_ctl);
+        batch_exec<false, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
+        batch_exec<false, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
+        batch_rowtile<false><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     }
-    n += 1 + NCLS;
+    n += 4;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
     internal_count_launches(n);
@@ -1071,7 +1049,7 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
 
 int launches_per_run(const tlibg_batch* bt)
 {
-    return (bt->select == TLIBG_SELECT_FIXED ? 2 : 1) + NCLS;
+    return bt->select == TLIBG_SELECT_FIXED ? 5 : 4;
 }
 
 void release(tlibg_batch* bt)
@@ -1191,7 +1169,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
 
     // descriptors; unit map and partial scratch sized for the worst variant of each problem
     std::vector<BProb> hp(count);
-    uint64_t total_units[NCLS] = {0, 0, 0, 0}, max_part = 0;
+    uint64_t total_units[NCLS] = {0, 0, 0}, max_part = 0;
     for (size_t i = 0; i < count; ++i) {
         const tlibg_problem& x = probs[i];
         s = internal_check_device_pointers(x.a, x.b, x.c);
@@ -1237,15 +1215,15 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         }
         // units in the class the problem runs in unless staged (its kind and load width
         // decide), and in the staged class where that variant applies
-        total_units[exec_class(b.kind, b.vec)] += mu;
+        total_units[(b.kind == KIND_COL && b.vec == 1) ? CLS_COL1 : CLS_GENERIC] += mu;
         max_part += mp;
         if ((b.valid_mask >> VARIANT_STAGED) & 1u) total_units[CLS_STAGED] += brt_units(b.nq, b.S);
     }
-    for (int c : {CLS_COLV, CLS_COL1, CLS_ROW}) {
-        bt->slots[c] = exec_ctas_per_sm(bt->kahan, c);
-        bt->grid[c] = sms * bt->slots[c];
-    }
+    bt->slots[CLS_GENERIC] = exec_ctas_per_sm(bt->kahan, CLS_GENERIC);
+    bt->slots[CLS_COL1] = exec_ctas_per_sm(bt->kahan, CLS_COL1);
     bt->slots[CLS_STAGED] = rowtile_ctas_per_sm(bt->kahan) * BRT_WARPS;
+    bt->grid[CLS_GENERIC] = sms * bt->slots[CLS_GENERIC];
+    bt->grid[CLS_COL1] = sms * bt->slots[CLS_COL1];
     bt->grid[CLS_STAGED] = sms * (bt->slots[CLS_STAGED] / BRT_WARPS);
     for (int c = 0; c < NCLS; ++c)
         if (total_units[c] >= ((uint64_t)1 << 32))
@@ -1257,7 +1235,6 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         (e = internal_malloc((void**)&bt->d_map[0], std::max<uint64_t>(total_units[0], 1) * sizeof(uint32_t))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_map[1], std::max<uint64_t>(total_units[1], 1) * sizeof(uint32_t))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_map[2], std::max<uint64_t>(total_units[2], 1) * sizeof(uint32_t))) != cudaSuccess ||
-        (e = internal_malloc((void**)&bt->d_map[3], std::max<uint64_t>(total_units[3], 1) * sizeof(uint32_t))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_part, std::max<uint64_t>(max_part, 1) * sizeof(BPair))) != cudaSuccess ||
         (!model.empty() && (e = internal_malloc((void**)&bt->d_model, MLP_PARAMS * sizeof(float))) != cudaSuccess)) {
         cudaGetLastError();
