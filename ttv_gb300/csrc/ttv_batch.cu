@@ -75,9 +75,10 @@ struct BProb {
 };
 
 // Executor classes, one persistent kernel each (launched in turn):
-//   CLS_GENERIC  row units (lane groups) and column units with 8- or 16-byte loads
-//   CLS_COL1     column units with scalar loads (odd prefixes): two outputs per
-//                thread 32 apart, running row pointers, more loads in flight
+//   CLS_GENERIC  row units (lane groups) and column units with 16-byte loads
+//   CLS_COL1     column units with scalar or 8-byte loads (prefixes that are
+//                odd, or even but not a multiple of 4): two vectors per thread
+//                32 vectors apart, running row pointers, more loads in flight
 //   CLS_STAGED   staged short rows (variant 8)
 constexpr int CLS_GENERIC = 0, CLS_COL1 = 1, CLS_STAGED = 2, NCLS = 3;
 
@@ -151,12 +152,12 @@ __host__ __device__ inline uint64_t rows_per_group(uint64_t seg_len, int group)
     return r < 1 ? 1 : (r > 256 ? 256 : r);
 }
 
-// Column form: outputs per thread (two, 32 apart, for scalar loads) and per
-// tile (the CTA's warp rows of 32 lanes).
+// Column form: vectors per thread (two, 32 vectors apart, for scalar and
+// 8-byte loads) and outputs per tile (the CTA's warp rows of 32 lanes).
 constexpr int COL1_MO = 2;
 __host__ __device__ inline uint64_t col_tile_outputs(int group, int vec)
 {
-    return (uint64_t)((BLOCK / 32) / group) * 32 * vec * (vec == 1 ? COL1_MO : 1);
+    return (uint64_t)((BLOCK / 32) / group) * 32 * vec * (vec <= 2 ? COL1_MO : 1);
 }
 
 // Column form: a unit is `tpu` consecutive tiles of one segment.
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
                 P.tiles = 0;
                 P.sdiv = make_idx_div(nseg, P.S * nseg);
             }
-            P.cls = P.staged ? CLS_STAGED : (P.kind == KIND_COL && P.vec == 1 ? CLS_COL1 : CLS_GENERIC);
+            P.cls = P.staged ? CLS_STAGED : (P.kind == KIND_COL && P.vec <= 2 ? CLS_COL1 : CLS_GENERIC);
             if (P.staged) {
                 P.units = (uint32_t)brt_units(P.nq, P.S);
             } else {
@@ -566,45 +567,63 @@ __device__ __forceinline__ void col_unit(const BProb& P, uint64_t lu, int WI, fl
     }
 }
 
-// Column unit with scalar loads (odd prefixes, or A at an odd offset): each
-// thread owns COL1_MO outputs 32 apart, so each row puts COL1_MO independent
-// coalesced warp loads in flight per thread, every output walks its column
-// with one running pointer (one 64-bit add per load), and blocks of
-// TLIBG_BATCH_COL1_LOADS loads (then halves, quarters, single rows) are issued
-// before their products.  An output past the end re-reads output o0's column
-// (its sum is never stored) instead of predicating every load.
+// Column unit with narrow loads (V = 1: odd prefixes or A at an odd offset;
+// V = 2: prefixes even but not a multiple of 4): each thread owns COL1_MO
+// vectors of V outputs, 32 vectors apart, so each row puts COL1_MO
+// independent coalesced warp loads in flight per thread; every vector walks
+// its column with one running pointer (one 64-bit add per load), and blocks of
+// TLIBG_BATCH_COL1_LOADS scalar (TLIBG_BATCH_COL2_LOADS 8-byte) loads -- then
+// halves, quarters, single rows -- are issued before their products.  A vector
+// past the end re-reads vector 0's column (its sums are never stored) instead
+// of predicating every load.
 #ifndef TLIBG_BATCH_COL1_LOADS
 #define TLIBG_BATCH_COL1_LOADS 24
 #endif
-template <int UB, bool KAHAN>
-__device__ __forceinline__ void col1_rows(Acc<float, KAHAN> (&acc)[COL1_MO], const float* (&rp)[COL1_MO], uint64_t step,
-                                          const float* __restrict__ bs, uint64_t i, uint32_t WI)
+#ifndef TLIBG_BATCH_COL2_LOADS
+#define TLIBG_BATCH_COL2_LOADS 16
+#endif
+template <int V> __device__ __forceinline__ void load_narrow(const float* p, float (&out)[V])
 {
-    float av[UB][COL1_MO];
+    if constexpr (V == 1) {
+        out[0] = __ldcs(p);
+    } else {
+        const float2 t = __ldcs(reinterpret_cast<const float2*>(p));
+        out[0] = t.x;
+        out[1] = t.y;
+    }
+}
+
+template <int UB, int V, bool KAHAN>
+__device__ __forceinline__ void coln_rows(Acc<float, KAHAN> (&acc)[COL1_MO][V], const float* (&rp)[COL1_MO],
+                                          uint64_t step, const float* __restrict__ bs, uint64_t i, uint32_t WI)
+{
+    float av[UB][COL1_MO][V];
 #pragma unroll
     for (int u = 0; u < UB; ++u)
 #pragma unroll
         for (int m = 0; m < COL1_MO; ++m) {
-            av[u][m] = __ldcs(rp[m]);
+            load_narrow<V>(rp[m], av[u][m]);
             rp[m] += step;
         }
 #pragma unroll
     for (int u = 0; u < UB; ++u) {
         const float bb = __ldg(bs + i + u * WI);
 #pragma unroll
-        for (int m = 0; m < COL1_MO; ++m) acc[m].fma_add(av[u][m], bb);
+        for (int m = 0; m < COL1_MO; ++m)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[m][v].fma_add(av[u][m][v], bb);
     }
 }
 
-template <bool KAHAN>
-__device__ __forceinline__ void col1_unit(const BProb& P, uint64_t lu, int WI, float* red, BPair* __restrict__ part)
+template <int V, bool KAHAN>
+__device__ __forceinline__ void coln_unit(const BProb& P, uint64_t lu, int WI, float* red, BPair* __restrict__ part)
 {
     constexpr int MO = COL1_MO;
-    constexpr int U = TLIBG_BATCH_COL1_LOADS / MO;
+    constexpr int U = (V == 1 ? TLIBG_BATCH_COL1_LOADS : TLIBG_BATCH_COL2_LOADS) / MO;
     const uint32_t WO = (BLOCK / 32) / WI;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t wi = warp % WI, wo = warp / WI;
-    const uint64_t TO = (uint64_t)WO * 32u * MO;
+    const uint64_t TO = (uint64_t)WO * 32u * V * MO;
     const uint64_t outputs = P.S * P.P;
     const uint64_t seg = P.nseg == 1 ? 0 : idx_div(lu, P.tdiv);
     const uint64_t tile0 = (lu - seg * P.upseg) * P.tpu;
@@ -617,49 +636,56 @@ __device__ __forceinline__ void col1_unit(const BProb& P, uint64_t lu, int WI, f
     const uint64_t step = (uint64_t)WI * Pp;
 
     for (uint64_t tile = tile0; tile < tile1; ++tile) {
-        const uint64_t o0 = tile * TO + (uint64_t)wo * 32u * MO + lane;   // outputs o0 + 32 m
+        // vector m of this thread: outputs o0 + 32 V m .. + V - 1
+        const uint64_t o0 = tile * TO + (uint64_t)wo * 32u * V * MO + (uint64_t)lane * V;
         bool ok[MO];
 #pragma unroll
-        for (int m = 0; m < MO; ++m) ok[m] = o0 + 32u * m < outputs;
-        Acc<float, KAHAN> acc[MO];
+        for (int m = 0; m < MO; ++m) ok[m] = o0 + 32u * V * m < outputs;
+        Acc<float, KAHAN> acc[MO][V];
 #pragma unroll
-        for (int m = 0; m < MO; ++m) acc[m].init();
+        for (int m = 0; m < MO; ++m)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[m][v].init();
         if (ok[0]) {
             const float* rp[MO];
 #pragma unroll
             for (int m = 0; m < MO; ++m) {
-                const uint64_t o = ok[m] ? o0 + 32u * m : o0;
+                const uint64_t o = ok[m] ? o0 + 32u * V * m : o0;
                 const uint64_t sl = idx_div(o, P.pdiv);
                 rp[m] = A + (sl * nq + ib + wi) * Pp + (o - sl * Pp);
             }
             uint64_t i = ib + wi;
-            for (; i + (U - 1) * WI < ie; i += U * WI) col1_rows<U>(acc, rp, step, bs, i, WI);
+            for (; i + (U - 1) * WI < ie; i += U * WI) coln_rows<U, V>(acc, rp, step, bs, i, WI);
             if (i + (U / 2 - 1) * WI < ie) {
-                col1_rows<U / 2>(acc, rp, step, bs, i, WI);
+                coln_rows<U / 2, V>(acc, rp, step, bs, i, WI);
                 i += (U / 2) * WI;
             }
             if (i + (U / 4 - 1) * WI < ie) {
-                col1_rows<U / 4>(acc, rp, step, bs, i, WI);
+                coln_rows<U / 4, V>(acc, rp, step, bs, i, WI);
                 i += (U / 4) * WI;
             }
-            for (; i < ie; i += WI) col1_rows<1>(acc, rp, step, bs, i, WI);
+            for (; i < ie; i += WI) coln_rows<1, V>(acc, rp, step, bs, i, WI);
         }
         if (WI > 1) {
             const uint32_t slot = wo * 32u + lane;
             if (wi > 0) {
-                float* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * MO);
+                float* r = red + ((size_t)(wi - 1) * (WO * 32u) + slot) * (2 * MO * V);
 #pragma unroll
-                for (int m = 0; m < MO; ++m) {
-                    r[2 * m] = acc[m].s;
-                    r[2 * m + 1] = acc[m].c;
-                }
+                for (int m = 0; m < MO; ++m)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        r[2 * (m * V + v)] = acc[m][v].s;
+                        r[2 * (m * V + v) + 1] = acc[m][v].c;
+                    }
             }
             __syncthreads();
             if (wi == 0) {
                 for (uint32_t w = 1; w < (uint32_t)WI; ++w) {
-                    const float* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * MO);
+                    const float* r = red + ((size_t)(w - 1) * (WO * 32u) + slot) * (2 * MO * V);
 #pragma unroll
-                    for (int m = 0; m < MO; ++m) acc[m].merge(r[2 * m], r[2 * m + 1]);
+                    for (int m = 0; m < MO; ++m)
+#pragma unroll
+                        for (int v = 0; v < V; ++v) acc[m][v].merge(r[2 * (m * V + v)], r[2 * (m * V + v) + 1]);
                 }
             }
             __syncthreads();
@@ -668,14 +694,17 @@ __device__ __forceinline__ void col1_unit(const BProb& P, uint64_t lu, int WI, f
 #pragma unroll
             for (int m = 0; m < MO; ++m) {
                 if (!ok[m]) continue;
-                const uint64_t o = o0 + 32u * m;
-                if (P.nseg == 1) {
-                    P.c[o] = acc[m].value();
-                } else {
-                    BPair pr;
-                    pr.s = acc[m].s;
-                    pr.c = KAHAN ? acc[m].c : 0.f;
-                    part[P.part_off + seg * outputs + o] = pr;
+                const uint64_t o = o0 + 32u * V * m;
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    if (P.nseg == 1) {
+                        P.c[o + v] = acc[m][v].value();
+                    } else {
+                        BPair pr;
+                        pr.s = acc[m][v].s;
+                        pr.c = KAHAN ? acc[m][v].c : 0.f;
+                        part[P.part_off + seg * outputs + o + v] = pr;
+                    }
                 }
             }
         }
@@ -756,7 +785,8 @@ __global__ void __launch_bounds__(BLOCK, exec_min_ctas<CLS>())
         const BProb& P = pr[pi];
         const uint64_t lu = u - P.unit_begin;
         if constexpr (CLS == CLS_COL1) {
-            col1_unit<KAHAN>(P, lu, P.group, red, part);
+            if (P.vec == 2) coln_unit<2, KAHAN>(P, lu, P.group, red, part);
+            else coln_unit<1, KAHAN>(P, lu, P.group, red, part);
         } else if (P.kind == KIND_ROW) {
             switch (P.vec) {
             case 4: row_unit<4, KAHAN>(P, lu, P.group, part); break;
@@ -764,10 +794,7 @@ __global__ void __launch_bounds__(BLOCK, exec_min_ctas<CLS>())
             default: row_unit<1, KAHAN>(P, lu, P.group, part); break;
             }
         } else {
-            switch (P.vec) {
-            case 4: col_unit<4, KAHAN>(P, lu, P.group, red, part); break;
-            default: col_unit<2, KAHAN>(P, lu, P.group, red, part); break;
-            }
+            col_unit<4, KAHAN>(P, lu, P.group, red, part);
         }
         if (P.nseg > 1) {
             __syncthreads();   // this CTA's partial stores are issued
@@ -1215,7 +1242,7 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
         }
         // units in the class the problem runs in unless staged (its kind and load width
         // decide), and in the staged class where that variant applies
-        total_units[(b.kind == KIND_COL && b.vec == 1) ? CLS_COL1 : CLS_GENERIC] += mu;
+        total_units[(b.kind == KIND_COL && b.vec <= 2) ? CLS_COL1 : CLS_GENERIC] += mu;
         max_part += mp;
         if ((b.valid_mask >> VARIANT_STAGED) & 1u) total_units[CLS_STAGED] += brt_units(b.nq, b.S);
     }
