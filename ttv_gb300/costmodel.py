@@ -193,35 +193,35 @@ def training_set(feats, times):
     return x[ok], y
 
 
-def derive_fixed_rule(feats, times):
-    """The best single variant per (kernel family, widest load) over tuned shapes:
-    the variant with the least total time in each class ({(kind, vec): v})."""
+def rule_class(feats):
+    """(kernel family, widest load, short row) of each shape: the classes the fixed
+    rule distinguishes (short: q-fastest rows of at most 64 elements, the ones the
+    staged variant can take)."""
     kind = np.where(feats[:, 2] > 0, 1, 0)          # log2 P > 0: column form
     vec = np.rint(feats[:, 7] * 4).astype(int)
+    nq = np.rint(2.0 ** (feats[:, 3].astype(np.float64) * 24))
+    short = ((kind == 0) & (nq <= 64)).astype(int)
+    return kind, vec, short
+
+
+def derive_fixed_rule(feats, times):
+    """The best single variant of each (kernel family, widest load, short row) class
+    over tuned shapes: the variant with the least total time in the class."""
+    kind, vec, short = rule_class(feats)
     rule = {}
     for k in (0, 1):
         for v in (1, 2, 4):
-            m = (kind == k) & (vec == v)
-            if m.any():
-                tot = np.where(np.isfinite(times[m]), times[m], np.inf).sum(axis=0)
-                rule[(k, v)] = int(np.argmin(tot))
+            for sh in (0, 1):
+                m = (kind == k) & (vec == v) & (short == sh)
+                if m.any():
+                    tot = np.where(np.isfinite(times[m]), times[m], np.inf).sum(axis=0)
+                    rule[(k, v, sh)] = int(np.argmin(tot))
     return rule
 
 
 def apply_fixed_rule(rule, feats):
-    kind = np.where(feats[:, 2] > 0, 1, 0)
-    vec = np.rint(feats[:, 7] * 4).astype(int)
-    return np.array([rule.get((k, v), 0) for k, v in zip(kind, vec)], np.int32)
-
-
-def train(feats, times, epochs=60, batch=512, lr=2e-3, seed=0):
-    import torch
-    x, y = training_set(feats, times)
-    dx = torch.from_numpy(x).cuda()
-    dy = torch.from_numpy(y).cuda()
-    params = torch.from_numpy(B.init_params(seed)).cuda()
-    losses = B.mlp_train(params, dx, dy, epochs=epochs, batch=batch, lr=lr, seed=seed)
-    return params.cpu().numpy(), losses
+    kind, vec, short = rule_class(feats)
+    return np.array([rule.get((k, v, sh), 0) for k, v, sh in zip(kind, vec, short)], np.int32)
 
 
 def predict_scores(params, feats, valid=None):
@@ -297,6 +297,9 @@ def main():
     # each (kernel family, widest load) class
     rule = derive_fixed_rule(feats[tr], times[tr])
     fixed = apply_fixed_rule(rule, feats)
+    if not args.reuse_db:   # the engine's rule is set to this one (the db records it)
+        np.savez_compressed(db_path, features=feats, times=times, heuristic=fixed, is_test=split,
+                            valid=valid, shapes=np.frombuffer(json.dumps(shapes).encode(), np.uint8))
     # the last tenth of the training shapes picks the selection margin
     tr_idx = np.where(tr)[0]
     fit, val = tr_idx[: len(tr_idx) * 9 // 10], tr_idx[len(tr_idx) * 9 // 10:]
@@ -317,7 +320,8 @@ def main():
     summary = {"train_shapes": int(len(fit)), "validation_shapes": int(len(val)),
                "test_shapes": int(te.sum()),
                "train_seconds": round(t_train, 2), "final_loss": float(losses[-1]),
-               "fixed_rule": {f"{'col' if k else 'row'}_vec{v}": r for (k, v), r in sorted(rule.items())},
+               "fixed_rule": {f"{'col' if k else 'row'}_vec{v}{'_short' if sh else ''}": r
+                              for (k, v, sh), r in sorted(rule.items())},
                "margin": margin, "validation_regret_by_margin": val_regret,
                "regret_learned": r_learn, "regret_learned_plain_argmin": r_argmin,
                "regret_fixed_rule": r_fixed_rule, "regret_engine_rule": r_engine_rule,

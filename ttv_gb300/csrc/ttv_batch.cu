@@ -241,9 +241,7 @@ __global__ void batch_set_variant(BProb* __restrict__ pr, int n, int v)
 // --------------------------------------------------------------------------
 constexpr int PLAN_SUMS = 4;   // units of the three executor classes, split partials
 
-__global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl,
-                                                   uint32_t* __restrict__ map0, uint32_t* __restrict__ map1,
-                                                   uint32_t* __restrict__ map2)
+__global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n, BCtl* ctl)
 {
     __shared__ unsigned long long s_sum[PLAN_SUMS][32];
     __shared__ unsigned long long carry[PLAN_SUMS];
@@ -326,8 +324,6 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
             BProb& P = pr[i];
             P.part_off = before[3];
             P.unit_begin = before[P.cls];
-            uint32_t* map = P.cls == CLS_GENERIC ? map0 : (P.cls == CLS_COL1 ? map1 : map2);
-            for (unsigned long long k = 0; k < x[P.cls]; ++k) map[before[P.cls] + k] = (uint32_t)i;
         }
         __syncthreads();
         if (threadIdx.x < PLAN_SUMS) carry[threadIdx.x] += s_sum[threadIdx.x][(blockDim.x >> 5) - 1];
@@ -337,6 +333,30 @@ __global__ void __launch_bounds__(1024) batch_plan(BProb* __restrict__ pr, int n
         ctl->total[threadIdx.x] = carry[threadIdx.x];
         ctl->head[threadIdx.x] = 0ull;
     }
+}
+
+// unit -> problem maps of the classes: one warp per problem, its lanes over its units
+__global__ void batch_fill_maps(const BProb* __restrict__ pr, int n, uint32_t* __restrict__ map0,
+                                uint32_t* __restrict__ map1, uint32_t* __restrict__ map2)
+{
+    const int i = (int)((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (i >= n) return;
+    const BProb& P = pr[i];
+    uint32_t* map = P.cls == CLS_GENERIC ? map0 : (P.cls == CLS_COL1 ? map1 : map2);
+    for (uint64_t k = lane; k < P.units; k += 32) map[P.unit_begin + k] = (uint32_t)i;
+}
+
+// Start of every launch of a planned batch: empty queues, completion counts and
+// recorded cycles.
+__global__ void batch_reset(BProb* __restrict__ pr, int n, BCtl* ctl)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        pr[i].done = 0u;
+        pr[i].cycles = 0ull;
+    }
+    if (i < NCLS) ctl->head[i] = 0ull;
 }
 
 // --------------------------------------------------------------------------
@@ -1043,20 +1063,41 @@ struct tlibg_batch {
     float* d_model = nullptr;
     float log2_count = 0.f;
     float log2_keep = 0.f;   // log2(1 - margin)
+    bool planned = false;          // the plan kernels ran for the current variants
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
 
 namespace {
 
-int enqueue(tlibg_batch* bt, cudaStream_t st)
+// The plan (variants -> units, queues, unit maps) runs once per variant set:
+// at creation and after a forced variant changes; every launch then only
+// resets the queues and counters and runs the class kernels.
+int enqueue_plan(tlibg_batch* bt, cudaStream_t st)
 {
     uint64_t n = 0;
     if (bt->select == TLIBG_SELECT_FIXED) {
         batch_set_variant<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->fixed_variant);
         ++n;
     }
-    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl, bt->d_map[0], bt->d_map[1], bt->d_map[2]);
+    batch_plan<<<1, 1024, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl);
+    batch_fill_maps<<<(bt->count + 7) / 8, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_map[0], bt->d_map[1],
+                                                        bt->d_map[2]);
+    n += 2;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return internal_cuda_fail(e, "batch plan");
+    internal_count_launches(n);
+    bt->planned = true;
+    return TLIBG_OK;
+}
+
+int enqueue(tlibg_batch* bt, cudaStream_t st)
+{
+    if (!bt->planned) {
+        const int s = enqueue_plan(bt, st);
+        if (s) return s;
+    }
+    batch_reset<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl);
     const size_t smem = exec_smem_bytes();
     if (bt->kahan) {
         batch_exec<true, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
@@ -1067,16 +1108,15 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
         batch_exec<false, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
         batch_rowtile<false><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     }
-    n += 4;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
-    internal_count_launches(n);
+    internal_count_launches(1 + NCLS);
     return TLIBG_OK;
 }
 
 int launches_per_run(const tlibg_batch* bt)
 {
-    return bt->select == TLIBG_SELECT_FIXED ? 5 : 4;
+    return 1 + NCLS;   // reset + the class kernels (the plan is not part of a launch)
 }
 
 void release(tlibg_batch* bt)
@@ -1285,6 +1325,11 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
             return internal_cuda_fail(e, "batch select");
         }
     }
+    // the plan runs once here (graph launches replay only reset + class kernels)
+    if ((s = enqueue_plan(bt, st))) {
+        release(bt);
+        return s;
+    }
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
         release(bt);
         return internal_cuda_fail(e, "tlibg_batch_create");
@@ -1346,6 +1391,7 @@ int tlibg_batch_set_variant(tlibg_batch* bt, int variant)
     if (variant < 0 || variant >= NVARIANT)
         return internal_fail(TLIBG_ERR_ARGUMENT,
                              "tlibg_batch_set_variant: variant must be in 0.." + std::to_string(NVARIANT - 1));
+    if (bt->fixed_variant != variant) bt->planned = false;
     bt->fixed_variant = variant;
     return internal_ok();
 }
