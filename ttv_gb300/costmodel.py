@@ -224,6 +224,16 @@ def apply_fixed_rule(rule, feats):
     return np.array([rule.get((k, v, sh), 0) for k, v, sh in zip(kind, vec, short)], np.int32)
 
 
+def train(feats, times, epochs=60, batch=512, lr=2e-3, seed=0):
+    import torch
+    x, y = training_set(feats, times)
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.from_numpy(y).cuda()
+    params = torch.from_numpy(B.init_params(seed)).cuda()
+    losses = B.mlp_train(params, dx, dy, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    return params.cpu().numpy(), losses
+
+
 def predict_scores(params, feats, valid=None):
     """Predicted log2 cost of every variant of every shape (the engine's inference
     kernel); variants a shape cannot run score +inf."""

@@ -1029,19 +1029,27 @@ int batch_vec(int kind, const CanonView& cn, const void* a, const void* b)
     return vec;
 }
 
-// The fixed rule the engine uses without the cost model.
+// The fixed rule the engine uses without the cost model: the best single
+// variant of each (kernel family, widest load, short row) class, re-derived
+// from the autotuner's data (ttv_gb300/data/tuning_db.npz, 20,000 training
+// shapes timed with every variant inside mixed batches; costmodel.py
+// derive_fixed_rule): q-fastest rows of at most 64 elements staged through
+// shared memory (variant 8), longer rows two lanes per row (variant 2),
+// column problems one warp row per tile and no split (variant 0), for every
+// load width.  Its aggregate time on held-out shapes is 2.5 % above
+// exhaustive tuning's.
+constexpr int FIXED_RULE[2][3][2] = {
+    // [kind][vec 1, 2, 4][long row, short row]
+    {{2, 8}, {2, 8}, {2, 8}},   // row form
+    {{0, 0}, {0, 0}, {0, 0}},   // column form
+};
 int heuristic_variant(int kind, uint64_t P, uint64_t nq, uint64_t S, int vec)
 {
-    // Row form: the first lane count (one lane per row); column form: one warp row
-    // per tile unless the problem has few outputs and a long contraction; never split.
-    (void)vec;
-    int g = 0;
-    if (kind == KIND_COL) {
-        const uint64_t outputs = S * P;
-        if (outputs < 512 && nq >= 128) g = 2;
-        else if (outputs < 2048 && nq >= 64) g = 1;
-    }
-    return 2 * g;
+    (void)P;
+    (void)S;
+    const int vi = vec >= 4 ? 2 : (vec == 2 ? 1 : 0);
+    const int shrt = (kind == KIND_ROW && nq <= (uint64_t)BRT_MAX_NQ) ? 1 : 0;
+    return FIXED_RULE[kind == KIND_ROW ? 0 : 1][vi][shrt];
 }
 
 }  // namespace
