@@ -1072,6 +1072,8 @@ struct tlibg_batch {
     float log2_count = 0.f;
     float log2_keep = 0.f;   // log2(1 - margin)
     bool planned = false;          // the plan kernels ran for the current variants
+    cudaStream_t side[2] = {nullptr, nullptr};      // the scalar-column and staged-row kernels' streams
+    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -1106,16 +1108,26 @@ int enqueue(tlibg_batch* bt, cudaStream_t st)
         if (s) return s;
     }
     batch_reset<<<(bt->count + 255) / 256, 256, 0, st>>>(bt->d_prob, bt->count, bt->d_ctl);
+    // The class kernels are independent: the scalar-column and staged-row
+    // kernels go on two side streams forked from `st` (branches of the CUDA
+    // graph), so each one's CTAs fill the SMs the others' last units leave.
     const size_t smem = exec_smem_bytes();
+    cudaEventRecord(bt->ev_fork, st);
+    cudaStreamWaitEvent(bt->side[0], bt->ev_fork, 0);
+    cudaStreamWaitEvent(bt->side[1], bt->ev_fork, 0);
     if (bt->kahan) {
         batch_exec<true, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
-        batch_exec<true, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
-        batch_rowtile<true><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
+        batch_exec<true, CLS_COL1><<<bt->grid[1], BLOCK, smem, bt->side[0]>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
+        batch_rowtile<true><<<bt->grid[2], BRT_THREADS, BRT_SMEM, bt->side[1]>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     } else {
         batch_exec<false, CLS_GENERIC><<<bt->grid[0], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[0], bt->d_ctl, bt->d_part);
-        batch_exec<false, CLS_COL1><<<bt->grid[1], BLOCK, smem, st>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
-        batch_rowtile<false><<<bt->grid[2], BRT_THREADS, BRT_SMEM, st>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
+        batch_exec<false, CLS_COL1><<<bt->grid[1], BLOCK, smem, bt->side[0]>>>(bt->d_prob, bt->d_map[1], bt->d_ctl, bt->d_part);
+        batch_rowtile<false><<<bt->grid[2], BRT_THREADS, BRT_SMEM, bt->side[1]>>>(bt->d_prob, bt->d_map[2], bt->d_ctl);
     }
+    cudaEventRecord(bt->ev_join[0], bt->side[0]);
+    cudaEventRecord(bt->ev_join[1], bt->side[1]);
+    cudaStreamWaitEvent(st, bt->ev_join[0], 0);
+    cudaStreamWaitEvent(st, bt->ev_join[1], 0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return internal_cuda_fail(e, "batch launch");
     internal_count_launches(1 + NCLS);
@@ -1132,6 +1144,11 @@ void release(tlibg_batch* bt)
     if (!bt) return;
     if (bt->exec) cudaGraphExecDestroy(bt->exec);
     if (bt->graph) cudaGraphDestroy(bt->graph);
+    for (int i = 0; i < 2; ++i) {
+        if (bt->side[i]) cudaStreamDestroy(bt->side[i]);
+        if (bt->ev_join[i]) cudaEventDestroy(bt->ev_join[i]);
+    }
+    if (bt->ev_fork) cudaEventDestroy(bt->ev_fork);
     if (bt->d_prob) cudaFree(bt->d_prob);
     if (bt->d_ctl) cudaFree(bt->d_ctl);
     for (int c = 0; c < NCLS; ++c)
@@ -1305,6 +1322,15 @@ int tlibg_batch_create(int dtype, const tlibg_problem* probs, size_t count, cons
             return create_fail(bt, TLIBG_ERR_UNSUPPORTED, "tlibg_batch_create: more than 2^32 work units");
 
     cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        if ((e = cudaStreamCreateWithFlags(&bt->side[i], cudaStreamNonBlocking)) == cudaSuccess)
+            e = cudaEventCreateWithFlags(&bt->ev_join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bt->ev_fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        release(bt);
+        return internal_cuda_fail(e, "tlibg_batch_create: streams");
+    }
     if ((e = internal_malloc((void**)&bt->d_prob, count * sizeof(BProb))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_ctl, sizeof(BCtl))) != cudaSuccess ||
         (e = internal_malloc((void**)&bt->d_map[0], std::max<uint64_t>(total_units[0], 1) * sizeof(uint32_t))) != cudaSuccess ||
