@@ -568,8 +568,11 @@ def run_batched(T, torch, dev, args, n=4096, seed=4096):
                              "GB/s": round(nbytes / ms / 1e6, 1)}
     res["speedup_learned_vs_plain"] = round(res["plain_per_call"]["ms"] / res["learned"]["ms"], 3)
     res["speedup_learned_vs_fixed_rule"] = round(res["fixed_rule"]["ms"] / res["learned"]["ms"], 3)
-    res["l2"] = ("13.5 GB of A per launch, 100x L2: consecutive launches find no problem "
-                 "resident (no flush)")
+    l2x = nbytes / (129 << 20)
+    res["l2"] = (f"{nbytes / 1e9:.2f} GB of A and C per launch, {l2x:.0f}x L2: consecutive launches "
+                 "find no problem resident (no flush)" if l2x >= 4 else
+                 f"{nbytes / 1e9:.2f} GB per launch, {l2x:.1f}x L2: part of the previous launch may "
+                 "still be resident (no flush; a profiling-size case)")
     # accuracy of the learned launch on a sample of problems
     import oracle
     errs = []

@@ -779,7 +779,7 @@ template <bool KAHAN, int CLS>
 __global__ void __launch_bounds__(BLOCK, exec_min_ctas<CLS>())
     batch_exec(BProb* __restrict__ pr, const uint32_t* __restrict__ unit_map, BCtl* ctl, BPair* __restrict__ part)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     float* red = reinterpret_cast<float*>(smem_raw);
     __shared__ unsigned long long s_unit;
     __shared__ int s_prob, s_last;

@@ -2,23 +2,22 @@
 //
 // The reference's ttvpy.ttvs (ttvpy/src/wrapped_ttv.cpp:85-199) runs p - 1
 // separate TTVs, each reading the previous intermediate and allocating the
-// next.  Here the chain reads A once.  In the canonical view of A with
-// respect to q, A = (S, n_q, P) row-major (P: the extents laid out before q,
-// S: those after), the result is
-//
-//     c[i] = sum_s wS[s] * sum_j A[s, i, j] * wP[j],
-//
-// where wP and wS are the Kronecker products of the vectors of the prefix and
-// suffix modes (in layout order).  So the chain is
-//   1. kron_kernel      wP and wS from the p - 1 vectors (products in fp64,
-//                       rounded once to the element type)
-//   2. row TTV          D[s, i] = sum_j A[s, i, j] wP[j]: rows of the
-//                       contiguous prefix (the engine's row-form kernels;
-//                       skipped when P == 1)
-//   3. column TTV       c[i] = sum_s wS[s] D[s, i] (the column-form kernels;
-//                       skipped when S == 1)
-// with no host synchronisation and no allocation after the first call on a
-// stream (wP, wS, D and split partials live in the stream's cached scratch).
+// next.  Here the chain reads A once, in a short sequence of stages planned
+// on the host.  Walk the modes of A in layout order (fastest first); q sits
+// at position k.  A stage contracts a contiguous group of modes at one end
+// of the layout with the Kronecker product of their vectors (computed once,
+// in fp64 and rounded to the element type):
+//   * row stage (k > 0): the fastest modes, as few as make rows of at least
+//     CHAIN_MIN_ROW elements (or all modes before q): A is rows of that
+//     length, each dotted with the weights -- the engine's row-form kernels on
+//     many moderate rows instead of a few very long ones;
+//   * column stage (q fastest): the slowest modes, as many as leave at least
+//     CHAIN_MIN_OUTPUTS outputs (at least one mode): a column GEMV over them
+//     -- the engine's column-form kernels with plenty of outputs.
+// The first stage reads A (about all the traffic); each later one reads the
+// previous, much smaller, intermediate.  All weights come from one kernel
+// launch, intermediates live in the stream's cached scratch: no host
+// synchronisation and no allocation after the first call on a stream.
 // Every contraction order of the reference gives the same sum up to
 // rounding; this one reads A once whatever order is asked for.
 #include "ttv_internal.h"
@@ -29,38 +28,49 @@
 namespace tlibg {
 
 constexpr int KRON_MAX_MODES = 32;
+constexpr int KRON_MAX_GROUPS = KRON_MAX_MODES;   // one weight vector per stage
+#ifndef TLIBG_CHAIN_MIN_ROW
+#define TLIBG_CHAIN_MIN_ROW 2048
+#endif
+#ifndef TLIBG_CHAIN_MIN_OUTPUTS
+#define TLIBG_CHAIN_MIN_OUTPUTS 65536
+#endif
+constexpr uint64_t CHAIN_MIN_ROW = TLIBG_CHAIN_MIN_ROW;           // row stage: rows at least this long
+constexpr uint64_t CHAIN_MIN_OUTPUTS = TLIBG_CHAIN_MIN_OUTPUTS;   // column stage: at least this many outputs
 
+// Weight vectors of the stages: group g has modes [m0[g], m1[g]) of vec/ext
+// (fastest first, each new mode slower) and writes len[g] weights at
+// out + off[g] (elements; every group starts 256-byte aligned).
 struct KronArgs {
-    const void* vec[KRON_MAX_MODES];   // prefix modes first (layout order), then suffix modes
+    const void* vec[KRON_MAX_MODES];
     uint64_t ext[KRON_MAX_MODES];
-    int np, ns;                        // number of prefix / suffix modes
-    uint64_t P, S;
-    void* wP;
-    void* wS;
+    int m0[KRON_MAX_GROUPS], m1[KRON_MAX_GROUPS];
+    uint64_t off[KRON_MAX_GROUPS + 1];   // group starts; off[ngroups] = end of the last
+    uint64_t len[KRON_MAX_GROUPS];
+    int ngroups;
+    void* out;
 };
 
-// One weight per thread: the mixed-radix digits of its index pick one element
-// of each mode's vector.  I: 32-bit index arithmetic when P + S < 2^32 (one
-// 32-bit division per mode instead of a 64-bit one).
+// One weight per thread: the mixed-radix digits of its index within its group
+// pick one element of each of the group's vectors.  I: 32-bit index
+// arithmetic when the weights number fewer than 2^32.
 template <typename T, typename I>
 __global__ void kron_kernel(KronArgs k)
 {
-    const I P = (I)k.P, total = (I)(k.P + k.S);
+    const I total = (I)k.off[k.ngroups];
     for (I idx = (I)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
-        const bool pre = idx < P;
-        I j = pre ? idx : idx - P;
-        const int m0 = pre ? 0 : k.np, m1 = pre ? k.np : k.np + k.ns;
+        int g = 0;
+        while ((I)k.off[g + 1] <= idx) ++g;
+        I j = idx - (I)k.off[g];
+        if (j >= (I)k.len[g]) continue;   // alignment gap after the group
         double w = 1.0;
-        for (int m = m0; m < m1; ++m) {
+        for (int m = k.m0[g]; m < k.m1[g]; ++m) {
             const I e = (I)k.ext[m];
             const I q = j / e;
             w *= (double)static_cast<const T*>(k.vec[m])[j - q * e];
             j = q;
         }
-        if (pre)
-            static_cast<T*>(k.wP)[idx] = (T)w;
-        else
-            static_cast<T*>(k.wS)[idx - P] = (T)w;
+        static_cast<T*>(k.out)[idx] = (T)w;
     }
 }
 
@@ -122,68 +132,113 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
     for (size_t r = 0; r + 1 < p; ++r)
         if (int st = internal_check_device_pointers(bs[r], bs[r], bs[r])) return st;
 
-    // Kronecker factors: prefix modes in layout order (fastest first), then suffix modes
-    KronArgs ka{};
-    size_t k = 0;
-    while (pia[k] != q) ++k;
-    auto vec_of = [&](size_t mode) { return bs[mode < q ? mode - 1 : mode - 2]; };
-    int nm = 0;
-    for (size_t r = 0; r < k; ++r) {
-        ka.vec[nm] = vec_of(pia[r]);
-        ka.ext[nm++] = na[pia[r] - 1];
+    // modes in layout order, fastest first: extent and vector (q: none)
+    std::vector<uint64_t> ext;
+    std::vector<const void*> vec;
+    for (size_t r = 0; r < p; ++r) {
+        const size_t m = pia[r];
+        ext.push_back(na[m - 1]);
+        vec.push_back(m == q ? nullptr : bs[m < q ? m - 1 : m - 2]);
     }
-    ka.np = nm;
-    for (size_t r = k + 1; r < p; ++r) {
-        ka.vec[nm] = vec_of(pia[r]);
-        ka.ext[nm++] = na[pia[r] - 1];
-    }
-    ka.ns = nm - ka.np;
-    ka.P = cn.P;
-    ka.S = cn.S;
-    const uint64_t P = cn.P, S = cn.S, nq = cn.nq;
-    const bool stage1 = P > 1, stage2 = S > 1;
+    size_t kq = 0;
+    while (pia[kq] != q) ++kq;
 
-    // plans (pointers for the alignment rules: scratch regions are 256-byte aligned)
+    // stages: [lo, hi) modes of the current tensor contracted, row or column form
+    struct Stage {
+        bool row;
+        int m0, m1;        // modes of the weights, in the current tensor's order
+        uint64_t L, R;     // row: rows R of length L; column: outputs L, contracted rows R
+        uint64_t woff;     // offset of the weights (elements)
+    };
+    std::vector<Stage> stages;
+    KronArgs ka{};
+    int nv = 0;
+    uint64_t wtot = 0, N = 1;
+    for (uint64_t e : ext) N *= e;
+    {
+        std::vector<uint64_t> ex = ext;
+        std::vector<const void*> ve = vec;
+        size_t k = kq;
+        uint64_t n = N;
+        while (ex.size() > 1) {
+            Stage sg{};
+            size_t lo, hi;   // contracted modes [lo, hi) of the current tensor
+            if (k > 0) {
+                uint64_t L = 1;
+                hi = 0;
+                while (hi < k && (L < CHAIN_MIN_ROW || hi == 0)) L *= ex[hi++];
+                lo = 0;
+                sg.row = true;
+                sg.L = L;
+                sg.R = n / L;
+            } else {
+                uint64_t inner = ex[0];
+                lo = 1;
+                while (lo + 1 < ex.size() && inner < CHAIN_MIN_OUTPUTS) inner *= ex[lo++];
+                hi = ex.size();
+                sg.row = false;
+                sg.L = inner;
+                sg.R = n / inner;
+            }
+            sg.woff = wtot;
+            sg.m0 = nv;
+            for (size_t r = lo; r < hi; ++r) {
+                ka.vec[nv] = ve[r];
+                ka.ext[nv++] = ex[r];
+            }
+            sg.m1 = nv;
+            const uint64_t wl = sg.row ? sg.L : sg.R;
+            ka.m0[stages.size()] = sg.m0;
+            ka.m1[stages.size()] = sg.m1;
+            ka.off[stages.size()] = wtot;
+            ka.len[stages.size()] = wl;
+            wtot += align256(wl * et) / et;
+            stages.push_back(sg);
+            // the intermediate keeps the other modes, in the same order
+            ex.erase(ex.begin() + lo, ex.begin() + hi);
+            ve.erase(ve.begin() + lo, ve.begin() + hi);
+            if (sg.row) k -= hi;
+            n = sg.row ? sg.R : sg.L;
+        }
+    }
+    ka.ngroups = (int)stages.size();
+    ka.off[ka.ngroups] = wtot;
+
+    // plans and scratch: weights, two intermediates, split partials
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const size_t off_wP = 0;
-    const size_t off_wS = off_wP + align256(stage1 ? P * et : 0);
-    const size_t off_D = off_wS + align256(stage2 ? S * et : 0);
-    const size_t off_part = off_D + align256(stage1 && stage2 ? S * nq * et : 0);
-    static const uint4 probe[1] = {};   // 256-byte aligned stand-in for scratch regions
-    Plan pl1, pl2;
-    if (stage1) {
-        CanonView c1;
-        c1.P = 1;
-        c1.nq = P;
-        c1.S = S * nq;
-        if (int s = internal_plan(dtype, c1, a, probe, nullptr, sms, &pl1)) return s;
+    static const uint4 probe[1] = {};   // aligned stand-in for scratch regions
+    std::vector<Plan> plans(stages.size());
+    size_t part_bytes = 0, inter = 0;
+    for (size_t i = 0; i < stages.size(); ++i) {
+        const Stage& sg = stages[i];
+        CanonView cv;
+        if (sg.row) {
+            cv.P = 1;
+            cv.nq = sg.L;
+            cv.S = sg.R;
+        } else {
+            cv.P = sg.L;
+            cv.nq = sg.R;
+            cv.S = 1;
+        }
+        const int dt = i == 0 ? dtype : tdt;
+        if (int s = internal_plan(dt, cv, i == 0 ? a : (const void*)probe, probe, nullptr, sms, &plans[i])) return s;
+        part_bytes = std::max(part_bytes, partial_bytes(plans[i]));
+        if (i + 1 < stages.size()) inter = std::max<size_t>(inter, (size_t)(sg.row ? sg.R : sg.L));
     }
-    if (stage2) {
-        CanonView c2;
-        c2.P = nq;
-        c2.nq = S;
-        c2.S = 1;
-        if (int s = internal_plan(stage1 ? tdt : dtype, c2, stage1 ? (const void*)probe : a, probe, nullptr, sms, &pl2))
-            return s;
-    }
-    const size_t part_bytes = std::max(stage1 ? partial_bytes(pl1) : 0, stage2 ? partial_bytes(pl2) : 0);
+    const size_t off_w = 0;
+    const size_t off_d0 = off_w + align256(wtot * et);
+    const size_t off_d1 = off_d0 + align256(inter * et);
+    const size_t off_part = off_d1 + align256(stages.size() > 2 ? inter * et : 0);
     void* scratch = nullptr;
     if (int s = internal_scratch(st, off_part + part_bytes, &scratch)) return s;
     char* base = static_cast<char*>(scratch);
-    void* wP = base + off_wP;
-    void* wS = base + off_wS;
-    void* D = stage1 && stage2 ? base + off_D : c;
-    void* part = base + off_part;
-    ka.wP = wP;
-    ka.wS = wS;
+    ka.out = base + off_w;
 
     uint64_t launches = 0;
-    const uint64_t nk = (stage1 ? P : 0) + (stage2 ? S : 0);
-    if (!stage1) ka.P = 0;
-    if (!stage2) ka.S = 0;
-    if (nk) {
-        const int grid = (int)std::min<uint64_t>((uint64_t)sms * 8, (nk + 255) / 256);
-        const bool narrow = nk < (uint64_t(1) << 32);
+    {
+        const int grid = (int)std::min<uint64_t>((uint64_t)sms * 8, (wtot + 255) / 256);
+        const bool narrow = wtot < (uint64_t(1) << 32);
         if (tdt == F64) {
             if (narrow) kron_kernel<double, uint32_t><<<grid, 256, 0, st>>>(ka);
             else kron_kernel<double, uint64_t><<<grid, 256, 0, st>>>(ka);
@@ -195,13 +250,14 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
         ++launches;
     }
-    if (stage1) {
-        cudaError_t e = launch_plan(pl1, a, wP, D, part, st, &launches);
+    const void* in = a;
+    for (size_t i = 0; i < stages.size(); ++i) {
+        const bool last = i + 1 == stages.size();
+        void* out = last ? c : base + ((i & 1) ? off_d1 : off_d0);
+        const void* w = base + off_w + stages[i].woff * et;
+        cudaError_t e = launch_plan(plans[i], in, w, out, base + off_part, st, &launches);
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
-    }
-    if (stage2) {
-        cudaError_t e = launch_plan(pl2, stage1 ? D : a, wS, c, part, st, &launches);
-        if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
+        in = out;
     }
     internal_count_launches(launches);
     return internal_ok();
