@@ -648,6 +648,17 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
                 if (ns >= 1 && (double)cost(ns) < 0.98 * (double)base && cost(ns) < cost(best)) best = ns;
             }
             nseg = best;
+        } else if (cn.S < 16 * slots) {
+            // Many rows, but few rounds of them: 16384 rows over 4864 lane groups take 4
+            // rounds, the last a third full.  Two to four segments per row fill the rounds
+            // better (2 segments: 7 rounds of half rows, 12.5 % less); taken when they cut
+            // rounds x segment length by more than 2 %.
+            const uint64_t min_len = (uint64_t)V * G * 16;
+            auto cost = [&](uint64_t ns) { return cdiv(cn.S * ns, slots) * cdiv(cn.nq, ns); };
+            const uint64_t base = cost(1);
+            for (uint64_t ns = 2; ns <= 4; ++ns)
+                if (cn.nq / ns >= min_len && (double)cost(ns) < 0.98 * (double)base && cost(ns) < cost(nseg))
+                    nseg = ns;
         }
         nseg = std::max<uint64_t>(1, std::min<uint64_t>(nseg, cn.nq));
         uint64_t seg_len = cdiv(cn.nq, nseg);

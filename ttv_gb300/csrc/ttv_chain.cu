@@ -22,7 +22,10 @@
 // rounding; this one reads A once whatever order is asked for.
 #include "ttv_internal.h"
 
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace tlibg {
@@ -77,6 +80,35 @@ __global__ void kron_kernel(KronArgs k)
 namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// A side stream and its fork / join events per (device, caller stream), created
+// on first use and kept for the life of the process.
+struct SideStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
+
+int side_stream(cudaStream_t caller, SideStream** out)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, cudaStream_t>, SideStream> cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return internal_cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(dev, caller);
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+        SideStream s{};
+        e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return internal_cuda_fail(e, "side stream");
+        it = cache.emplace(key, s).first;
+    }
+    *out = &it->second;
+    return 0;
+}
 
 const char* const E_ORDER = "Error calling ttvpy::ttvs: input tensor order should be greater than zero.";
 const char* const E_MODE =
@@ -146,9 +178,9 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
     // stages: [lo, hi) modes of the current tensor contracted, row or column form
     struct Stage {
         bool row;
-        int m0, m1;        // modes of the weights, in the current tensor's order
+        int group;         // weight group of the Kronecker launch, or -1: one mode, its vector
+        const void* w;     // the vector (group < 0)
         uint64_t L, R;     // row: rows R of length L; column: outputs L, contracted rows R
-        uint64_t woff;     // offset of the weights (elements)
     };
     std::vector<Stage> stages;
     KronArgs ka{};
@@ -161,12 +193,17 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
         size_t k = kq;
         uint64_t n = N;
         while (ex.size() > 1) {
+            // The first stage reads A: rows long enough (row form) or outputs enough
+            // (column form) for the engine's kernels to stream at full rate.  Later
+            // stages read an intermediate that is orders of magnitude smaller: each
+            // takes all remaining modes on its side of q, so at most two follow.
+            const bool first = stages.empty();
             Stage sg{};
-            size_t lo, hi;   // contracted modes [lo, hi) of the current tensor
+            size_t lo, hi;
             if (k > 0) {
                 uint64_t L = 1;
                 hi = 0;
-                while (hi < k && (L < CHAIN_MIN_ROW || hi == 0)) L *= ex[hi++];
+                while (hi < k && (!first || L < CHAIN_MIN_ROW || hi == 0)) L *= ex[hi++];
                 lo = 0;
                 sg.row = true;
                 sg.L = L;
@@ -174,25 +211,29 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
             } else {
                 uint64_t inner = ex[0];
                 lo = 1;
-                while (lo + 1 < ex.size() && inner < CHAIN_MIN_OUTPUTS) inner *= ex[lo++];
+                while (first && lo + 1 < ex.size() && inner < CHAIN_MIN_OUTPUTS) inner *= ex[lo++];
                 hi = ex.size();
                 sg.row = false;
                 sg.L = inner;
                 sg.R = n / inner;
             }
-            sg.woff = wtot;
-            sg.m0 = nv;
-            for (size_t r = lo; r < hi; ++r) {
-                ka.vec[nv] = ve[r];
-                ka.ext[nv++] = ex[r];
+            if (hi - lo == 1) {
+                sg.group = -1;
+                sg.w = ve[lo];
+            } else {
+                const int g = ka.ngroups++;
+                sg.group = g;
+                ka.m0[g] = nv;
+                for (size_t r = lo; r < hi; ++r) {
+                    ka.vec[nv] = ve[r];
+                    ka.ext[nv++] = ex[r];
+                }
+                ka.m1[g] = nv;
+                const uint64_t wl = sg.row ? sg.L : sg.R;
+                ka.off[g] = wtot;
+                ka.len[g] = wl;
+                wtot += align256(wl * et) / et;
             }
-            sg.m1 = nv;
-            const uint64_t wl = sg.row ? sg.L : sg.R;
-            ka.m0[stages.size()] = sg.m0;
-            ka.m1[stages.size()] = sg.m1;
-            ka.off[stages.size()] = wtot;
-            ka.len[stages.size()] = wl;
-            wtot += align256(wl * et) / et;
             stages.push_back(sg);
             // the intermediate keeps the other modes, in the same order
             ex.erase(ex.begin() + lo, ex.begin() + hi);
@@ -201,7 +242,6 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
             n = sg.row ? sg.R : sg.L;
         }
     }
-    ka.ngroups = (int)stages.size();
     ka.off[ka.ngroups] = wtot;
 
     // plans and scratch: weights, two intermediates, split partials
@@ -222,7 +262,8 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
             cv.S = 1;
         }
         const int dt = i == 0 ? dtype : tdt;
-        if (int s = internal_plan(dt, cv, i == 0 ? a : (const void*)probe, probe, nullptr, sms, &plans[i])) return s;
+        const void* pw = sg.group < 0 ? sg.w : (const void*)probe;
+        if (int s = internal_plan(dt, cv, i == 0 ? a : (const void*)probe, pw, nullptr, sms, &plans[i])) return s;
         part_bytes = std::max(part_bytes, partial_bytes(plans[i]));
         if (i + 1 < stages.size()) inter = std::max<size_t>(inter, (size_t)(sg.row ? sg.R : sg.L));
     }
@@ -235,26 +276,47 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
     char* base = static_cast<char*>(scratch);
     ka.out = base + off_w;
 
+    // The weights: one launch for every group.  When the first stage contracts a
+    // single mode it needs none of them, and the launch runs beside it on a
+    // side stream (forked from and joined back to the caller's stream).
     uint64_t launches = 0;
-    {
+    const bool overlap = ka.ngroups > 0 && stages[0].group < 0;
+    SideStream* side = nullptr;
+    if (overlap) {
+        if (int s = side_stream(st, &side)) return s;
+        cudaError_t e = cudaEventRecord(side->fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream, side->fork, 0);
+        if (e != cudaSuccess) return internal_cuda_fail(e, "stream fork");
+    }
+    if (ka.ngroups > 0) {
+        cudaStream_t ks = overlap ? side->stream : st;
         const int grid = (int)std::min<uint64_t>((uint64_t)sms * 8, (wtot + 255) / 256);
         const bool narrow = wtot < (uint64_t(1) << 32);
         if (tdt == F64) {
-            if (narrow) kron_kernel<double, uint32_t><<<grid, 256, 0, st>>>(ka);
-            else kron_kernel<double, uint64_t><<<grid, 256, 0, st>>>(ka);
+            if (narrow) kron_kernel<double, uint32_t><<<grid, 256, 0, ks>>>(ka);
+            else kron_kernel<double, uint64_t><<<grid, 256, 0, ks>>>(ka);
         } else {
-            if (narrow) kron_kernel<float, uint32_t><<<grid, 256, 0, st>>>(ka);
-            else kron_kernel<float, uint64_t><<<grid, 256, 0, st>>>(ka);
+            if (narrow) kron_kernel<float, uint32_t><<<grid, 256, 0, ks>>>(ka);
+            else kron_kernel<float, uint64_t><<<grid, 256, 0, ks>>>(ka);
         }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
         ++launches;
+        if (overlap) {
+            e = cudaEventRecord(side->join, side->stream);
+            if (e != cudaSuccess) return internal_cuda_fail(e, "stream join");
+        }
     }
     const void* in = a;
     for (size_t i = 0; i < stages.size(); ++i) {
         const bool last = i + 1 == stages.size();
         void* out = last ? c : base + ((i & 1) ? off_d1 : off_d0);
-        const void* w = base + off_w + stages[i].woff * et;
+        const Stage& sg = stages[i];
+        const void* w = sg.group < 0 ? sg.w : base + off_w + ka.off[sg.group] * et;
+        if (overlap && i == 1) {
+            cudaError_t e = cudaStreamWaitEvent(st, side->join, 0);
+            if (e != cudaSuccess) return internal_cuda_fail(e, "stream join");
+        }
         cudaError_t e = launch_plan(plans[i], in, w, out, base + off_part, st, &launches);
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
         in = out;
