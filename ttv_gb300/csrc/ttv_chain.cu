@@ -40,6 +40,8 @@ constexpr int KRON_MAX_GROUPS = KRON_MAX_MODES;   // one weight vector per stage
 #endif
 constexpr uint64_t CHAIN_MIN_ROW = TLIBG_CHAIN_MIN_ROW;           // row stage: rows at least this long
 constexpr uint64_t CHAIN_MIN_OUTPUTS = TLIBG_CHAIN_MIN_OUTPUTS;   // column stage: at least this many outputs
+constexpr uint64_t CHAIN_SMALL = uint64_t(1) << 22;   // intermediates up to this many elements: one stage
+constexpr uint64_t CHAIN_LATE_OUTPUTS = 4096;         // larger ones: column stages keep this many outputs
 
 // Weight vectors of the stages: group g has modes [m0[g], m1[g]) of vec/ext
 // (fastest first, each new mode slower) and writes len[g] weights at
@@ -196,7 +198,9 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
             // The first stage reads A: rows long enough (row form) or outputs enough
             // (column form) for the engine's kernels to stream at full rate.  Later
             // stages read an intermediate that is orders of magnitude smaller: each
-            // takes all remaining modes on its side of q, so at most two follow.
+            // takes all remaining modes on its side of q (a column stage over an
+            // intermediate of more than CHAIN_SMALL elements stops at
+            // CHAIN_LATE_OUTPUTS outputs), so one to three follow.
             const bool first = stages.empty();
             Stage sg{};
             size_t lo, hi;
@@ -209,9 +213,12 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
                 sg.L = L;
                 sg.R = n / L;
             } else {
+                // a large intermediate keeps enough outputs for the column kernels too
+                // (a GEMV with a few dozen outputs over megabytes is latency-bound)
+                const uint64_t min_out = first ? CHAIN_MIN_OUTPUTS : (n > CHAIN_SMALL ? CHAIN_LATE_OUTPUTS : 0);
                 uint64_t inner = ex[0];
                 lo = 1;
-                while (first && lo + 1 < ex.size() && inner < CHAIN_MIN_OUTPUTS) inner *= ex[lo++];
+                while (lo + 1 < ex.size() && inner < min_out) inner *= ex[lo++];
                 hi = ex.size();
                 sg.row = false;
                 sg.L = inner;

@@ -658,9 +658,14 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k
 // combine kernel: C[o] = sum over segments of partial[seg][o], fixed order
 // --------------------------------------------------------------------------
 // tpo threads per output (a power of two): thread t sums segments t, t + tpo,
-// ... in order, then the tpo partial sums meet in a fixed shared-memory tree,
-// so the result is the same on every run.  Few outputs with many segments
-// (thin prefixes, long contractions) spread over the whole block.
+// ... in order, loading COMBINE_U of them before the first sum so their
+// latencies overlap; then the tpo partial sums meet in a fixed tree (pairs
+// (t, t + h) for h = tpo/2 .. 1: through shared memory while h spans warps,
+// by warp shuffles below), so the result is the same on every run.  Few
+// outputs with many segments (thin prefixes, long contractions) spread over
+// the whole block.
+constexpr int COMBINE_U = 8;
+
 template <typename T, bool KAHAN, bool F64>
 __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restrict__ part,
                                                         T* __restrict__ out, uint64_t outputs,
@@ -676,34 +681,58 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
         Acc<T, KAHAN> acc;               // else: compensated merge of (s, c) pairs
         acc.init();
         if (o < outputs) {
-            for (uint32_t g = t; g < nseg; g += tpo) {
-                const Pair<T> p = part[uint64_t(g) * outputs + o];
-                if (F64)
-                    fs += (double)p.s - (double)p.c;
-                else
-                    acc.merge(p.s, p.c);
+            for (uint32_t g0 = t; g0 < nseg; g0 += COMBINE_U * tpo) {
+                Pair<T> pv[COMBINE_U];
+#pragma unroll
+                for (int u = 0; u < COMBINE_U; ++u) {
+                    const uint32_t g = g0 + (uint32_t)u * tpo;
+                    if (g < nseg) {
+                        pv[u] = part[uint64_t(g) * outputs + o];
+                    } else {
+                        pv[u].s = T(0);
+                        pv[u].c = T(0);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < COMBINE_U; ++u) {
+                    if (g0 + (uint32_t)u * tpo < nseg) {
+                        if (F64)
+                            fs += (double)pv[u].s - (double)pv[u].c;
+                        else
+                            acc.merge(pv[u].s, pv[u].c);
+                    }
+                }
             }
         }
         if (tpo > 1) {
-            red[2 * threadIdx.x] = F64 ? fs : (double)acc.s;
-            red[2 * threadIdx.x + 1] = F64 ? 0.0 : (double)acc.c;
-            __syncthreads();
-            for (uint32_t h = tpo >> 1; h > 0; h >>= 1) {
+            uint32_t h = tpo >> 1;
+            for (; h >= 32; h >>= 1) {
+                red[2 * threadIdx.x] = F64 ? fs : (double)acc.s;
+                red[2 * threadIdx.x + 1] = F64 ? 0.0 : (double)acc.c;
+                __syncthreads();
                 if (t < h) {
                     const double os = red[2 * (threadIdx.x + h)], oc = red[2 * (threadIdx.x + h) + 1];
-                    if (F64) {
+                    if (F64)
                         fs += os;
-                    } else {
+                    else
                         acc.merge((T)os, (T)oc);
-                    }
-                    red[2 * threadIdx.x] = F64 ? fs : (double)acc.s;
-                    red[2 * threadIdx.x + 1] = F64 ? 0.0 : (double)acc.c;
                 }
                 __syncthreads();
             }
+            // the rest of the tree inside a warp (a group of tpo <= 32 lanes, or the
+            // first warp of a larger group)
+            for (; h > 0; h >>= 1) {
+                if (F64) {
+                    const double os = __shfl_down_sync(0xffffffffu, fs, h);
+                    if (t < h) fs += os;
+                } else {
+                    const T os = __shfl_down_sync(0xffffffffu, acc.s, h);
+                    const T oc = __shfl_down_sync(0xffffffffu, acc.c, h);
+                    if (t < h) acc.merge(os, oc);
+                }
+            }
         }
         if (t == 0 && o < outputs) out[o] = F64 ? (T)fs : acc.value();
-        if (tpo > 1) __syncthreads();
     }
 }
 
