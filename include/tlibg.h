@@ -194,9 +194,12 @@ size_t tlibg_inverse_mode(const size_t* pi, size_t p, size_t mode);
  * mode r + 1 for r < q - 1, else mode r + 2); nbs (HOST) their lengths; c
  * (DEVICE) receives na[q-1] elements.  A is any dense layout (na, wa, pia as
  * in the single call).  The chain reads A once, whatever order the reference
- * would contract in: Kronecker weights of the prefix and suffix modes, a row
- * contraction over the prefix, a column contraction over the suffix -- no
- * host synchronisation; intermediates in the stream's cached scratch.  Same
+ * would contract in: a first stage over the fastest modes (rows) or the
+ * slowest (columns) reads A, one to three stages over the much smaller
+ * intermediates follow; stages over several modes use Kronecker weights built
+ * by one kernel, a stage over one mode reads its vector in place.  No host
+ * synchronisation; intermediates in the stream's cached scratch; each launch
+ * after the first is a programmatic dependent of the one before.  Same
  * messages as ttvpy for bad q, order or vector lengths.  dtype TLIBG_BF16A:
  * A bfloat16, vectors and c float.
  * ------------------------------------------------------------------------- */

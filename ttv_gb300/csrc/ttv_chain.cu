@@ -17,15 +17,14 @@
 // The first stage reads A (about all the traffic); each later one reads the
 // previous, much smaller, intermediate.  All weights come from one kernel
 // launch, intermediates live in the stream's cached scratch: no host
-// synchronisation and no allocation after the first call on a stream.
+// synchronisation and no allocation after the first call on a stream.  Each
+// launch after the first is a programmatic dependent of the one before, so
+// its launch overlaps its predecessor's tail.
 // Every contraction order of the reference gives the same sum up to
 // rounding; this one reads A once whatever order is asked for.
 #include "ttv_internal.h"
 
-#include <map>
-#include <mutex>
 #include <string>
-#include <utility>
 #include <vector>
 
 namespace tlibg {
@@ -40,6 +39,7 @@ constexpr int KRON_MAX_GROUPS = KRON_MAX_MODES;   // one weight vector per stage
 #endif
 constexpr uint64_t CHAIN_MIN_ROW = TLIBG_CHAIN_MIN_ROW;           // row stage: rows at least this long
 constexpr uint64_t CHAIN_MIN_OUTPUTS = TLIBG_CHAIN_MIN_OUTPUTS;   // column stage: at least this many outputs
+constexpr uint64_t CHAIN_ONE_MODE_ROW = 64;           // first row stage: one mode if it is this long
 constexpr uint64_t CHAIN_SMALL = uint64_t(1) << 22;   // intermediates up to this many elements: one stage
 constexpr uint64_t CHAIN_LATE_OUTPUTS = 4096;         // larger ones: column stages keep this many outputs
 
@@ -59,9 +59,18 @@ struct KronArgs {
 // One weight per thread: the mixed-radix digits of its index within its group
 // pick one element of each of the group's vectors.  I: 32-bit index
 // arithmetic when the weights number fewer than 2^32.
-template <typename T, typename I>
+template <typename T, typename I, bool AFTER>
 __global__ void kron_kernel(KronArgs k)
 {
+    // AFTER: launched as a programmatic dependent of the first stage, which does not
+    // read the weights: let the next stage be scheduled, compute, and only then wait
+    // for the first stage, so that a kernel waiting for this one also waits for it.
+    // Otherwise the engine kernels' usual prologue (wait, then allow dependents; the
+    // wait returns at once when launched normally).
+    if (AFTER)
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    else
+        asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
     const I total = (I)k.off[k.ngroups];
     for (I idx = (I)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
         int g = 0;
@@ -77,40 +86,12 @@ __global__ void kron_kernel(KronArgs k)
         }
         static_cast<T*>(k.out)[idx] = (T)w;
     }
+    if (AFTER) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// A side stream and its fork / join events per (device, caller stream), created
-// on first use and kept for the life of the process.
-struct SideStream {
-    cudaStream_t stream;
-    cudaEvent_t fork, join;
-};
-
-int side_stream(cudaStream_t caller, SideStream** out)
-{
-    static std::mutex mu;
-    static std::map<std::pair<int, cudaStream_t>, SideStream> cache;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return internal_cuda_fail(e, "cudaGetDevice");
-    std::lock_guard<std::mutex> lk(mu);
-    auto key = std::make_pair(dev, caller);
-    auto it = cache.find(key);
-    if (it == cache.end()) {
-        SideStream s{};
-        e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
-        if (e != cudaSuccess) return internal_cuda_fail(e, "side stream");
-        it = cache.emplace(key, s).first;
-    }
-    *out = &it->second;
-    return 0;
-}
 
 const char* const E_ORDER = "Error calling ttvpy::ttvs: input tensor order should be greater than zero.";
 const char* const E_MODE =
@@ -205,9 +186,13 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
             Stage sg{};
             size_t lo, hi;
             if (k > 0) {
+                // rows of the fastest mode alone when they are long and whole 16-byte
+                // vectors: that stage needs no Kronecker weights, so the weight launch
+                // for the later stages overlaps it
+                const bool one = first && ex[0] >= CHAIN_ONE_MODE_ROW && (ex[0] * ea) % 16 == 0;
                 uint64_t L = 1;
                 hi = 0;
-                while (hi < k && (!first || L < CHAIN_MIN_ROW || hi == 0)) L *= ex[hi++];
+                while (hi < k && (!first || hi == 0 || (!one && L < CHAIN_MIN_ROW))) L *= ex[hi++];
                 lo = 0;
                 sg.row = true;
                 sg.L = L;
@@ -283,36 +268,42 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
     char* base = static_cast<char*>(scratch);
     ka.out = base + off_w;
 
-    // The weights: one launch for every group.  When the first stage contracts a
-    // single mode it needs none of them, and the launch runs beside it on a
-    // side stream (forked from and joined back to the caller's stream).
+    // The weights: one launch for every group, then the stages, each launched as a
+    // programmatic dependent of the kernel before it (it waits for that kernel in
+    // its prologue).  When the first stage contracts a single mode it needs no
+    // weights: it goes first and the weight launch follows it as a dependent that
+    // computes at once, beside the stage, and waits for it only before exiting,
+    // so the next stage (waiting for the weights) also comes after the first.
     uint64_t launches = 0;
-    const bool overlap = ka.ngroups > 0 && stages[0].group < 0;
-    SideStream* side = nullptr;
-    if (overlap) {
-        if (int s = side_stream(st, &side)) return s;
-        cudaError_t e = cudaEventRecord(side->fork, st);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream, side->fork, 0);
-        if (e != cudaSuccess) return internal_cuda_fail(e, "stream fork");
-    }
-    if (ka.ngroups > 0) {
-        cudaStream_t ks = overlap ? side->stream : st;
+    const bool weights_after = ka.ngroups > 0 && stages[0].group < 0;
+    auto launch_weights = [&](bool dependent) -> cudaError_t {
         const int grid = (int)std::min<uint64_t>((uint64_t)sms * 8, (wtot + 255) / 256);
         const bool narrow = wtot < (uint64_t(1) << 32);
-        if (tdt == F64) {
-            if (narrow) kron_kernel<double, uint32_t><<<grid, 256, 0, ks>>>(ka);
-            else kron_kernel<double, uint64_t><<<grid, 256, 0, ks>>>(ka);
-        } else {
-            if (narrow) kron_kernel<float, uint32_t><<<grid, 256, 0, ks>>>(ka);
-            else kron_kernel<float, uint64_t><<<grid, 256, 0, ks>>>(ka);
+        void (*fn)(KronArgs);
+        if (tdt == F64)
+            fn = narrow ? (dependent ? kron_kernel<double, uint32_t, true> : kron_kernel<double, uint32_t, false>)
+                        : (dependent ? kron_kernel<double, uint64_t, true> : kron_kernel<double, uint64_t, false>);
+        else
+            fn = narrow ? (dependent ? kron_kernel<float, uint32_t, true> : kron_kernel<float, uint32_t, false>)
+                        : (dependent ? kron_kernel<float, uint64_t, true> : kron_kernel<float, uint64_t, false>);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(256);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        if (dependent) {
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
         }
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = cudaLaunchKernelEx(&cfg, fn, ka);
+        if (e == cudaSuccess) ++launches;
+        return e;
+    };
+    if (ka.ngroups > 0 && !weights_after) {
+        cudaError_t e = launch_weights(false);
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
-        ++launches;
-        if (overlap) {
-            e = cudaEventRecord(side->join, side->stream);
-            if (e != cudaSuccess) return internal_cuda_fail(e, "stream join");
-        }
     }
     const void* in = a;
     for (size_t i = 0; i < stages.size(); ++i) {
@@ -320,12 +311,15 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
         void* out = last ? c : base + ((i & 1) ? off_d1 : off_d0);
         const Stage& sg = stages[i];
         const void* w = sg.group < 0 ? sg.w : base + off_w + ka.off[sg.group] * et;
-        if (overlap && i == 1) {
-            cudaError_t e = cudaStreamWaitEvent(st, side->join, 0);
-            if (e != cudaSuccess) return internal_cuda_fail(e, "stream join");
-        }
-        cudaError_t e = launch_plan(plans[i], in, w, out, base + off_part, st, &launches);
+        // the first stage follows the weights (if they go first), every later stage the
+        // engine's previous kernel
+        const bool dependent = i > 0 || ka.ngroups > 0;
+        cudaError_t e = launch_plan(plans[i], in, w, out, base + off_part, st, &launches, dependent && !(i == 0 && weights_after));
         if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
+        if (i == 0 && weights_after) {
+            e = launch_weights(true);
+            if (e != cudaSuccess) return internal_cuda_fail(e, "kernel launch");
+        }
         in = out;
     }
     internal_count_launches(launches);

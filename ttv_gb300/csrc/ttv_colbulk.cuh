@@ -110,6 +110,7 @@ __device__ __forceinline__ void cb_produce(const KArgs& k, const CbWalk& w, unsi
 template <typename TA, typename T, bool KAHAN>
 __global__ void __launch_bounds__(CB_THREADS) col_bulk_kernel(KArgs k)
 {
+    pdl_prologue();
     constexpr int TJ = cb_tj<TA>();
     constexpr int V = TJ / CB_CONSUMERS;
     constexpr bool PRES = presplit_b<T, KAHAN>();

@@ -21,6 +21,26 @@ constexpr unsigned ERR_WAIT_TIMEOUT = 1u;
 constexpr uint32_t WAIT_POLL_LIMIT = 1u << 22;
 
 // --------------------------------------------------------------------------
+// programmatic dependent launch
+// --------------------------------------------------------------------------
+// First statement of every engine kernel.  `griddepcontrol.wait` returns at
+// once unless the kernel was launched as a programmatic dependent of the
+// previous kernel in its stream; then it blocks until that kernel has
+// completed and its writes are visible, so nothing below it can read an
+// input that is still being written or overwrite one still being read.
+// `griddepcontrol.launch_dependents` lets a kernel launched as this one's
+// programmatic dependent be scheduled once every CTA of this grid has issued
+// it (so every CTA of this grid is already resident: a dependent that waits
+// can never hold resources this grid still needs).  The host launches a
+// kernel as a dependent only when its predecessor is the engine's own kernel
+// of the same call (a combine after its main kernel, a chain stage after the
+// one before); the dependent's launch then overlaps its predecessor's tail.
+__device__ __forceinline__ void pdl_prologue()
+{
+    asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// --------------------------------------------------------------------------
 // element conversion: A may be float, double or raw bfloat16 bits
 // --------------------------------------------------------------------------
 template <typename TA, typename T> struct Cvt;

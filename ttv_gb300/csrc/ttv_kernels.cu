@@ -27,6 +27,7 @@
 #include <mutex>
 #include <type_traits>
 #include <unordered_map>
+#include <utility>
 
 namespace tlibg {
 
@@ -358,6 +359,7 @@ __device__ __forceinline__ void row_short(const KArgs& k, uint32_t G, uint32_t l
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k)
 {
+    pdl_prologue();
     const uint32_t G = k.group;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t gl = lane & (G - 1u);
@@ -441,6 +443,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_short_kernel(KArgs k)
 {
+    pdl_prologue();
     constexpr bool PRES = presplit_b<T, KAHAN>();
     const TA* __restrict__ A = static_cast<const TA*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
@@ -517,6 +520,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_short_kernel(K
 template <typename TA, typename T, int V, bool KAHAN, int M>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_short_kernel(KArgs k)
 {
+    pdl_prologue();
     constexpr int U = loads_in_flight<TA, V>();
     constexpr int R = M == 1 ? U : (U >= 2 ? U / 2 : 1);
     const uint64_t warp_id = (uint64_t(blockIdx.x) * BLOCK + threadIdx.x) >> 5;
@@ -530,6 +534,7 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_short_kernel(K
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_kernel(KArgs k)
 {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);
@@ -671,6 +676,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
                                                         T* __restrict__ out, uint64_t outputs,
                                                         uint32_t nseg, uint32_t tpo)
 {
+    pdl_prologue();
     __shared__ double red[2 * BLOCK];
     const uint32_t t = threadIdx.x & (tpo - 1u);
     const uint32_t ob = threadIdx.x / tpo;
@@ -943,8 +949,30 @@ int plan_ctas_per_sm(const Plan& p)
     return n;
 }
 
+// One kernel launch, as a programmatic dependent of the stream's previous
+// kernel when `dependent` is set (every engine kernel opens with
+// pdl_prologue, which waits for that kernel before touching memory).
+template <typename... Params, typename... Args>
+static cudaError_t launch_ex(void (*fn)(Params...), int grid, int threads, size_t smem, cudaStream_t stream,
+                             bool dependent, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    if (dependent) {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, fn, std::forward<Args>(args)...);
+}
+
 cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c, void* partial,
-                        cudaStream_t stream, uint64_t* launches)
+                        cudaStream_t stream, uint64_t* launches, bool dependent)
 {
     if (plan.kind == KIND_STREAM) {
         SArgs sa;
@@ -969,8 +997,7 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(reinterpret_cast<const void*>(sf), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
-        sf<<<plan.grid, STREAM_THREADS, smem, stream>>>(sa);
-        cudaError_t err = cudaGetLastError();
+        cudaError_t err = launch_ex(sf, plan.grid, STREAM_THREADS, smem, stream, dependent, sa);
         if (err != cudaSuccess) return err;
         if (launches) ++*launches;
         if (plan.split > 1) return launch_combine(plan, partial, c, stream, launches);
@@ -1017,8 +1044,7 @@ cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c,
     if ((plan.kind == KIND_ROW_TILE || plan.kind == KIND_COL_BULK) && smem > 48 * 1024)
         cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int threads = plan.kind == KIND_ROW_TILE ? ROWT_THREADS : (plan.kind == KIND_COL_BULK ? CB_THREADS : BLOCK);
-    fn<<<plan.grid, threads, smem, stream>>>(k);
-    cudaError_t err = cudaGetLastError();
+    cudaError_t err = launch_ex(fn, plan.grid, threads, smem, stream, dependent, k);
     if (err != cudaSuccess) return err;
     if (launches) ++*launches;
     if (plan.split > 1) return launch_combine(plan, partial, c, stream, launches);
@@ -1041,29 +1067,28 @@ cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_
         const uint64_t opb = BLOCK / tpo;
         int g = (int)std::min<uint64_t>(sms * 16, (outputs + opb - 1) / opb);
         if (g < 1) g = 1;
+        const uint32_t ns = (uint32_t)plan.split;
         switch (plan.dtype) {
         case F32:
-        case BF16A:
+        case BF16A: {
+            const Pair<float>* pf = static_cast<const Pair<float>*>(partial);
+            float* cf = static_cast<float*>(c);
             if (plan.f64_combine)
-                combine_kernel<float, true, true><<<g, BLOCK, 0, stream>>>(
-                    static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
-                    (uint32_t)plan.split, tpo);
+                err = launch_ex(combine_kernel<float, true, true>, g, BLOCK, 0, stream, true, pf, cf, outputs, ns, tpo);
             else if (plan.kahan)
-                combine_kernel<float, true, false><<<g, BLOCK, 0, stream>>>(
-                    static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
-                    (uint32_t)plan.split, tpo);
+                err = launch_ex(combine_kernel<float, true, false>, g, BLOCK, 0, stream, true, pf, cf, outputs, ns, tpo);
             else
-                combine_kernel<float, false, false><<<g, BLOCK, 0, stream>>>(
-                    static_cast<const Pair<float>*>(partial), static_cast<float*>(c), outputs,
-                    (uint32_t)plan.split, tpo);
-            break;
-        case F64:
-            combine_kernel<double, false, false><<<g, BLOCK, 0, stream>>>(
-                static_cast<const Pair<double>*>(partial), static_cast<double*>(c), outputs,
-                (uint32_t)plan.split, tpo);
+                err = launch_ex(combine_kernel<float, false, false>, g, BLOCK, 0, stream, true, pf, cf, outputs, ns,
+                                tpo);
             break;
         }
-        err = cudaGetLastError();
+        case F64:
+            err = launch_ex(combine_kernel<double, false, false>, g, BLOCK, 0, stream, true,
+                            static_cast<const Pair<double>*>(partial), static_cast<double*>(c), outputs, ns, tpo);
+            break;
+        default:
+            err = cudaErrorInvalidValue;
+        }
         if (err != cudaSuccess) return err;
         if (launches) ++*launches;
     }

@@ -143,9 +143,12 @@ size_t partial_bytes(const Plan& p);
 
 // Enqueue the plan's kernels (main kernel and, when split > 1, the combine).
 // `partial` must hold partial_bytes(plan) bytes.  Returns cudaSuccess or the
-// launch error.  Adds the number of launched kernels to *launches.
+// launch error.  Adds the number of launched kernels to *launches.  The
+// combine is launched as a programmatic dependent of the main kernel; the
+// main kernel too when `dependent` is set (its predecessor in the stream is
+// an engine kernel of the same call).
 cudaError_t launch_plan(const Plan& plan, const void* a, const void* b, void* c, void* partial,
-                        cudaStream_t stream, uint64_t* launches);
+                        cudaStream_t stream, uint64_t* launches, bool dependent = false);
 
 // Second phase of a split plan: C[o] = sum over segments of the partials.
 cudaError_t launch_combine(const Plan& plan, void* partial, void* c, cudaStream_t stream, uint64_t* launches);

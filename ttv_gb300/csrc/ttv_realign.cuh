@@ -41,6 +41,7 @@ __device__ __forceinline__ void realign_vec(const T (&c)[V], const T (&n)[V], ui
 template <typename T, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
 {
+    pdl_prologue();
     constexpr int V = 16 / (int)sizeof(T);
     constexpr int U = 4;
     extern __shared__ __align__(128) unsigned char smem_raw[];

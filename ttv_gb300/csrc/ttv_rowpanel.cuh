@@ -35,6 +35,7 @@ constexpr int RP_RB = 8;    // rows whose warp partials are gathered per CTA bar
 template <typename TA, typename T, int V, bool KAHAN, int RR>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_panel_kernel(KArgs k)
 {
+    pdl_prologue();
     __shared__ double s_red[BLOCK / 32][RP_RB][2];
     typedef typename AccSel<T, KAHAN>::type AccT;
     const TA* __restrict__ A = static_cast<const TA*>(k.a);

@@ -41,6 +41,7 @@ __device__ __forceinline__ void rowt_issue(const TA* A, uint64_t S, uint64_t nq,
 template <typename TA, typename T, bool KAHAN, int R>
 __global__ void __launch_bounds__(ROWT_THREADS) row_tile_kernel(KArgs k)
 {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nq = (uint32_t)k.nq;

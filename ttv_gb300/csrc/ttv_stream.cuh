@@ -101,6 +101,7 @@ __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;"
 template <typename TA, typename T, bool KAHAN, bool COL>
 __global__ void __launch_bounds__(STREAM_THREADS) stream_kernel(SArgs k)
 {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
     uint64_t* empty = full + STREAM_NS;

@@ -84,6 +84,7 @@ __device__ __forceinline__ void strided_loop(AccT (&acc)[MO], const TA* (&rp)[MO
 template <typename TA, typename T, int MO, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK) col_strided_kernel(KArgs k)
 {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     int* abort_flag = reinterpret_cast<int*>(smem_raw + 8);

@@ -16,6 +16,7 @@ namespace tlibg {
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_thin_kernel(KArgs k)
 {
+    pdl_prologue();
     constexpr int NW = BLOCK / 32;
     constexpr int U = loads_in_flight<TA, V>();
     extern __shared__ __align__(128) unsigned char smem_raw[];
