@@ -183,3 +183,49 @@ def test_noalloc_refuses_oversize_scratch(engine, cuda):
     assert st == engine.ERR_ARGUMENT
     assert engine._last_error() == ("Error in tlib::tensor_times_vector: contraction dimension "
                                     "of A and B are not equal.")
+
+
+def test_noalloc_and_chain_captured_in_a_cuda_graph(engine, orc, cuda):
+    """The allocation-free call (main kernel + its dependent combine) and the fused
+    chain (dependent stages) captured into one CUDA graph and replayed on new data."""
+    import torch
+    lib = bind(engine)
+    na, pia, q = [64, 1 << 20], [1, 2], 2          # heavy split: main kernel + combine
+    cna = [48, 40, 56, 36]                           # chain: four stages' worth of modes
+    s = torch.cuda.Stream(device=cuda)
+    g = torch.Generator(device=cuda)
+    g.manual_seed(77)
+    A = torch.empty(int(np.prod(na)), device=cuda)
+    b = torch.empty(na[q - 1], device=cuda)
+    c = torch.empty(int(np.prod(na)) // na[q - 1], device=cuda)
+    T4 = torch.empty(*cna, device=cuda)
+    bs = [torch.empty(cna[m], device=cuda) for m in (0, 2, 3)]   # chain over every mode but 2
+
+    def fill():
+        A.uniform_(-1, 1, generator=g)
+        b.uniform_(-1, 1, generator=g)
+        T4.uniform_(-1, 1, generator=g)
+        for v in bs:
+            v.uniform_(-1, 1, generator=g)
+
+    fill()
+    with torch.cuda.stream(s):   # warm-up on the capture stream: scratch, symbol address, plans
+        assert call(engine, lib.tlibg_ttv_f32_noalloc, q, na, pia, A, b, c, s.cuda_stream) == 0
+        engine.ttvs(2, T4, bs, stream=s)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        st = call(engine, lib.tlibg_ttv_f32_noalloc, q, na, pia, A, b, c, s.cuda_stream)
+        out = engine.ttvs(2, T4, bs, stream=s)
+    assert st == 0, engine._last_error()
+    for _ in range(2):
+        fill()
+        c.fill_(float("nan"))
+        out.fill_(float("nan"))
+        graph.replay()
+        torch.cuda.synchronize()
+        assert oracle_error(orc, engine, q, na, pia, A, b, c) <= 1e-5
+        ref, absn = orc.ttvs_truth(2, T4.view(-1).cpu().numpy(), cna, [4, 3, 2, 1],
+                                   [v.cpu().numpy() for v in bs])
+        assert orc.rel_error(out.cpu().numpy(), ref, absn) <= 1e-5
+    assert engine.device_error() == 0
