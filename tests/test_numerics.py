@@ -1,6 +1,8 @@
 """The integer-arithmetic building blocks of the kernels, restated in numpy and
 checked against exact arithmetic (CPU only; the GPU parity tests check the
-kernels themselves).
+kernels themselves).  The invariant division is also checked in its shipped
+form: tests/cpp/idx_div_check.cpp compiles ttv_kernels.cuh's make_idx_div and
+idx_div as host code.
 
 * ttv_kernels.cuh make_idx_div / idx_div: division by an invariant divisor
   (Granlund and Montgomery's round-up method) for every 32-bit dividend.
@@ -8,7 +10,14 @@ kernels themselves).
   built from its bits (lo = (1.m - 1) 2^k, exact), |x - hi - lo| < 2^-46 |x|.
 * ttv_device.cuh f2d: float -> double from the float's bits for normal floats.
 """
+import os
+import shutil
+import subprocess
+
 import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def idx_div_params(d):
@@ -88,3 +97,17 @@ def test_float_to_double_from_bits():
     # zeros and subnormals are not normal: the kernels build or convert those separately
     _, n0 = f2d(np.array([0.0, -0.0, 1e-45, 1e-40], np.float32))
     assert not n0.any()
+
+
+def test_shipped_invariant_division_on_the_host(tmp_path):
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if not gxx or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers missing")
+    exe = str(tmp_path / "idx_div_check")
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", cuda_inc,
+                        os.path.join(ROOT, "tests", "cpp", "idx_div_check.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.startswith("PASSED"), r.stdout + r.stderr

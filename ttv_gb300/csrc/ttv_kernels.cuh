@@ -114,11 +114,16 @@ __host__ __device__ inline IdxDiv make_idx_div(uint64_t d, uint64_t max_dividend
     return v;
 }
 
-__device__ __forceinline__ uint64_t idx_div(uint64_t n, const IdxDiv& v)
+// (Host-callable too, so the CPU tests run this very code.)
+__host__ __device__ __forceinline__ uint64_t idx_div(uint64_t n, const IdxDiv& v)
 {
     if (v.fast) {
         const uint32_t x = (uint32_t)n;
+#ifdef __CUDA_ARCH__
         const uint32_t t = __umulhi(v.m, x);
+#else
+        const uint32_t t = (uint32_t)(((uint64_t)v.m * x) >> 32);
+#endif
         return (t + ((x - t) >> v.s1)) >> v.s2;
     }
     return n / v.d;
