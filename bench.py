@@ -201,7 +201,8 @@ def kernel_label(T, c):
     fam = {T.KIND_ROW: "row_kernel", T.KIND_COL: "col_kernel",
            T.KIND_STREAM: "stream_kernel", T.KIND_COL_REALIGN: "col_realign_kernel",
            T.KIND_COL_THIN: "col_thin_kernel", T.KIND_ROW_TILE: "row_tile_kernel",
-           T.KIND_COL_BULK: "col_bulk_kernel", T.KIND_ROW_PANEL: "row_panel_kernel"}[pl["kind"]]
+           T.KIND_COL_BULK: "col_bulk_kernel", T.KIND_ROW_PANEL: "row_panel_kernel",
+           T.KIND_ROW_SHIFT: "row_shift_kernel"}[pl["kind"]]
     if pl["kind"] == T.KIND_COL and pl["vec"] == 1:
         fam = "col_strided_kernel"   # scalar loads, two outputs per thread
     templ = "" if pl["kind"] in (T.KIND_STREAM, T.KIND_ROW_TILE, T.KIND_COL_BULK) else f",V{pl['vec']}"

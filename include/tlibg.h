@@ -70,6 +70,11 @@ extern "C" {
                                    /*   rows): a CTA holds a segment of b in registers and streams  */
                                    /*   that segment of a block of rows, so b is read once per row  */
                                    /*   block; `group` = rows in flight.  On request only           */
+#define TLIBG_KIND_ROW_SHIFT 8     /* q-fastest rows that are not whole 16-byte vectors (P == 1,    */
+                                   /*   fp32 / fp64): 16-byte loads of each row's aligned body      */
+                                   /*   against shifted copies of b in shared memory, head and tail */
+                                   /*   elements scalar; `group` = lanes per row.  Default for rows */
+                                   /*   of >= 64 elements when the rows fill the lane groups        */
 
 typedef struct tlibg_options {
     int accumulate;   /* TLIBG_ACC_*                                                      */

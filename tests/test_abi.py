@@ -139,10 +139,14 @@ def test_metadata_helpers_match_reference(engine):
 
 
 def test_planner_kernel_family(engine):
-    # q-fastest rows: aligned -> register row kernel; unaligned fp32 within a 16 KB
-    # stage -> the streamed kernel (row form); fp64 rows -> row kernel
+    # q-fastest rows: aligned -> register row kernel; unaligned rows of 64 or more
+    # elements, many of them -> the row-shift kernel (fp32 and fp64), few -> row kernel
     assert engine.plan(1, [64, 32, 16], [1, 2, 3])["kind"] == engine.KIND_ROW
-    assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_ROW
+    assert engine.plan(3, [645, 645, 645], [3, 2, 1])["kind"] == engine.KIND_ROW_SHIFT
+    assert engine.plan(3, [645, 645, 645], [3, 2, 1], dtype=engine.F64)["kind"] == engine.KIND_ROW_SHIFT
+    assert engine.plan(1, [645, 99], [1, 2])["kind"] == engine.KIND_ROW
+    assert engine.plan(3, [645, 645, 645], [3, 2, 1], vec=1)["kind"] == engine.KIND_ROW
+    assert engine.plan(1, [4001, 9999], [1, 2])["kind"] == engine.KIND_ROW   # copies of b over 48 KB
     # unaligned fp32 rows under 64 elements: the row-tile kernel; aligned ones the row kernel
     assert engine.plan(3, [25, 25, 25], [3, 2, 1])["kind"] == engine.KIND_ROW_TILE
     assert engine.plan(1, [63, 99], [1, 2])["kind"] == engine.KIND_ROW_TILE
@@ -173,7 +177,7 @@ def test_planner_kernel_family(engine):
     assert engine.plan(2, [645, 33, 7], [1, 2, 3])["kind"] == engine.KIND_COL
     with pytest.raises(engine.TTVError):
         engine.plan(1, [16, 9], [1, 2], kind=engine.KIND_COL_BULK)
-    assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW
+    assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=engine.F64)["kind"] == engine.KIND_ROW_SHIFT
     # fp64 column kernel: the DFMA / double-float mix by default
     assert engine.plan(2, [64, 32, 16], [1, 2, 3], dtype=engine.F64)["accumulate"] == \
         engine.ACC_COMPENSATED

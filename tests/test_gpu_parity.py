@@ -628,6 +628,58 @@ def test_row_panel_kernel(engine, orc, torch_dev):
                    kind=engine.KIND_ROW_PANEL)
 
 
+def test_row_shift_kernel(engine, orc, torch_dev):
+    """Rows that are not whole 16-byte vectors through the row-shift kernel
+    (aligned vector bodies against shifted copies of b in shared memory, head
+    and tail elements scalar): odd and even unaligned n_q from 1 to the shared-
+    memory limit, A at every element offset of the 16-byte grid, S from 1 to
+    many rounds, lanes per row 1..32, fp32 (compensated and plain), fp64 (mix
+    and native); default for rows of 645 elements; refused for bf16-stored A
+    and for rows whose shifted copies exceed 48 KB."""
+    torch, dev = torch_dev
+    rng = np.random.default_rng(91)
+    for dt in (np.float32, np.float64):
+        V = 16 // np.dtype(dt).itemsize
+        tdt = torch.float32 if dt == np.float32 else torch.float64
+        nmax = 3068 if dt == np.float32 else 1534
+        for nq, S in ((1, 5), (3, 7), (V + 1, 33), (63, 100), (645, 2000), (625, 3001), (1001, 17),
+                      (nmax, 40), (nmax - 1, 3)):
+            if nq % V == 0:
+                continue
+            N = nq * S
+            for off in range(V):
+                a = rng.uniform(-1, 1, N + V).astype(dt)
+                b = rng.uniform(-1, 1, nq).astype(dt)
+                da_full, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+                da = da_full[off:off + N]
+                truth = orc.truth(S, nq, 1, a[off:off + N], b)
+                dc = torch.empty(S, dtype=tdt, device=dev)
+                for acc in (engine.ACC_COMPENSATED, engine.ACC_PLAIN):
+                    for G in ((1, 8, 32) if off == 0 else (4,)):
+                        dc.fill_(float("nan"))
+                        engine.ttv(1, 2, da, [nq, S], [1, nq], [1, 2], db, [nq], dc, [S], [1], [1],
+                                   kind=engine.KIND_ROW_SHIFT, group=G, accumulate=acc, sync=True)
+                        err = orc.rel_error(dc.cpu().numpy(), *truth)
+                        assert err <= TOL[dt], (nq, S, off, dt, acc, G, err)
+    # the planner's default for the sweep's rows of 645 (and the chain's rows of 625)
+    for dt, code in ((np.float32, engine.F32), (np.float64, engine.F64)):
+        assert engine.plan(1, [645, 645, 645], [1, 2, 3], dtype=code)["kind"] == engine.KIND_ROW_SHIFT
+        assert engine.plan(1, [625, 625, 625], [1, 2, 3], dtype=code)["kind"] == engine.KIND_ROW_SHIFT
+    na = [645, 645, 645]
+    a = rng.uniform(-1, 1, 645 ** 3).astype(np.float64)
+    b = rng.uniform(-1, 1, 645).astype(np.float64)
+    check(orc, engine, torch, dev, 1, na, [1, 2, 3], a, b)
+    # refused where it does not apply
+    with pytest.raises(engine.TTVError):
+        engine.ttv(1, 2, torch.zeros(4000 * 4, device=dev), [4000, 4], [1, 4000], [1, 2],
+                   torch.zeros(4000, device=dev), [4000], torch.zeros(4, device=dev), [4], [1], [1],
+                   kind=engine.KIND_ROW_SHIFT)
+    with pytest.raises(engine.TTVError):
+        engine.ttv(1, 2, torch.zeros(645 * 4, device=dev, dtype=torch.bfloat16).view(torch.int16),
+                   [645, 4], [1, 645], [1, 2], torch.zeros(645, device=dev), [645],
+                   torch.zeros(4, device=dev), [4], [1], [1], dtype=engine.BF16A, kind=engine.KIND_ROW_SHIFT)
+
+
 def test_short_contraction_column_kernel(engine, orc, torch_dev):
     """Column form with n_q <= 4 and vector loads: two tiles per thread, every row
     loaded before any product; odd and even tile counts, one slice and many,

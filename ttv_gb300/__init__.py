@@ -31,6 +31,7 @@ __all__ = [
     "plan_hint", "clear_plan_hint", "F32", "F64", "BF16A",
     "ACC_COMPENSATED", "ACC_PLAIN", "ACC_DOUBLE_FLOAT", "KIND_ROW", "KIND_COL", "KIND_STREAM",
     "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE", "KIND_COL_BULK", "KIND_ROW_PANEL",
+    "KIND_ROW_SHIFT",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -39,7 +40,7 @@ LIB_PATH = os.path.join(HERE, "libttvgpu.so")
 F32, F64, BF16A = 0, 1, 2
 ACC_COMPENSATED, ACC_PLAIN, ACC_DOUBLE_FLOAT = 0, 1, 2
 KIND_ROW, KIND_COL, KIND_STREAM, KIND_COL_REALIGN, KIND_COL_THIN, KIND_ROW_TILE, KIND_COL_BULK, \
-    KIND_ROW_PANEL = 0, 1, 2, 3, 4, 5, 6, 7
+    KIND_ROW_PANEL, KIND_ROW_SHIFT = 0, 1, 2, 3, 4, 5, 6, 7, 8
 OK, ERR_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = range(6)
 
 

@@ -495,6 +495,38 @@ int make_row_panel_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int 
     return TLIBG_OK;
 }
 
+// Rows that are not whole 16-byte vectors: the row-shift kernel (aligned
+// vector bodies against shifted copies of b in shared memory), G lanes per row
+// by the row kernel's rule, no split.
+int make_row_shift_plan(Plan pl, const Canon& cn, const tlibg_options* opt, int sms, Plan* out)
+{
+    const int vmax = (int)(16 / elem_size_a(pl.dtype));
+    if (opt && opt->vec > 0 && opt->vec != vmax)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-shift kernel loads 16 bytes per vector");
+    if (opt && opt->split > 1)
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-shift kernel does not split the contracted mode");
+    int G;
+    if (pl.dtype == F64)
+        G = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 64))));
+    else
+        G = std::max(2, std::min(32, pow2_floor(std::max<uint64_t>(1, cn.nq / 4 / 16))));
+    if (opt && opt->group > 0) G = opt->group;
+    if (G < 1 || G > 32 || (G & (G - 1)))
+        return fail(TLIBG_ERR_ARGUMENT, "tlibg: lanes per row must be a power of two in 1..32");
+    pl.kind = KIND_ROW_SHIFT;
+    pl.vec = vmax;
+    pl.group = G;
+    pl.split = 1;
+    pl.seg_len = cn.nq;
+    pl.items = cn.S;
+    pl.items_per_cta = 0;
+    const int cps = std::max(1, plan_ctas_per_sm(pl));
+    pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * cps, cdiv(cn.S, BLOCK / G)));
+    pl.smem = plan_smem_bytes(pl);
+    *out = pl;
+    return TLIBG_OK;
+}
+
 int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, const tlibg_options* opt,
                     int sms, Plan* out)
 {
@@ -547,6 +579,14 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
                                             "than one segment of b");
         return make_row_panel_plan(pl, cn, opt, sms, out);
     }
+    const bool shift_ok = cn.P == 1 && dtype != BF16A &&
+                          rs_smem_bytes(cn.nq, et, dtype == F64 && pl.kahan) <= RS_SMEM_MAX;
+    if (opt && opt->kind == KIND_ROW_SHIFT) {
+        if (!shift_ok)
+            return fail(TLIBG_ERR_ARGUMENT, "tlibg: the row-shift kernel needs prefix P == 1, fp32 or fp64 A, "
+                                            "and b's shifted copies within 48 KB of shared memory");
+        return make_row_shift_plan(pl, cn, opt, sms, out);
+    }
     if (opt && opt->kind >= 0 && opt->kind != KIND_STREAM && opt->kind != KIND_COL_REALIGN &&
         opt->kind != KIND_COL_THIN && opt->kind != KIND_ROW_TILE && opt->kind != pl.kind)
         return fail(TLIBG_ERR_ARGUMENT, "tlibg: forced kernel kind does not match the problem "
@@ -576,6 +616,22 @@ int make_plan_inner(int dtype, const Canon& cn, const void* a, const void* b, co
     if (opt && opt->kind == KIND_STREAM) {
         if (dtype == F64) pl.kahan = (opt && opt->accumulate == TLIBG_ACC_DOUBLE_FLOAT) ? 1 : 0;
         return make_stream_plan(pl, cn, opt, sms, out);
+    }
+    // Rows of 64 or more elements that are not whole 16-byte vectors (or A off the
+    // 16-byte grid), with enough rows to fill the lane groups without a split: the
+    // row-shift kernel instead of the row kernel's scalar loads (measured on GB300
+    // for the sweep's rows of 645 floats / doubles).
+    if (shift_ok && !rows_aligned && cn.nq >= 64 && no_split && !(opt && (opt->kind >= 0 || opt->vec > 0))) {
+        Plan sp;
+        if (make_row_shift_plan(pl, cn, opt, sms, &sp) == TLIBG_OK) {
+            // at least four rounds of rows over the resident lane groups (the kernel
+            // has no split to fill the GPU with fewer rows)
+            const uint64_t groups = (uint64_t)sms * std::max(1, plan_ctas_per_sm(sp)) * (BLOCK / sp.group);
+            if (cn.S >= 4 * groups) {
+                *out = sp;
+                return TLIBG_OK;
+            }
+        }
     }
     const int vmax = (int)(16 / ea);
 

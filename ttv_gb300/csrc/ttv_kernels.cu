@@ -751,6 +751,7 @@ __global__ void __launch_bounds__(BLOCK) combine_kernel(const Pair<T>* __restric
 #include "ttv_rowtile.cuh"
 #include "ttv_colbulk.cuh"
 #include "ttv_rowpanel.cuh"
+#include "ttv_rowshift.cuh"
 
 namespace tlibg {
 
@@ -777,6 +778,10 @@ static KernelFn pick_main(int kind, int vec, int rows_m, int mo)
 {
     constexpr int VMAX = 16 / (int)sizeof(TA);
     if (kind == KIND_COL_BULK) return col_bulk_kernel<TA, T, KAHAN>;
+    if (kind == KIND_ROW_SHIFT) {
+        if constexpr (std::is_same<TA, T>::value) return row_shift_kernel<T, KAHAN>;
+        else return nullptr;
+    }
     if (kind == KIND_ROW_PANEL) {
         if (vec != VMAX) return nullptr;
         return rows_m == 2 ? row_panel_kernel<TA, T, VMAX, KAHAN, 2> : row_panel_kernel<TA, T, VMAX, KAHAN, 1>;
@@ -895,6 +900,7 @@ size_t plan_smem_bytes(const Plan& p)
     }
     if (p.kind == KIND_COL && p.rows_m == 1) return 0;   // short contraction: b in registers
     if (p.kind == KIND_ROW_PANEL) return 0;               // b in registers, static reduction buffer
+    if (p.kind == KIND_ROW_SHIFT) return rs_smem_bytes(p.nq, acc_size(p.dtype), p.dtype == F64 && p.kahan);
     if (p.kind == KIND_ROW)   // fp64 mix: b's split for rows of up to ROW_SPLIT_MAX elements
         return (p.dtype == F64 && p.kahan && p.rows_m == 0 && p.group > 1 && p.nq <= (uint64_t)ROW_SPLIT_MAX)
                    ? ROW_SPLIT_MAX * 8 : 0;

@@ -9,7 +9,7 @@ namespace tlibg {
 enum DType { F32 = 0, F64 = 1, BF16A = 2 };
 enum Kind {
     KIND_ROW = 0, KIND_COL = 1, KIND_STREAM = 2, KIND_COL_REALIGN = 3, KIND_COL_THIN = 4, KIND_ROW_TILE = 5,
-    KIND_COL_BULK = 6, KIND_ROW_PANEL = 7
+    KIND_COL_BULK = 6, KIND_ROW_PANEL = 7, KIND_ROW_SHIFT = 8
 };
 
 constexpr int BLOCK = 256;            // threads per CTA for every TTV kernel
@@ -80,6 +80,18 @@ struct Plan {
     uint64_t L = 0, R = 0, units = 0, units_per_cta = 0;
     int RG = 1, J = 1;
 };
+
+// Row-shift kernel (rows that are not whole 16-byte vectors): V shifted copies
+// of b, each W = n_q + V rounded up to V elements, plus their double-float
+// splits for fp64 with the mix; at most RS_SMEM_MAX bytes.
+constexpr size_t RS_SMEM_MAX = 48 * 1024;
+__host__ __device__ inline uint64_t rs_width(uint64_t nq, int V) { return (nq + V + V - 1) / V * V; }
+__host__ __device__ inline size_t rs_smem_bytes(uint64_t nq, size_t es, bool split)
+{
+    const int V = (int)(16 / es);
+    const uint64_t W = rs_width(nq, V);
+    return (size_t)V * W * es + (split ? (size_t)V * W * 8 : 0);
+}
 
 // Whether the streamed kernel can take a problem (whole rows fit a stage).
 bool stream_eligible(int dtype, uint64_t P, uint64_t nq);

@@ -21,8 +21,8 @@ import sys
 
 import numpy as np
 
-from . import F32, F64, KIND_COL, KIND_COL_BULK, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_PANEL, KIND_ROW_TILE, \
-    KIND_STREAM, \
+from . import F32, F64, KIND_COL, KIND_COL_BULK, KIND_COL_REALIGN, KIND_ROW, KIND_ROW_PANEL, KIND_ROW_SHIFT, \
+    KIND_ROW_TILE, KIND_STREAM, \
     ACC_DOUBLE_FLOAT, \
     clear_plan_hint, output_layout, output_shape, plan, plan_hint, strides, ttv
 
@@ -47,6 +47,11 @@ def candidates(dtype, P, nq, S):
         if nq % (16 // es) == 0 and nq > 1024 * (16 // es):   # longer than one segment of b
             for rr in (1, 2):
                 out.append({"kind": KIND_ROW_PANEL, "group": rr})
+        # rows that are not whole 16-byte vectors, b's shifted copies within 48 KB
+        w = (nq + 2 * (16 // es) - 1) // (16 // es) * (16 // es)
+        if nq % (16 // es) and (16 // es) * w * (es + (8 if dtype == F64 else 0)) <= 48 * 1024:
+            for g in (4, 8, 16, 32):
+                out.append({"kind": KIND_ROW_SHIFT, "group": g})
     else:
         min_split = -(-nq // (16384 // es))
         kinds = (KIND_COL, KIND_COL_REALIGN) if P % (16 // es) else (KIND_COL,)
