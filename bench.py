@@ -743,11 +743,21 @@ def run_e2e(T, torch, sw, args):
 
     for x in prepared[:3]:
         one(x)
+    per_case = [0.0] * len(prepared)
     t = time.perf_counter()
     for _ in range(steps):
-        for x in prepared:
-            one(x)
+        for i, x in enumerate(prepared):
+            t0 = time.perf_counter()
+            one(x)   # synchronous: returns after the kernels and C are done
+            per_case[i] += time.perf_counter() - t0
     dt_s = time.perf_counter() - t
+    by_kernel = {}
+    for i, (_f, _a, _k, nb, kname, _c) in enumerate(prepared):
+        d = by_kernel.setdefault(kname, [0, 0.0])
+        d[0] += nb * steps
+        d[1] += per_case[i]
+    worst = sorted(((x[3] * steps / per_case[i] / 1e9, x[5]) for i, x in enumerate(prepared)),
+                   key=lambda t_: t_[0])[:3]
     nbytes = sum(x[3] for x in prepared)
     h2d = sum(esize(c["dtype"]) * (int(np.prod(c["na"])) + c["na"][c["q"] - 1])
               for *_x, c in prepared)
@@ -759,7 +769,10 @@ def run_e2e(T, torch, sw, args):
     return {"value": round(v, 1), "unit": "GB/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
             "api": "tlibg_ttv_host (host pointers, pinned)",
-            "link_GBps": link, "frac_of_link_h2d": round(v / link["h2d"], 3)}
+            "link_GBps": link, "frac_of_link_h2d": round(v / link["h2d"], 3),
+            "by_kernel_GBps": {k: round(d[0] / d[1] / 1e9, 1) for k, d in by_kernel.items()},
+            "slowest_cases": [{"GB/s": round(g, 1), "na": c["na"], "pia": c["pia"], "q": c["q"],
+                               "dtype": c["dtype"]} for g, c in worst]}
 
 
 # --------------------------------------------------------------------------

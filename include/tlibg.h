@@ -132,11 +132,13 @@ int tlibg_ttv_ex(int dtype, size_t q, size_t p,
                  const tlibg_options* opt, void* stream);
 
 /* Same call with HOST pointers a, b, c, as the reference takes them.  A in
- * page-locked memory is read in place by the kernels over the host link (one
- * pass, no staging copy), and then a page-locked C is written in place too;
- * pageable A is streamed to the device in chunks on a copy stream overlapped
- * with the kernels.  b (and otherwise C) go through device buffers; the call
- * returns when C is complete on the host (the reference's synchronous
+ * page-locked memory whose plan reads 512-byte runs per warp load (column
+ * tiles with 16-byte loads, rows taken by a whole warp) is read in place by
+ * the kernels over the host link (one pass, no staging copy); every
+ * other A (other plans, pageable memory) is streamed to the device in chunks
+ * on a copy stream overlapped with the kernels.  A page-locked C is written in
+ * place by the kernels; b (and a pageable C) go through device buffers.  The
+ * call returns when C is complete on the host (the reference's synchronous
  * semantics). */
 int tlibg_ttv_host(int dtype, size_t q, size_t p,
                    const void* a, const size_t* na, const size_t* wa, const size_t* pia,

@@ -336,13 +336,16 @@ def test_full_size_properties(engine, torch_dev):
 
 def test_host_buffers(engine, orc, torch_dev):
     """The host-pointer entry point (the reference's own calling convention): pinned A
-    is read in place, pinned C written in place, pageable buffers staged."""
+    is read in place by the column kernels with 16-byte loads, other plans and
+    pageable A are staged through device memory in chunks; pinned C is written in
+    place, pageable C copied back."""
     torch, dev = torch_dev
     rng = np.random.default_rng(4)
-    # pinned A is read in place by the kernels (the streamed kernel's shapes, here
-    # rows of 25, take the register row kernel instead); pageable A is staged
+    # column forms with 16-byte loads read pinned A in place; row forms (rows of 25,
+    # rows of 645 over two staged chunks) and odd prefixes are staged
     for na, pia, q in (([200, 300, 50], [1, 2, 3], 2), ([128, 64, 300], [3, 1, 2], 3),
-                       ([4096, 4096], [1, 2], 2), ([25, 4000], [1, 2], 1), ([7, 999, 5], [1, 2, 3], 2)):
+                       ([4096, 4096], [1, 2], 2), ([25, 4000], [1, 2], 1), ([7, 999, 5], [1, 2, 3], 2),
+                       ([645, 60000], [1, 2], 1)):
         wa, nc, wc, pic = meta(engine, na, pia, q)
         a = rng.uniform(-1, 1, int(np.prod(na))).astype(np.float32)
         b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)

@@ -1074,6 +1074,15 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
 // ---------------------------------------------------------------------------
 // host-buffer path: chunked copies overlapped with the kernels
 // ---------------------------------------------------------------------------
+// Bytes of A per staged chunk (MB), and the in-place read rule (-1: by plan, as
+// described below; 0: always staged; 1: in place whenever A is page-locked).
+#ifndef TLIBG_HOST_CHUNK_MB
+#define TLIBG_HOST_CHUNK_MB 64
+#endif
+#ifndef TLIBG_HOST_DIRECT
+#define TLIBG_HOST_DIRECT -1
+#endif
+
 int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
                    const size_t* pia, const void* b, const size_t* nb, void* c, const size_t* nc,
                    const size_t* wc, const size_t* pic, const tlibg_options* opt)
@@ -1090,7 +1099,7 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     const size_t ea = elem_size_a(dtype), et = elem_size_t(dtype);
     // chunk along the suffix S (independent panels); one chunk when S == 1
     const uint64_t panel = cn.nq * cn.P;                     // elements of A per panel
-    const uint64_t chunk_bytes_target = 64ull << 20;
+    const uint64_t chunk_bytes_target = (uint64_t)TLIBG_HOST_CHUNK_MB << 20;
     uint64_t spc = std::max<uint64_t>(1, chunk_bytes_target / std::max<uint64_t>(1, panel * ea));
     spc = std::min<uint64_t>(spc, cn.S);
     const uint64_t nchunks = cdiv(cn.S, spc);
@@ -1154,24 +1163,44 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     if ((st = grow(&hc.bbuf, &hc.bbytes, need_b))) return st;
     if ((st = grow(&hc.cbuf, &hc.cbytes, need_c))) return st;
 
-    // Page-locked A: the kernels read it in place over the host link (one pass,
-    // no staging copy; on GB300 a kernel reading page-locked memory moves it as
-    // fast as the copy engines do).  The bulk copies of the streamed, row-tile and
-    // TMA-staged column kernels are kept to device memory: the register kernels
-    // take those problems.
+    // Page-locked A whose plan reads 512-byte runs per warp load (column tiles with
+    // 16-byte loads, rows taken by a whole warp): the kernels read it in place over
+    // the host link (one pass, no staging copy; on GB300 such reads move
+    // page-locked memory as fast as the copy engines do).  Every other plan (short
+    // rows, whose lane groups issue one short run per row, and scalar loads) goes
+    // through the staged path below: copy-engine copies of chunks into device
+    // memory overlapped with the device kernels (measured over the symmetric
+    // sweep: rows of 16-25 elements 123-149 GB/s read in place, 190-202 staged,
+    // against the 211 GB/s link).  The bulk copies of the streamed, row-tile and
+    // TMA-staged column kernels are kept to device memory.
     cudaPointerAttributes at{};
     const bool a_pinned = cudaPointerGetAttributes(&at, a) == cudaSuccess && at.type == cudaMemoryTypeHost &&
                           at.devicePointer != nullptr;
     cudaGetLastError();
+    cudaPointerAttributes atc{};
+    const bool c_pinned = cudaPointerGetAttributes(&atc, c) == cudaSuccess && atc.type == cudaMemoryTypeHost &&
+                          atc.devicePointer != nullptr;
+    cudaGetLastError();
+    bool direct = false;
     if (a_pinned) {
+        tlibg_options o2{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, 0};
+        if (opt) o2 = *opt;
+        if (o2.kind == KIND_STREAM || o2.kind == KIND_ROW_TILE || o2.kind == KIND_COL_BULK) o2.kind = -1;
+        Plan probe_pl;
+        if ((st = make_plan(dtype, cn, at.devicePointer, hc.bbuf, &o2, d.sms, &probe_pl))) return st;
+        // a warp's 16-byte loads cover one 512-byte run: column tiles, thin prefixes of
+        // at least 512 bytes, rows taken by a whole warp
+        const bool v16 = (size_t)probe_pl.vec * ea == 16;
+        direct = v16 && (probe_pl.kind == KIND_COL ||
+                         (probe_pl.kind == KIND_COL_THIN && cn.P * ea >= 512) ||
+                         (probe_pl.kind == KIND_ROW && probe_pl.group == 32 && probe_pl.rows_m == 0));
+        if (TLIBG_HOST_DIRECT >= 0) direct = TLIBG_HOST_DIRECT == 1;
+    }
+    if (a_pinned && direct) {
         if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.comp)) != cudaSuccess)
             return cuda_fail(e, "copy of b");
         // page-locked C too: the kernels store C in place over the link while they
         // read A (the link carries both directions at once), no copy after them
-        cudaPointerAttributes atc{};
-        const bool c_pinned = cudaPointerGetAttributes(&atc, c) == cudaSuccess && atc.type == cudaMemoryTypeHost &&
-                              atc.devicePointer != nullptr;
-        cudaGetLastError();
         void* cdst = c_pinned ? atc.devicePointer : hc.cbuf;
         tlibg_options o2{TLIBG_ACC_COMPENSATED, -1, 0, 0, 0, 0};
         if (opt) o2 = *opt;
@@ -1216,13 +1245,14 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         if ((st = make_plan(dtype, ck, hc.abuf[slot], hc.bbuf, opt, d.sms, &pl))) return st;
         void* part = nullptr;
         if ((st = get_scratch(hc.comp, partial_bytes(pl), &part))) return st;
-        char* cdst = static_cast<char*>(hc.cbuf) + s0 * cn.P * et;
+        // page-locked C: each chunk's kernels store their part of C in place
+        char* cdst = static_cast<char*>(c_pinned ? atc.devicePointer : hc.cbuf) + s0 * cn.P * et;
         e = launch_plan(pl, hc.abuf[slot], hc.bbuf, cdst, part, hc.comp, &launches);
         if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
         cudaEventRecord(hc.done[slot], hc.comp);
     }
     g_launches += launches;
-    if ((e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
+    if (!c_pinned && (e = cudaMemcpyAsync(c, hc.cbuf, need_c, cudaMemcpyDeviceToHost, hc.comp)) != cudaSuccess)
         return cuda_fail(e, "copy of C");
     if ((e = cudaStreamSynchronize(hc.comp)) != cudaSuccess) return cuda_fail(e, "stream synchronize");
     unsigned int derr = read_and_clear_device_error();
