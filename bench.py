@@ -741,7 +741,7 @@ def run_e2e(T, torch, sw, args):
         if st:
             raise RuntimeError(f"ttv_host failed: {T._last_error()}")
 
-    for x in prepared[:3]:
+    for x in prepared:   # one untimed pass: the host path's staging buffers reach their size
         one(x)
     per_case = [0.0] * len(prepared)
     t = time.perf_counter()
