@@ -135,8 +135,8 @@ int tlibg_ttv_ex(int dtype, size_t q, size_t p,
  * page-locked memory whose plan reads 512-byte runs per warp load (column
  * tiles with 16-byte loads, rows taken by a whole warp) is read in place by
  * the kernels over the host link (one pass, no staging copy); every
- * other A (other plans, pageable memory) is streamed to the device in chunks
- * on a copy stream overlapped with the kernels.  A page-locked C is written in
+ * other A is staged to the device in chunks overlapped with the kernels
+ * (page-locked: copied by the SMs; pageable: by the copy engine).  A page-locked C is written in
  * place by the kernels; b (and a pageable C) go through device buffers.  The
  * call returns when C is complete on the host (the reference's synchronous
  * semantics). */

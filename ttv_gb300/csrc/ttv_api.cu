@@ -1074,6 +1074,24 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
 // ---------------------------------------------------------------------------
 // host-buffer path: chunked copies overlapped with the kernels
 // ---------------------------------------------------------------------------
+// Copy of n16 16-byte blocks from page-locked host memory (through its device
+// address) to device memory: four loads in flight per thread, each warp load one
+// 512-byte run.
+__global__ void __launch_bounds__(256) host_stage_kernel(uint4* __restrict__ dst, const uint4* __restrict__ src,
+                                                         uint64_t n16)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = src[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) dst[i + u * stride] = v[u];
+    }
+    for (; i < n16; i += stride) dst[i] = src[i];
+}
+
 // Bytes of A per staged chunk (MB), and the in-place read rule (-1: by plan, as
 // described below; 0: always staged; 1: in place whenever A is page-locked).
 #ifndef TLIBG_HOST_CHUNK_MB
@@ -1130,7 +1148,7 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
             cudaEventCreateWithFlags(&hc.done[i], cudaEventDisableTiming);
         }
     }
-    const size_t need_a = (size_t)(spc * panel * ea);
+    const size_t need_a = (size_t)(spc * panel * ea) + 32;   // + the 16-byte cover of a chunk
     const size_t need_b = (size_t)(cn.nq * et);
     const size_t need_c = (size_t)(cn.S * cn.P * et);
     auto grow = [&](void** p_, size_t* have, size_t need) -> int {
@@ -1168,18 +1186,25 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     // the host link (one pass, no staging copy; on GB300 such reads move
     // page-locked memory as fast as the copy engines do).  Every other plan (short
     // rows, whose lane groups issue one short run per row, and scalar loads) goes
-    // through the staged path below: copy-engine copies of chunks into device
-    // memory overlapped with the device kernels (measured over the symmetric
-    // sweep: rows of 16-25 elements 123-149 GB/s read in place, 190-202 staged,
-    // against the 211 GB/s link).  The bulk copies of the streamed, row-tile and
-    // TMA-staged column kernels are kept to device memory.
+    // through the staged path below: chunks copied into device memory by the SMs
+    // (512-byte runs per warp load again) overlapped with the device kernels
+    // (measured over the symmetric sweep: rows of 16-25 elements 123-149 GB/s read
+    // in place against the 211 GB/s link; copy-engine staging of the same chunks
+    // varied from 27 to 200 GB/s between runs).  The bulk copies of the streamed,
+    // row-tile and TMA-staged column kernels are kept to device memory.
     cudaPointerAttributes at{};
     const bool a_pinned = cudaPointerGetAttributes(&at, a) == cudaSuccess && at.type == cudaMemoryTypeHost &&
                           at.devicePointer != nullptr;
     cudaGetLastError();
     cudaPointerAttributes atc{};
+    // Page-locked C is written in place by the kernels only where that pays: column
+    // forms (each warp stores contiguous runs) with C at least 1/16 of A, whose copy
+    // after the kernels would cost time.  Row forms store one short run per row
+    // group, and such scattered stores over the host link measured from 27 to
+    // 200 GB/s depending on where the buffer sits; their C (at most 1/16 of A)
+    // goes to device memory and back in one copy.
     const bool c_pinned = cudaPointerGetAttributes(&atc, c) == cudaSuccess && atc.type == cudaMemoryTypeHost &&
-                          atc.devicePointer != nullptr;
+                          atc.devicePointer != nullptr && cn.P > 1 && cn.nq <= 16;   // C >= A / 16
     cudaGetLastError();
     bool direct = false;
     if (a_pinned) {
@@ -1235,19 +1260,36 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         // the copy into this slot must wait until the kernels that read it are done
         if (k >= 2) cudaStreamWaitEvent(hc.copy, hc.done[slot], 0);
         const char* src = static_cast<const char*>(a) + s0 * panel * ea;
-        if ((e = cudaMemcpyAsync(hc.abuf[slot], src, (size_t)(sn * panel * ea), cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess)
+        const size_t len = (size_t)(sn * panel * ea);
+        char* adev = static_cast<char*>(hc.abuf[slot]);
+        if (a_pinned) {
+            // page-locked A: the SMs copy the chunk's 16-byte-aligned cover (one 512-byte
+            // run per warp load, the kind of read that keeps the host link full), and the
+            // kernels read the chunk at its own offset in the cover
+            const char* hsrc = static_cast<const char*>(at.devicePointer) + s0 * panel * ea;
+            const uintptr_t lo = reinterpret_cast<uintptr_t>(hsrc) & ~uintptr_t(15);
+            const uintptr_t hi = (reinterpret_cast<uintptr_t>(hsrc) + len + 15) & ~uintptr_t(15);
+            const uint64_t n16 = (hi - lo) / 16;
+            const int grid = (int)std::min<uint64_t>((uint64_t)d.sms * 2, std::max<uint64_t>(1, n16 / 1024));
+            host_stage_kernel<<<grid, 256, 0, hc.copy>>>(reinterpret_cast<uint4*>(adev),
+                                                         reinterpret_cast<const uint4*>(lo), n16);
+            if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "copy of A");
+            ++launches;
+            adev += reinterpret_cast<uintptr_t>(hsrc) - lo;
+        } else if ((e = cudaMemcpyAsync(adev, src, len, cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess) {
             return cuda_fail(e, "copy of A");
+        }
         cudaEventRecord(hc.ev[slot], hc.copy);
         cudaStreamWaitEvent(hc.comp, hc.ev[slot], 0);
         Canon ck = cn;
         ck.S = sn;
         Plan pl;
-        if ((st = make_plan(dtype, ck, hc.abuf[slot], hc.bbuf, opt, d.sms, &pl))) return st;
+        if ((st = make_plan(dtype, ck, adev, hc.bbuf, opt, d.sms, &pl))) return st;
         void* part = nullptr;
         if ((st = get_scratch(hc.comp, partial_bytes(pl), &part))) return st;
         // page-locked C: each chunk's kernels store their part of C in place
         char* cdst = static_cast<char*>(c_pinned ? atc.devicePointer : hc.cbuf) + s0 * cn.P * et;
-        e = launch_plan(pl, hc.abuf[slot], hc.bbuf, cdst, part, hc.comp, &launches);
+        e = launch_plan(pl, adev, hc.bbuf, cdst, part, hc.comp, &launches);
         if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
         cudaEventRecord(hc.done[slot], hc.comp);
     }
