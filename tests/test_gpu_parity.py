@@ -471,9 +471,10 @@ REALIGN_SHAPES = [
 
 @pytest.mark.parametrize("na,pia,q", REALIGN_SHAPES)
 def test_realigned_column_kernel(engine, orc, torch_dev, na, pia, q):
-    """The column kernel with shuffle-realigned 16-byte loads: every warp-row
-    count and split, A at element offsets 0-3, fp32 (compensated and plain) and
-    fp64 (native and double-float)."""
+    """The column kernel with aligned 16-byte loads into shifted per-lane
+    accumulators: every warp-row count and split, A at element offsets 0-3 (every
+    row misalignment), fp32 (compensated and plain) and fp64 (native and
+    double-float)."""
     torch, dev = torch_dev
     rng = np.random.default_rng(sum(na) * 7 + q)
     P, nq, S = orc.canonical(na, pia, q)

@@ -7,11 +7,17 @@
 // falls back to scalar loads.  Here a warp owns a window of 32*V consecutive
 // outputs of one row of one slab and, for every row i, loads the 33 aligned
 // 16-byte vectors that cover the window: lane L the L-th, lane 31 also the
-// 33rd when the window is misaligned.  The lane's V elements are its own
-// vector shifted by the row's misalignment r (warp-uniform, 0..V-1) with the
-// start of its right neighbour's vector, fetched by one warp shuffle per
-// element.  Every load is a full 16-byte load and contains at least one
-// element of the window, so no access leaves A's allocation.  Windows that
+// 33rd when the window is misaligned.  Element v of lane L's vector belongs
+// to output V L + v - r of the window, r the row's misalignment (warp-uniform,
+// 0..V-1).  Instead of moving data between lanes every row, each lane keeps
+// 2V - 1 accumulators, for outputs V L - (V - 1) .. V L + V - 1, and adds each
+// element into the one its row's shift names (a warp-uniform switch on r, so
+// every index is a compile-time constant); after the last row, one warp
+// shuffle hands each lane's V - 1 low accumulators to its left neighbour,
+// whose outputs they are (lane 0's belong to the previous window, whose lane
+// 31 read the same elements from its 33rd vector).  Every load is a full
+// 16-byte load and contains at least one element of the window, so no access
+// leaves A's allocation.  Windows that
 // straddle two slabs or end past a row (the last window of each row) take
 // scalar loads.  Work items, the b stage, the warps stacked along q and the
 // split reduction are those of the column kernel.  Chosen only on request
@@ -21,20 +27,88 @@
 
 namespace tlibg {
 
-// o[v] = window element v of a lane: (c ++ n)[v + r] for r in 0..V-1, with
-// compile-time indices only (no local-memory arrays).
-template <typename T, int V>
-__device__ __forceinline__ void realign_vec(const T (&c)[V], const T (&n)[V], uint32_t r, T (&o)[V])
+// w[BASE + v] += av[v] * bb for v < NV (the fp64 mix alternates native and
+// emulated products over (u, v) as row_fma does).
+template <int V, bool PRE, int BASE, int NV, typename AccT, typename T>
+__device__ __forceinline__ void win_fma(AccT* w, const T (&av)[V], T bb, int u, const float2* bsp)
+{
+    if constexpr (std::is_same<AccT, AccDF>::value) {
+        DSplit bs;
+        if constexpr (PRE) {
+            const float2 t = *bsp;
+            bs.hi = t.x;
+            bs.lo = t.y;
+            bs.ok = true;
+        } else {
+            bs = split_double(bb);
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            if (f64_native<V>(u, v))
+                w[BASE + v].d = fma(av[v], bb, w[BASE + v].d);
+            else
+                w[BASE + v].add_split(split_double(av[v]), bs, av[v], bb);
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) w[BASE + v].fma_add(av[v], bb);
+    }
+}
+
+// One row of a lane: its vector (shift r) and, for lane 31, the 33rd vector.
+template <int V, bool PRE, typename AccT, typename T>
+__device__ __forceinline__ void win_row(AccT* w, const T (&cur)[V], const T (&ext)[V], uint32_t r, bool last,
+                                        T bb, int u, const float2* bsp)
+{
+    switch (r) {
+    case 0:
+        win_fma<V, PRE, V - 1, V>(w, cur, bb, u, bsp);
+        break;
+    case 1:
+        win_fma<V, PRE, V - 2, V>(w, cur, bb, u, bsp);
+        if (last) win_fma<V, PRE, 2 * V - 2, 1>(w, ext, bb, u, bsp);
+        break;
+    case 2:
+        if constexpr (V > 2) {
+            win_fma<V, PRE, V - 3, V>(w, cur, bb, u, bsp);
+            if (last) win_fma<V, PRE, 2 * V - 3, 2>(w, ext, bb, u, bsp);
+        }
+        break;
+    default:
+        if constexpr (V > 3) {
+            win_fma<V, PRE, V - 4, V>(w, cur, bb, u, bsp);
+            if (last) win_fma<V, PRE, 2 * V - 4, 3>(w, ext, bb, u, bsp);
+        }
+        break;
+    }
+}
+
+// After the last row: lane L's accumulators 0..V-2 are outputs of lane L - 1;
+// acc[v] = w[V - 1 + v] plus the right neighbour's w[v - 1] (none for lane 31).
+template <int V, typename T, bool KAHAN>
+__device__ __forceinline__ void win_collect(Acc<T, KAHAN> (&w)[2 * V - 1], Acc<T, KAHAN> (&acc)[V], uint32_t lane)
 {
 #pragma unroll
-    for (int v = 0; v < V; ++v) {
-        T x = c[v];
+    for (int v = 0; v < V; ++v) acc[v] = w[V - 1 + v];
 #pragma unroll
-        for (int k = 1; k < V; ++k) {
-            const T y = (v + k < V) ? c[v + k] : n[v + k - V];
-            x = (r == (uint32_t)k) ? y : x;
-        }
-        o[v] = x;
+    for (int v = 1; v < V; ++v) {
+        const T os = __shfl_down_sync(0xffffffffu, w[v - 1].s, 1);
+        const T oc = __shfl_down_sync(0xffffffffu, w[v - 1].c, 1);
+        if (lane < 31u) acc[v].merge(os, oc);
+    }
+}
+template <int V>
+__device__ __forceinline__ void win_collect(AccDF (&w)[2 * V - 1], AccDF (&acc)[V], uint32_t lane)
+{
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = w[V - 1 + v];
+#pragma unroll
+    for (int v = 1; v < V; ++v) {
+        AccDF o;
+        o.hi = __shfl_down_sync(0xffffffffu, w[v - 1].hi, 1);
+        o.lo = __shfl_down_sync(0xffffffffu, w[v - 1].lo, 1);
+        o.d = __shfl_down_sync(0xffffffffu, w[v - 1].d, 1);
+        if (lane < 31u) acc[v].absorb(o);
     }
 }
 
@@ -103,8 +177,13 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
             const uint64_t sw = idx_div(ow, k.pdiv);
             const uint64_t jw = ow - sw * P;
             if (jw + 32u * V <= P) {
-                // whole window inside row (sw, i, .): realigned vector loads
+                // whole window inside row (sw, i, .): aligned vector loads, shifted accumulators
                 const uint64_t base = sw * k.nq * P + jw;   // element index of A[sw, 0, jw]
+                typename AccSel<T, KAHAN>::type w[2 * V - 1];
+#pragma unroll
+                for (int v = 0; v < 2 * V - 1; ++v) w[v].init();
+                const bool last_lane = lane == 31u;
+                const bool pre = PRES && b_split_ok;
                 uint64_t i = ib + wi;
                 for (; i + (U - 1) * WI < ie; i += U * WI) {
                     T cur[U][V], ext[U][V] = {};
@@ -115,43 +194,32 @@ __global__ void __launch_bounds__(BLOCK) col_realign_kernel(KArgs k)
                         r[u] = (uint32_t)((amis + e) & (V - 1));
                         const T* vp = A + (int64_t)(e - r[u]);   // 16-byte aligned, in A's first block at worst
                         load_a<T, T, V>(vp + lane * V, cur[u]);
-                        if (lane == 31u && r[u] != 0u) load_a<T, T, V>(vp + 32u * V, ext[u]);
+                        if (last_lane && r[u] != 0u) load_a<T, T, V>(vp + 32u * V, ext[u]);
                     }
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
-                        T nxt[V], av[V];
-#pragma unroll
-                        for (int v = 0; v < V; ++v) {
-                            const T t = __shfl_down_sync(0xffffffffu, cur[u][v], 1);
-                            nxt[v] = lane == 31u ? ext[u][v] : t;
-                        }
-                        realign_vec<T, V>(cur[u], nxt, r[u], av);
-                        if (PRES && b_split_ok)
-                            row_fma<V, PRES>(acc, av, bs[i + u * WI], u, bsp + i + u * WI);
+                        if (pre)
+                            win_row<V, PRES>(w, cur[u], ext[u], r[u], last_lane, bs[i + u * WI], u,
+                                             bsp + i + u * WI);
                         else
-                            row_fma<V>(acc, av, bs[i + u * WI], u);
+                            win_row<V, false>(w, cur[u], ext[u], r[u], last_lane, bs[i + u * WI], u, nullptr);
                     }
-                    renorm_all<V>(acc);
+                    renorm_all<2 * V - 1>(w);
                 }
                 for (; i < ie; i += WI) {
-                    T cur[V], ext[V] = {}, nxt[V], av[V];
+                    T cur[V], ext[V] = {};
                     const uint64_t e = base + i * P;
                     const uint32_t rr = (uint32_t)((amis + e) & (V - 1));
                     const T* vp = A + (int64_t)(e - rr);
                     load_a<T, T, V>(vp + lane * V, cur);
-                    if (lane == 31u && rr != 0u) load_a<T, T, V>(vp + 32u * V, ext);
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        const T t = __shfl_down_sync(0xffffffffu, cur[v], 1);
-                        nxt[v] = lane == 31u ? ext[v] : t;
-                    }
-                    realign_vec<T, V>(cur, nxt, rr, av);
-                    if (PRES && b_split_ok)
-                        row_fma<V, PRES>(acc, av, bs[i], 0, bsp + i);
+                    if (last_lane && rr != 0u) load_a<T, T, V>(vp + 32u * V, ext);
+                    if (pre)
+                        win_row<V, PRES>(w, cur, ext, rr, last_lane, bs[i], 0, bsp + i);
                     else
-                        row_fma<V>(acc, av, bs[i]);
+                        win_row<V, false>(w, cur, ext, rr, last_lane, bs[i], 0, nullptr);
+                    renorm_all<2 * V - 1>(w);
                 }
-                renorm_all<V>(acc);
+                win_collect<V>(w, acc, lane);
             } else {
                 // window straddles two slabs or ends past the row: scalar loads
                 uint64_t ofs[V];
