@@ -368,6 +368,22 @@ def test_host_buffers(engine, orc, torch_dev):
         tc.zero_()
         engine.ttv_host(q, len(na), a, na, wa, pia, b, [nq], tc, nc, wc, pic)
         assert orc.rel_error(tc.numpy(), ref, absn) <= 1e-5
+        # pinned A one element off the 16-byte grid: staged chunks start mid-block
+        ta1 = torch.from_numpy(np.concatenate([np.zeros(1, np.float32), a])).pin_memory()[1:]
+        tc.zero_()
+        engine.ttv_host(q, len(na), ta1, na, wa, pia, tb, [nq], tc, nc, wc, pic)
+        assert orc.rel_error(tc.numpy(), ref, absn) <= 1e-5
+    # fp64, pinned, every path: in place (column tiles), staged (rows, odd prefix)
+    for na, pia, q in (([64, 300, 50], [1, 2, 3], 2), ([645, 3000], [1, 2], 1), ([25, 999, 7], [1, 2, 3], 2)):
+        wa, nc, wc, pic = meta(engine, na, pia, q)
+        a = rng.uniform(-1, 1, int(np.prod(na)))
+        b = rng.uniform(-1, 1, na[q - 1])
+        P, nq, S = orc.canonical(na, pia, q)
+        ref, absn = orc.truth(S, nq, P, a, b)
+        ta = torch.from_numpy(a).pin_memory()
+        tc = torch.zeros(int(np.prod(nc)), dtype=torch.float64).pin_memory()
+        engine.ttv_host(q, len(na), ta, na, wa, pia, torch.from_numpy(b).pin_memory(), [nq], tc, nc, wc, pic)
+        assert orc.rel_error(tc.numpy(), ref, absn) <= 1e-13
 
 
 def test_array_api_matches_einsum(engine, torch_dev):
