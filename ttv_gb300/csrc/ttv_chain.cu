@@ -40,6 +40,13 @@ constexpr int KRON_MAX_GROUPS = KRON_MAX_MODES;   // one weight vector per stage
 constexpr uint64_t CHAIN_MIN_ROW = TLIBG_CHAIN_MIN_ROW;           // row stage: rows at least this long
 constexpr uint64_t CHAIN_MIN_OUTPUTS = TLIBG_CHAIN_MIN_OUTPUTS;   // column stage: at least this many outputs
 constexpr uint64_t CHAIN_ONE_MODE_ROW = 64;           // first row stage: one mode if it is this long
+#ifndef TLIBG_CHAIN_SEG_KB
+#define TLIBG_CHAIN_SEG_KB 128
+#endif
+#ifndef TLIBG_CHAIN_SPLIT_CAP
+#define TLIBG_CHAIN_SPLIT_CAP 1
+#endif
+constexpr uint64_t CHAIN_SEG_BYTES = (uint64_t)TLIBG_CHAIN_SEG_KB << 10;   // later stages: bytes per split segment
 constexpr uint64_t CHAIN_SMALL = uint64_t(1) << 22;   // intermediates up to this many elements: one stage
 constexpr uint64_t CHAIN_LATE_OUTPUTS = 4096;         // larger ones: column stages keep this many outputs
 
@@ -256,6 +263,21 @@ extern "C" int tlibg_ttvs(int dtype, size_t q, size_t p, const void* a, const si
         const int dt = i == 0 ? dtype : tdt;
         const void* pw = sg.group < 0 ? sg.w : (const void*)probe;
         if (int s = internal_plan(dt, cv, i == 0 ? a : (const void*)probe, pw, nullptr, sms, &plans[i])) return s;
+        if (i > 0 && TLIBG_CHAIN_SPLIT_CAP && plans[i].kind == KIND_COL_THIN) {
+            // A later stage reads an intermediate that the stage before has just
+            // written (in L2 when small): the thin-prefix kernel's split, sized to fill
+            // the GPU twice over HBM-resident data, leaves thousands of partials to
+            // combine.  Segments of CHAIN_SEG_BYTES (and at most 256 rows, and at
+            // least half as many segments as SMs) are enough here (128^4 fp32, q = 3
+            // and 4: 2-3 us less per call; other kernels measured no gain).
+            const uint64_t want = std::max(std::max<uint64_t>(cv.P * cv.nq * cv.S * et / CHAIN_SEG_BYTES, cv.nq / 256),
+                                           std::max<uint64_t>((uint64_t)sms / 2, 1));
+            if (plans[i].split > 1 && (uint64_t)plans[i].split > want) {
+                tlibg_options o{TLIBG_ACC_COMPENSATED, -1, 0, 0, (int)want, 0};
+                Plan alt;
+                if (internal_plan(dt, cv, probe, pw, &o, sms, &alt) == 0) plans[i] = alt;
+            }
+        }
         part_bytes = std::max(part_bytes, partial_bytes(plans[i]));
         if (i + 1 < stages.size()) inter = std::max<size_t>(inter, (size_t)(sg.row ? sg.R : sg.L));
     }
