@@ -35,6 +35,13 @@ def test_candidates_row_form(T):
     # fp64 adds the double-float accumulation to every row candidate
     f64 = TU.candidates(T.F64, 1, 48, 1 << 20)
     assert {c.get("accumulate") for c in f64 if c.get("kind") == T.KIND_ROW} == {0, T.ACC_DOUBLE_FLOAT}
+    # rows that are not whole 16-byte vectors: row-shift candidates while b's shifted copies fit 48 KB
+    odd = TU.candidates(T.F32, 1, 645, 1 << 16)
+    assert sorted(c["group"] for c in odd if c.get("kind") == T.KIND_ROW_SHIFT) == [4, 8, 16, 32]
+    assert T.KIND_ROW_SHIFT not in {c.get("kind") for c in TU.candidates(T.F32, 1, 644, 1 << 16)}
+    assert T.KIND_ROW_SHIFT not in {c.get("kind") for c in TU.candidates(T.F32, 1, 4001, 1 << 16)}
+    assert T.KIND_ROW_SHIFT in {c.get("kind") for c in TU.candidates(T.F64, 1, 1533, 1 << 16)}
+    assert T.KIND_ROW_SHIFT not in {c.get("kind") for c in TU.candidates(T.F64, 1, 1535, 1 << 16)}
 
 
 def test_candidates_column_form(T):
