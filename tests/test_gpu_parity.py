@@ -342,10 +342,12 @@ def test_host_buffers(engine, orc, torch_dev):
     torch, dev = torch_dev
     rng = np.random.default_rng(4)
     # column forms with 16-byte loads read pinned A in place; row forms (rows of 25,
-    # rows of 645 over two staged chunks) and odd prefixes are staged
+    # rows of 645 over two staged chunks) and odd prefixes are staged; n_q <= 16
+    # column outputs go to pinned C in place (read in place and staged)
     for na, pia, q in (([200, 300, 50], [1, 2, 3], 2), ([128, 64, 300], [3, 1, 2], 3),
                        ([4096, 4096], [1, 2], 2), ([25, 4000], [1, 2], 1), ([7, 999, 5], [1, 2, 3], 2),
-                       ([645, 60000], [1, 2], 1)):
+                       ([645, 60000], [1, 2], 1), ([512, 4, 1024], [1, 2, 3], 2),
+                       ([645, 4, 301], [1, 2, 3], 2)):
         wa, nc, wc, pic = meta(engine, na, pia, q)
         a = rng.uniform(-1, 1, int(np.prod(na))).astype(np.float32)
         b = rng.uniform(-1, 1, na[q - 1]).astype(np.float32)
