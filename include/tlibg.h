@@ -131,6 +131,24 @@ int tlibg_ttv_ex(int dtype, size_t q, size_t p,
                  void* c, const size_t* nc, const size_t* wc, const size_t* pic,
                  const tlibg_options* opt, void* stream);
 
+/* Extension (no reference counterpart): the same contraction on DEVICE
+ * pointers with the natural meaning of every stride, for sliced, padded or
+ * transposed views -- A's element (i_1..i_p) at a[sum_r i_r wa[r]] (zero-based
+ * indices, strides in elements), b's element i at b[i wb], C's element
+ * (j_1..j_{p-1}) at c[sum_r j_r wc[r]], C's modes being A's modes without q.
+ * Same checks and messages as tlibg_ttv_f32 for shapes, layouts and monotonic
+ * strides; unlike the drop-in calls (whose dense-only rule follows the
+ * reference, which gives non-dense strides no single meaning) any stride
+ * vector is taken, as long as no two outputs share an element of C
+ * (TLIBG_ERR_UNSUPPORTED otherwise) and every offset stays below 2^62.
+ * dtype TLIBG_F32 or TLIBG_F64; compensated accumulation; asynchronous on
+ * `stream`.  Views that are dense take the dense kernels' speed only through
+ * tlibg_ttv_*. */
+int tlibg_ttv_strided(int dtype, size_t q, size_t p,
+                      const void* a, const size_t* na, const size_t* wa, const size_t* pia,
+                      const void* b, const size_t* nb, size_t wb,
+                      void* c, const size_t* nc, const size_t* wc, const size_t* pic, void* stream);
+
 /* Same call with HOST pointers a, b, c, as the reference takes them.  A in
  * page-locked memory whose plan reads 512-byte runs per warp load (column
  * tiles with 16-byte loads, rows taken by a whole warp) is read in place by

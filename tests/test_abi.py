@@ -395,3 +395,33 @@ def test_pointer_location_without_device(engine):
         has_gpu = False
     if not has_gpu:
         assert L.tlibg_pointer_location(ctypes.addressof(buf)) == 0
+
+
+def test_strided_extension_checks(engine):
+    """tlibg_ttv_strided's host checks (no device needed): the reference's messages
+    for shapes, layouts and monotonic strides; C strides that make two outputs
+    share an element, b's zero stride and bf16 storage refused."""
+    lib = engine.library()
+    def call(na, wa, pia, q, nc, wc, pic, wb=1, dtype=engine.F32):
+        keep = [engine._sizes(v) for v in (na, wa, pia, [na[q - 1]], nc, wc, pic)]
+        st = lib.tlibg_ttv_strided(dtype, q, len(na), 16, engine._p(keep[0]), engine._p(keep[1]),
+                                   engine._p(keep[2]), 32, engine._p(keep[3]), wb, 48, engine._p(keep[4]),
+                                   engine._p(keep[5]), engine._p(keep[6]), None)
+        return st, engine._last_error()
+    # C's strides overlap (both modes stride 1)
+    st, msg = call([4, 5, 6], [1, 4, 20], [1, 2, 3], 2, [4, 6], [1, 1], [1, 2])
+    assert st == engine.ERR_UNSUPPORTED and "share an element" in msg
+    # A's strides not monotonic along its layout: the reference's message
+    st, msg = call([4, 5, 6], [20, 4, 1], [1, 2, 3], 2, [4, 6], [1, 4], [1, 2])
+    assert st == engine.ERR_ARGUMENT and "stride" in msg
+    # b's stride zero
+    st, msg = call([4, 5, 6], [1, 4, 20], [1, 2, 3], 2, [4, 6], [1, 4], [1, 2], wb=0)
+    assert st == engine.ERR_ARGUMENT and "b's stride" in msg
+    # bf16-stored A is not taken here
+    st, msg = call([4, 5, 6], [1, 4, 20], [1, 2, 3], 2, [4, 6], [1, 4], [1, 2], dtype=engine.BF16A)
+    assert st == engine.ERR_UNSUPPORTED
+    # valid padded metadata passes the host checks (then needs a device)
+    st, msg = call([4, 5, 6], [1, 5, 40], [1, 2, 3], 2, [4, 6], [1, 7], [1, 2])
+    assert st in (engine.ERR_CUDA, engine.ERR_ARGUMENT, engine.OK)
+    if st == engine.ERR_ARGUMENT:
+        assert "device-accessible" in msg

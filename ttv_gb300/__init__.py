@@ -31,7 +31,7 @@ __all__ = [
     "plan_hint", "clear_plan_hint", "F32", "F64", "BF16A",
     "ACC_COMPENSATED", "ACC_PLAIN", "ACC_DOUBLE_FLOAT", "KIND_ROW", "KIND_COL", "KIND_STREAM",
     "KIND_COL_REALIGN", "KIND_COL_THIN", "KIND_ROW_TILE", "KIND_COL_BULK", "KIND_ROW_PANEL",
-    "KIND_ROW_SHIFT",
+    "KIND_ROW_SHIFT", "ttv_strided", "ttv_view",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -116,6 +116,9 @@ def library() -> C.CDLL:
         L.tlibg_ttvs.restype = C.c_int
         L.tlibg_ttvs.argtypes = [C.c_int, _sz, _sz, _vp, _psz, _psz, _psz, C.POINTER(_vp), _psz,
                                  _vp, _vp]
+        L.tlibg_ttv_strided.restype = C.c_int
+        L.tlibg_ttv_strided.argtypes = [C.c_int, _sz, _sz, _vp, _psz, _psz, _psz, _vp, _psz, _sz, _vp,
+                                        _psz, _psz, _psz, _vp]
         L.tlibg_device_alloc_count.restype = C.c_uint64
         L.tlibg_plan_hint.restype = C.c_int
         L.tlibg_plan_hint.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64,
@@ -237,6 +240,57 @@ def _check_buffers(dtype, q, p, keep, a, b, c):
         if have < need[name] * esz[name]:
             raise TTVError(f"tlibg: buffer {name} holds {have} bytes, its layout addresses "
                            f"{need[name] * esz[name]}")
+
+
+def ttv_strided(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, *, wb=1, dtype=None, stream=None):
+    """Extension: C = A x_q b on device memory with the natural meaning of every
+    stride (tlibg_ttv_strided): A's element (i_1..i_p) at a[sum i_r wa[r]], b's
+    i-th at b[i wb], C's at c[sum j_r wc[r]] (zero-based, in elements), for
+    sliced, padded or transposed views.  Same checks and messages as ``ttv``
+    for shapes, layouts and monotonic strides; refused when two outputs would
+    share an element of C.  Tensors must hold every element their strides
+    address."""
+    if dtype is None:
+        dtype = _dtype_of(a)
+    keep = [_sizes(v) for v in (na, wa, pia, nb, nc, wc, pic)]
+    need = {"a": _addressed(keep[0][:p], keep[1][:p]),
+            "b": (int(keep[3][0]) - 1) * int(wb) + 1 if len(keep[3]) and int(keep[3][0]) else 0,
+            "c": _addressed(keep[4][:p - 1], keep[5][:p - 1]) if p > 1 else 0}
+    for name, t in (("a", a), ("b", b), ("c", c)):
+        if hasattr(t, "untyped_storage"):
+            # elements from the tensor's first element to the end of its storage (views too)
+            have = t.untyped_storage().nbytes() // t.element_size() - t.storage_offset()
+            if have < need[name]:
+                raise TTVError(f"tlibg: buffer {name} holds {have} elements, its strides address "
+                               f"{need[name]}")
+    st = library().tlibg_ttv_strided(dtype, q, p, _ptr(a), _p(keep[0]), _p(keep[1]), _p(keep[2]),
+                                     _ptr(b), _p(keep[3]), int(wb), _ptr(c), _p(keep[4]), _p(keep[5]),
+                                     _p(keep[6]), _stream_handle(stream))
+    _raise(st)
+    return c
+
+
+def ttv_view(q, A, b, out=None, *, stream=None):
+    """``ttv_array`` for any strided torch view (slices, transposes, padding)
+    without a copy: A's own strides go to tlibg_ttv_strided; b may be strided
+    too.  Returns C (the modes of A without q, in order), contiguous, or fills
+    ``out`` (any strides that give every output its own element)."""
+    torch = _torch()
+    p = A.dim()
+    if not 1 <= q <= p:
+        raise TTVError("Error in tlib::tensor_times_vector: contraction mode should be greater zero or "
+                       "less than or equal to p.")
+    na = list(A.shape)
+    wa = list(A.stride())
+    shape_c = [n for m, n in enumerate(na) if m != q - 1]
+    if out is None:
+        out = torch.empty(shape_c, dtype=A.dtype, device=A.device)
+    wc = list(out.stride())
+    # layouts that pass the reference's monotonic-stride check: modes by increasing stride
+    pia = [m + 1 for m in sorted(range(p), key=lambda m: (wa[m], m))]
+    pic = [m + 1 for m in sorted(range(p - 1), key=lambda m: (wc[m], m))] or [1]
+    return ttv_strided(q, p, A, na, wa, pia, b, [int(b.shape[0])], out, shape_c or [1], wc or [1], pic,
+                       wb=int(b.stride(0)), stream=stream)
 
 
 def ttv_host(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic, *, dtype=None, **opts):

@@ -4,6 +4,8 @@
 #include "../../include/tlibg.h"
 #include "ttv_internal.h"
 #include "ttv_kernels.cuh"
+#include "ttv_device.cuh"
+#include "ttv_general.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -1068,6 +1070,94 @@ int tlibg_plan(int dtype, size_t q, size_t p, const size_t* na, const size_t* pi
     out->grid = pl.grid;
     out->block = pl.kind == KIND_STREAM ? STREAM_CONSUMERS + 32
                  : (pl.kind == KIND_ROW_TILE ? ROWT_THREADS : (pl.kind == KIND_COL_BULK ? CB_THREADS : BLOCK));
+    return ok();
+}
+
+// ---------------------------------------------------------------------------
+// general strides (extension; the drop-in calls keep the dense-only rule)
+// ---------------------------------------------------------------------------
+int tlibg_ttv_strided(int dtype, size_t q, size_t p, const void* a, const size_t* na, const size_t* wa,
+                      const size_t* pia, const void* b, const size_t* nb, size_t wb, void* c, const size_t* nc,
+                      const size_t* wc, const size_t* pic, void* stream)
+{
+    NvtxRange nvtx("tlibg_ttv_strided");
+    if (dtype != F32 && dtype != F64)
+        return fail(dtype == BF16A ? TLIBG_ERR_UNSUPPORTED : TLIBG_ERR_ARGUMENT,
+                    dtype == BF16A ? "tlibg_ttv_strided: fp32 and fp64 only" : "tlibg: unknown element type");
+    // the reference's checks and messages (shape, layout, monotonic strides, C's metadata)
+    const int code = check_call(q, p, a, na, wa, pia, b, nb, c, nc, wc, pic);
+    if (code) return fail(TLIBG_ERR_ARGUMENT, MSG[code]);
+    if (p - 1 > (size_t)GS_MAX_MODES) return fail(TLIBG_ERR_UNSUPPORTED, "tlibg_ttv_strided: at most 17 modes");
+    if (wb == 0) return fail(TLIBG_ERR_ARGUMENT, "tlibg_ttv_strided: b's stride must be at least 1");
+    // natural meaning: every output its own element of C (no two outputs share an
+    // address), every offset within 2^62 elements
+    {
+        std::vector<std::pair<size_t, size_t>> sw;   // (stride, extent) of C's modes with extent > 1
+        for (size_t r = 0; r + 1 < p; ++r)
+            if (nc[r] > 1) sw.push_back({wc[r], nc[r]});
+        std::sort(sw.begin(), sw.end());
+        uint64_t span = 1;
+        for (auto& e : sw) {
+            if (e.first < span)
+                return fail(TLIBG_ERR_UNSUPPORTED, "tlibg_ttv_strided: C's strides make two outputs share an "
+                                                   "element");
+            uint64_t t;
+            if (mul_overflows(e.first, e.second, &t)) return fail(TLIBG_ERR_UNSUPPORTED, "tlibg_ttv_strided: "
+                                                                                         "offsets exceed 2^62");
+            span = t;
+        }
+        uint64_t amax = 0;
+        for (size_t r = 0; r < p; ++r) {
+            uint64_t t;
+            if (mul_overflows(na[r] - 1, wa[r], &t) || (amax += t) > (uint64_t(1) << 62))
+                return fail(TLIBG_ERR_UNSUPPORTED, "tlibg_ttv_strided: offsets exceed 2^62");
+        }
+        uint64_t t;
+        if (mul_overflows(na[q - 1] - 1, wb, &t)) return fail(TLIBG_ERR_UNSUPPORTED, "tlibg_ttv_strided: "
+                                                                                     "offsets exceed 2^62");
+    }
+    if (int st = check_elem_align(dtype, a, b, c)) return st;
+    if (!dev_info().ok) return fail(TLIBG_ERR_CUDA, "tlibg: no usable CUDA device");
+    if (int st = check_device_pointers(a, b, c)) return st;
+
+    // modes other than q, A-stride order; C's mode r (0-based) is A's mode r or r + 1
+    GSArgs k{};
+    std::vector<std::tuple<size_t, size_t, size_t>> modes;   // (wa, extent, wc)
+    for (size_t m = 0; m < p; ++m) {
+        if (m == q - 1) continue;
+        const size_t cm = m < q - 1 ? m : m - 1;
+        if (na[m] > 1) modes.emplace_back(wa[m], na[m], wc[cm]);
+    }
+    std::sort(modes.begin(), modes.end());
+    k.nm = (int)modes.size();
+    k.outputs = 1;
+    for (int r = 0; r < k.nm; ++r) {
+        k.wa[r] = std::get<0>(modes[r]);
+        k.ext[r] = std::get<1>(modes[r]);
+        k.wc[r] = std::get<2>(modes[r]);
+        k.outputs *= k.ext[r];
+    }
+    k.a = a;
+    k.b = b;
+    k.c = c;
+    k.nq = na[q - 1];
+    k.waq = na[q - 1] > 1 ? wa[q - 1] : 0;
+    k.wb = wb;
+    const bool row = k.nm == 0 || (k.nq > 1 && k.waq <= k.wa[0]);
+    const int sms = dev_info().sms;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint64_t threads = row ? k.outputs * 32 : k.outputs;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (threads + 255) / 256));
+    if (dtype == F64) {
+        if (row) gs_row_kernel<double><<<grid, 256, 0, st>>>(k);
+        else gs_col_kernel<double><<<grid, 256, 0, st>>>(k);
+    } else {
+        if (row) gs_row_kernel<float><<<grid, 256, 0, st>>>(k);
+        else gs_col_kernel<float><<<grid, 256, 0, st>>>(k);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    g_launches += 1;
     return ok();
 }
 

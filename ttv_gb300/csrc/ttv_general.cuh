@@ -1,0 +1,108 @@
+// General-stride TTV (included by ttv_api.cu): tlibg_ttv_strided, an extension
+// beside the drop-in calls with the natural meaning of every stride -- A's
+// element (i_1..i_p) at a[sum_r i_r wa[r]], b's element i at b[i wb], C's
+// element (j_1..j_{p-1}) at c[sum_r j_r wc[r]] -- for views (sliced, padded,
+// transposed) that the dense kernels do not take.
+//
+// The outputs are numbered in a mixed radix over the modes other than q,
+// sorted by A stride (fastest first), so consecutive outputs sit next to each
+// other in A where the views allow it.
+//   column form (q is not A's fastest mode): one output per thread; the
+//     threads of a warp read neighbouring elements of each of the n_q rows,
+//     eight rows in flight per thread;
+//   row form (q is A's fastest mode): one warp per output, the lanes stride
+//     over the n_q elements (one coalesced run per load when wa[q] == 1), a
+//     warp shuffle tree sums the lanes in fixed order.
+// Compensated accumulation (Kahan) in the element type.
+#pragma once
+
+namespace tlibg {
+
+constexpr int GS_MAX_MODES = 16;   // modes other than q
+
+struct GSArgs {
+    const void* a;
+    const void* b;
+    void* c;
+    uint64_t ext[GS_MAX_MODES];   // extents of the modes other than q, A-stride order
+    uint64_t wa[GS_MAX_MODES];
+    uint64_t wc[GS_MAX_MODES];
+    int nm;
+    uint64_t outputs;             // product of ext
+    uint64_t nq, waq, wb;
+};
+
+__device__ __forceinline__ void gs_offsets(const GSArgs& k, uint64_t o, uint64_t& ao, uint64_t& co)
+{
+    ao = 0;
+    co = 0;
+    for (int m = 0; m < k.nm; ++m) {
+        const uint64_t e = k.ext[m];
+        const uint64_t q = o / e;
+        const uint64_t d = o - q * e;
+        ao += d * k.wa[m];
+        co += d * k.wc[m];
+        o = q;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) gs_col_kernel(GSArgs k)
+{
+    pdl_prologue();
+    const T* __restrict__ A = static_cast<const T*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    constexpr int U = 8;
+    for (uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < k.outputs;
+         o += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t ao, co;
+        gs_offsets(k, o, ao, co);
+        Acc<T, true> acc;
+        acc.init();
+        uint64_t i = 0;
+        for (; i + U <= k.nq; i += U) {
+            T av[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) av[u] = A[ao + (i + u) * k.waq];
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc.fma_add(av[u], __ldg(B + (i + u) * k.wb));
+        }
+        for (; i < k.nq; ++i) acc.fma_add(A[ao + i * k.waq], __ldg(B + i * k.wb));
+        static_cast<T*>(k.c)[co] = acc.value();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) gs_row_kernel(GSArgs k)
+{
+    pdl_prologue();
+    const T* __restrict__ A = static_cast<const T*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    constexpr int U = 4;
+    for (uint64_t o = warp; o < k.outputs; o += nwarps) {
+        uint64_t ao, co;
+        gs_offsets(k, o, ao, co);
+        Acc<T, true> acc;
+        acc.init();
+        uint64_t i = lane;
+        for (; i + 32 * (U - 1) < k.nq; i += 32 * U) {
+            T av[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) av[u] = A[ao + (i + 32 * u) * k.waq];
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc.fma_add(av[u], __ldg(B + (i + 32 * u) * k.wb));
+        }
+        for (; i < k.nq; i += 32) acc.fma_add(A[ao + i * k.waq], __ldg(B + i * k.wb));
+        for (uint32_t off = 16; off > 0; off >>= 1) {
+            const T os = __shfl_xor_sync(0xffffffffu, acc.s, off);
+            const T oc = __shfl_xor_sync(0xffffffffu, acc.c, off);
+            acc.merge(os, oc);
+        }
+        if (lane == 0) static_cast<T*>(k.c)[co] = acc.value();
+    }
+}
+
+}  // namespace tlibg
