@@ -1144,9 +1144,10 @@ int tlibg_ttv_strided(int dtype, size_t q, size_t p, const void* a, const size_t
     k.waq = na[q - 1] > 1 ? wa[q - 1] : 0;
     k.wb = wb;
     const bool row = k.nm == 0 || (k.nq > 1 && k.waq <= k.wa[0]);
+    k.group = (uint32_t)std::max(1, std::min(32, pow2_floor(std::max<uint64_t>(1, k.nq / 16))));
     const int sms = dev_info().sms;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const uint64_t threads = row ? k.outputs * 32 : k.outputs;
+    const uint64_t threads = row ? k.outputs * k.group : k.outputs;
     const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 8, (threads + 255) / 256));
     if (dtype == F64) {
         if (row) gs_row_kernel<double><<<grid, 256, 0, st>>>(k);

@@ -10,9 +10,10 @@
 //   column form (q is not A's fastest mode): one output per thread; the
 //     threads of a warp read neighbouring elements of each of the n_q rows,
 //     eight rows in flight per thread;
-//   row form (q is A's fastest mode): one warp per output, the lanes stride
-//     over the n_q elements (one coalesced run per load when wa[q] == 1), a
-//     warp shuffle tree sums the lanes in fixed order.
+//   row form (q is A's fastest mode): a group of G lanes per output (G from
+//     n_q: about 16 elements per lane, 1..32), the lanes stride over the n_q
+//     elements (one coalesced run per load when wa[q] == 1), a shuffle tree
+//     sums the group's lanes in fixed order.
 // Compensated accumulation (Kahan) in the element type.
 #pragma once
 
@@ -30,6 +31,7 @@ struct GSArgs {
     int nm;
     uint64_t outputs;             // product of ext
     uint64_t nq, waq, wb;
+    uint32_t group;               // row form: lanes per output
 };
 
 __device__ __forceinline__ void gs_offsets(const GSArgs& k, uint64_t o, uint64_t& ao, uint64_t& co)
@@ -78,30 +80,39 @@ __global__ void __launch_bounds__(256) gs_row_kernel(GSArgs k)
     pdl_prologue();
     const T* __restrict__ A = static_cast<const T*>(k.a);
     const T* __restrict__ B = static_cast<const T*>(k.b);
+    const uint32_t G = k.group;                 // lanes per output (power of two)
     const uint32_t lane = threadIdx.x & 31u;
-    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t gl = lane & (G - 1u);
+    const uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const uint64_t ngroups = ((uint64_t)gridDim.x * blockDim.x) / G;
     constexpr int U = 4;
-    for (uint64_t o = warp; o < k.outputs; o += nwarps) {
-        uint64_t ao, co;
-        gs_offsets(k, o, ao, co);
+    // every lane of a warp runs the same number of rounds (the shuffles below)
+    const uint64_t rounds = (k.outputs + ngroups - 1) / ngroups;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        const uint64_t o = gid + r * ngroups;
+        const bool valid = o < k.outputs;
         Acc<T, true> acc;
         acc.init();
-        uint64_t i = lane;
-        for (; i + 32 * (U - 1) < k.nq; i += 32 * U) {
-            T av[U];
+        uint64_t co = 0;
+        if (valid) {
+            uint64_t ao;
+            gs_offsets(k, o, ao, co);
+            uint64_t i = gl;
+            for (; i + (uint64_t)G * (U - 1) < k.nq; i += (uint64_t)G * U) {
+                T av[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) av[u] = A[ao + (i + 32 * u) * k.waq];
+                for (int u = 0; u < U; ++u) av[u] = A[ao + (i + (uint64_t)G * u) * k.waq];
 #pragma unroll
-            for (int u = 0; u < U; ++u) acc.fma_add(av[u], __ldg(B + (i + 32 * u) * k.wb));
+                for (int u = 0; u < U; ++u) acc.fma_add(av[u], __ldg(B + (i + (uint64_t)G * u) * k.wb));
+            }
+            for (; i < k.nq; i += G) acc.fma_add(A[ao + i * k.waq], __ldg(B + i * k.wb));
         }
-        for (; i < k.nq; i += 32) acc.fma_add(A[ao + i * k.waq], __ldg(B + i * k.wb));
-        for (uint32_t off = 16; off > 0; off >>= 1) {
+        for (uint32_t off = G >> 1; off > 0; off >>= 1) {
             const T os = __shfl_xor_sync(0xffffffffu, acc.s, off);
             const T oc = __shfl_xor_sync(0xffffffffu, acc.c, off);
             acc.merge(os, oc);
         }
-        if (lane == 0) static_cast<T*>(k.c)[co] = acc.value();
+        if (valid && gl == 0) static_cast<T*>(k.c)[co] = acc.value();
     }
 }
 
