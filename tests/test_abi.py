@@ -147,6 +147,11 @@ def test_planner_kernel_family(engine):
     assert engine.plan(1, [645, 99], [1, 2])["kind"] == engine.KIND_ROW
     assert engine.plan(3, [645, 645, 645], [3, 2, 1], vec=1)["kind"] == engine.KIND_ROW
     assert engine.plan(1, [4001, 9999], [1, 2])["kind"] == engine.KIND_ROW   # copies of b over 48 KB
+    # rows that fill few rounds of lane groups are split in two (16384 rows of 16384 over the
+    # lane groups of 152 SMs without a device); rows that fill many rounds are not
+    assert engine.plan(1, [16384, 16384], [1, 2])["split"] == 2
+    assert engine.plan(1, [16384, 16384], [1, 2], dtype=engine.F64)["split"] == 2
+    assert engine.plan(1, [4096, 65536], [1, 2])["split"] == 1
     # unaligned fp32 rows under 64 elements: the row-tile kernel; aligned ones the row kernel
     assert engine.plan(3, [25, 25, 25], [3, 2, 1])["kind"] == engine.KIND_ROW_TILE
     assert engine.plan(1, [63, 99], [1, 2])["kind"] == engine.KIND_ROW_TILE
