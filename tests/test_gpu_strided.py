@@ -136,3 +136,24 @@ def test_torch_views(engine, cuda):
             torch.cuda.synchronize()
             assert c.shape == ref.shape
             assert ((c - ref).abs() / absn.clamp_min(1e-300)).max().item() <= 1e-13
+
+
+def test_vector_forms(engine, cuda):
+    """Views on the 16-byte grid take the 16-byte forms: padded rows contracted
+    along the row (row form) and across rows (column form, which takes them when
+    the outputs fill the GPU: the 4 x 800 x 800 view), fp32 and fp64, with rows
+    long and short, against torch in fp64."""
+    import torch
+    g = torch.Generator(device=cuda)
+    g.manual_seed(11)
+    for dt, V in ((torch.float32, 4), (torch.float64, 2)):
+        for shape, pad in (((48, 30, 64), 4), ((7, 5, 1000), 8), ((3, 200, 8), 2 * V), ((4, 800, 800), 8)):
+            base = torch.rand(shape[0], shape[1], shape[2] + pad, generator=g, device=cuda, dtype=dt) * 2 - 1
+            A = base[:, :, :shape[2]]
+            for q in (1, 2, 3):
+                b = torch.rand(A.shape[q - 1], generator=g, device=cuda, dtype=dt) * 2 - 1
+                c = engine.ttv_view(q, A, b)
+                ref = torch.tensordot(A.double(), b.double(), dims=([q - 1], [0]))
+                absn = torch.tensordot(A.double().abs(), b.double().abs(), dims=([q - 1], [0]))
+                bar = 1e-5 if dt == torch.float32 else 1e-13
+                assert ((c.double() - ref).abs() / absn.clamp_min(1e-300)).max().item() <= bar, (dt, shape, q)

@@ -14,7 +14,8 @@
 //     n_q: about 16 elements per lane, 1..32), the lanes stride over the n_q
 //     elements (one coalesced run per load when wa[q] == 1), a shuffle tree
 //     sums the group's lanes in fixed order.
-// Compensated accumulation (Kahan) in the element type.
+// Where the view puts rows or outputs on the 16-byte grid, the same two forms
+// with 16-byte loads.  Compensated accumulation (Kahan) in the element type.
 #pragma once
 
 namespace tlibg {
@@ -113,6 +114,117 @@ __global__ void __launch_bounds__(256) gs_row_kernel(GSArgs k)
             acc.merge(os, oc);
         }
         if (valid && gl == 0) static_cast<T*>(k.c)[co] = acc.value();
+    }
+}
+
+// 16 bytes of b through the read-only path (16-byte aligned).
+template <typename T, int V>
+__device__ __forceinline__ void gs_load_b(const T* p, T (&out)[V])
+{
+    const uint4 r = __ldg(reinterpret_cast<const uint4*>(p));
+    memcpy(out, &r, 16);
+}
+
+// 16-byte forms, where the views allow aligned vector loads (set by the host):
+// row form with contiguous rows (wa[q] == 1, b contiguous, n_q and every row
+// start on the 16-byte grid); column form with V consecutive outputs of A's
+// fastest other mode (its stride 1, its extent and every other stride
+// multiples of V, A on the 16-byte grid).
+template <typename T>
+__global__ void __launch_bounds__(256) gs_row_vec_kernel(GSArgs k)
+{
+    pdl_prologue();
+    constexpr int V = 16 / (int)sizeof(T);
+    constexpr int U = 4;
+    const T* __restrict__ A = static_cast<const T*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    const uint32_t G = k.group;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gl = lane & (G - 1u);
+    const uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const uint64_t ngroups = ((uint64_t)gridDim.x * blockDim.x) / G;
+    const uint64_t nv = k.nq / V;
+    const uint64_t rounds = (k.outputs + ngroups - 1) / ngroups;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        const uint64_t o = gid + r * ngroups;
+        const bool valid = o < k.outputs;
+        Acc<T, true> acc[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].init();
+        uint64_t co = 0;
+        if (valid) {
+            uint64_t ao;
+            gs_offsets(k, o, ao, co);
+            const T* ap = A + ao;
+            uint64_t kv = gl;
+            for (; kv + (uint64_t)G * (U - 1) < nv; kv += (uint64_t)G * U) {
+                T av[U][V], bv[U][V];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    load_a<T, T, V>(ap + (kv + (uint64_t)G * u) * V, av[u]);
+                    gs_load_b<T, V>(B + (kv + (uint64_t)G * u) * V, bv[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bv[u][v]);
+            }
+            for (; kv < nv; kv += G) {
+                T av[V], bv[V];
+                load_a<T, T, V>(ap + kv * V, av);
+                gs_load_b<T, V>(B + kv * V, bv);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bv[v]);
+            }
+        }
+        fold_vec<V>(acc);
+        for (uint32_t off = G >> 1; off > 0; off >>= 1) {
+            const T os = __shfl_xor_sync(0xffffffffu, acc[0].s, off);
+            const T oc = __shfl_xor_sync(0xffffffffu, acc[0].c, off);
+            acc[0].merge(os, oc);
+        }
+        if (valid && gl == 0) static_cast<T*>(k.c)[co] = acc[0].value();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) gs_col_vec_kernel(GSArgs k)
+{
+    pdl_prologue();
+    constexpr int V = 16 / (int)sizeof(T);
+    constexpr int U = 4;
+    const T* __restrict__ A = static_cast<const T*>(k.a);
+    const T* __restrict__ B = static_cast<const T*>(k.b);
+    const uint64_t groups = k.outputs / V;
+    for (uint64_t og = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; og < groups;
+         og += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t ao, co;
+        gs_offsets(k, og * V, ao, co);
+        Acc<T, true> acc[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[v].init();
+        uint64_t i = 0;
+        for (; i + U <= k.nq; i += U) {
+            T av[U][V];
+#pragma unroll
+            for (int u = 0; u < U; ++u) load_a<T, T, V>(A + ao + (i + u) * k.waq, av[u]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const T bb = __ldg(B + (i + u) * k.wb);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[u][v], bb);
+            }
+        }
+        for (; i < k.nq; ++i) {
+            T av[V];
+            load_a<T, T, V>(A + ao + i * k.waq, av);
+            const T bb = __ldg(B + i * k.wb);
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bb);
+        }
+        T* C = static_cast<T*>(k.c);
+#pragma unroll
+        for (int v = 0; v < V; ++v) C[co + (uint64_t)v * k.wc[0]] = acc[v].value();
     }
 }
 
