@@ -1272,20 +1272,6 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         *have = need;
         return TLIBG_OK;
     };
-    if (hc.abytes < need_a) {
-        cudaStreamSynchronize(hc.comp);
-        for (int i = 0; i < 2; ++i) {
-            if (hc.abuf[i]) cudaFree(hc.abuf[i]);
-            hc.abuf[i] = nullptr;
-        }
-        hc.abytes = 0;
-        for (int i = 0; i < 2; ++i)
-            if (device_malloc(&hc.abuf[i], need_a) != cudaSuccess) {
-                cudaGetLastError();
-                return fail(TLIBG_ERR_NOMEM, "tlibg: cannot allocate device staging buffers");
-            }
-        hc.abytes = need_a;
-    }
     if ((st = grow(&hc.bbuf, &hc.bbytes, need_b))) return st;
     if ((st = grow(&hc.cbuf, &hc.cbytes, need_c))) return st;
 
@@ -1309,8 +1295,8 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
     // forms (each warp stores contiguous runs) with C at least 1/16 of A, whose copy
     // after the kernels would cost time.  Row forms store one short run per row
     // group, and such scattered stores over the host link measured from 27 to
-    // 200 GB/s depending on where the buffer sits; their C (at most 1/16 of A)
-    // goes to device memory and back in one copy.
+    // 200 GB/s depending on where the buffer sits; their C, like the smaller C of
+    // longer contractions, goes to device memory and back in one copy.
     const bool c_pinned = cudaPointerGetAttributes(&atc, c) == cudaSuccess && atc.type == cudaMemoryTypeHost &&
                           atc.devicePointer != nullptr && cn.P > 1 && cn.nq <= 16;   // C >= A / 16
     cudaGetLastError();
@@ -1358,6 +1344,22 @@ int tlibg_ttv_host(int dtype, size_t q, size_t p, const void* a, const size_t* n
         return ok();
     }
 
+    // staged path: two chunk buffers in device memory (only this path needs them)
+    if (hc.abytes < need_a) {
+        cudaStreamSynchronize(hc.comp);
+        cudaStreamSynchronize(hc.copy);
+        for (int i = 0; i < 2; ++i) {
+            if (hc.abuf[i]) cudaFree(hc.abuf[i]);
+            hc.abuf[i] = nullptr;
+        }
+        hc.abytes = 0;
+        for (int i = 0; i < 2; ++i)
+            if (device_malloc(&hc.abuf[i], need_a) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(TLIBG_ERR_NOMEM, "tlibg: cannot allocate device staging buffers");
+            }
+        hc.abytes = need_a;
+    }
     if ((e = cudaMemcpyAsync(hc.bbuf, b, need_b, cudaMemcpyHostToDevice, hc.copy)) != cudaSuccess)
         return cuda_fail(e, "copy of b");
     uint64_t launches = 0;
