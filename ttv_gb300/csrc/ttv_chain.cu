@@ -5,18 +5,20 @@
 // next.  Here the chain reads A once, in a short sequence of stages planned
 // on the host.  Walk the modes of A in layout order (fastest first); q sits
 // at position k.  A stage contracts a contiguous group of modes at one end
-// of the layout with the Kronecker product of their vectors (computed once,
-// in fp64 and rounded to the element type):
-//   * row stage (k > 0): the fastest modes, as few as make rows of at least
-//     CHAIN_MIN_ROW elements (or all modes before q): A is rows of that
-//     length, each dotted with the weights -- the engine's row-form kernels on
-//     many moderate rows instead of a few very long ones;
-//   * column stage (q fastest): the slowest modes, as many as leave at least
-//     CHAIN_MIN_OUTPUTS outputs (at least one mode): a column GEMV over them
-//     -- the engine's column-form kernels with plenty of outputs.
-// The first stage reads A (about all the traffic); each later one reads the
-// previous, much smaller, intermediate.  All weights come from one kernel
-// launch, intermediates live in the stream's cached scratch: no host
+// of the layout:
+//   * first stage, row form (k > 0): the fastest mode alone when it is long
+//     and its rows are whole 16-byte vectors, else the fastest modes as few as
+//     make rows of at least CHAIN_MIN_ROW elements (or all modes before q);
+//   * first stage, column form (q fastest): the slowest modes, as many as
+//     leave at least CHAIN_MIN_OUTPUTS outputs (at least one mode);
+//   * later stages: all remaining modes on one side of q (a column stage over
+//     a large intermediate keeps CHAIN_LATE_OUTPUTS outputs).
+// Each stage runs on the engine's own planner and kernels.  A stage over one
+// mode reads that mode's vector in place; stages over several modes read the
+// Kronecker product of their vectors (computed in fp64, rounded once to the
+// element type), all built by one kernel launch.  The first stage reads A
+// (about all the traffic); each later one reads the previous, much smaller,
+// intermediate.  Intermediates live in the stream's cached scratch: no host
 // synchronisation and no allocation after the first call on a stream.  Each
 // launch after the first is a programmatic dependent of the one before, so
 // its launch overlaps its predecessor's tail.
