@@ -377,6 +377,32 @@ __device__ __forceinline__ void row_load(const float* p, float (&out)[V])
         load_a<float, float, V>(p, out);
 }
 
+// V elements of b in one load (row problems: b is aligned to V floats and
+// segments start on multiples of V).
+#ifndef TLIBG_BATCH_BVEC
+#define TLIBG_BATCH_BVEC 1
+#endif
+template <int V>
+__device__ __forceinline__ void b_load(const float* p, float (&out)[V])
+{
+    if constexpr (!TLIBG_BATCH_BVEC) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) out[v] = __ldg(p + v);
+    } else if constexpr (V == 4) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+        out[0] = t.x;
+        out[1] = t.y;
+        out[2] = t.z;
+        out[3] = t.w;
+    } else if constexpr (V == 2) {
+        const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+        out[0] = t.x;
+        out[1] = t.y;
+    } else {
+        out[0] = __ldg(p);
+    }
+}
+
 template <int V, bool KAHAN>
 __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPair* __restrict__ part)
 {
@@ -410,8 +436,12 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
 #pragma unroll
                     for (int v = 0; v < V; ++v) a1[t][v] = 0.f;
                 }
+                if (in) {
+                    b_load<V>(P.b + kv * V, bv[t]);
+                } else {
 #pragma unroll
-                for (int v = 0; v < V; ++v) bv[t][v] = in ? __ldg(P.b + kv * V + v) : 0.f;
+                    for (int v = 0; v < V; ++v) bv[t][v] = 0.f;
+                }
             }
             Acc<float, KAHAN> c0, c1;
             c0.init();
@@ -459,8 +489,7 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     row_load<V>(ap + (kv + u * G) * V, av[u]);
-#pragma unroll
-                    for (int v = 0; v < V; ++v) bv[u][v] = __ldg(bp + (kv + u * G) * V + v);
+                    b_load<V>(bp + (kv + u * G) * V, bv[u]);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u)
@@ -469,10 +498,11 @@ __device__ __forceinline__ void row_unit(const BProb& P, uint64_t lu, int G, BPa
             }
 #pragma unroll 4
             for (; kv < nv; kv += G) {
-                float av[V];
+                float av[V], bv[V];
                 row_load<V>(ap + kv * V, av);
+                b_load<V>(bp + kv * V, bv);
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], __ldg(bp + kv * V + v));
+                for (int v = 0; v < V; ++v) acc[v].fma_add(av[v], bv[v]);
             }
             for (uint64_t e = nv * V + gl; e < n; e += G) acc[0].fma_add(__ldcs(ap + e), __ldg(bp + e));
         }
