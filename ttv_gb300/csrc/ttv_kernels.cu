@@ -440,6 +440,9 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) row_kernel(KArgs k
 // owns V consecutive outputs in each of two tiles TO apart and loads every row
 // of both before any product: 2 n_q vector loads in flight per thread.  b's
 // n_q values (and for fp64 their split) live in registers.
+#ifndef TLIBG_CS_VSTORE
+#define TLIBG_CS_VSTORE 1
+#endif
 template <typename TA, typename T, int V, bool KAHAN>
 __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_short_kernel(KArgs k)
 {
@@ -505,10 +508,29 @@ __global__ void __launch_bounds__(BLOCK, (min_ctas<TA, V>())) col_short_kernel(K
             renorm_all<V>(acc);
             if (valid[h]) {
                 const uint64_t o = (2 * pair + h) * TO + (uint64_t)threadIdx.x * V;
+                T vals[V];
 #pragma unroll
                 for (int v = 0; v < V; ++v) {
                     acc[v].fold();
-                    static_cast<T*>(k.out)[o + v] = acc[v].value();
+                    vals[v] = acc[v].value();
+                }
+                T* out = static_cast<T*>(k.out) + o;
+                // C is a quarter of A or more here: one vector store per thread where aligned
+                constexpr int VB = V * (int)sizeof(T);
+                bool vec_done = false;
+                if constexpr (VB <= 16 && TLIBG_CS_VSTORE) {
+                    if (o + V <= outputs && (reinterpret_cast<uintptr_t>(out) % VB) == 0) {
+                        typedef typename RawVec<VB>::type R;
+                        R r;
+                        memcpy(&r, vals, sizeof(R));
+                        *reinterpret_cast<R*>(out) = r;
+                        vec_done = true;
+                    }
+                }
+                if (!vec_done) {
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        if (o + v < outputs) out[v] = vals[v];
                 }
             }
         }
